@@ -1,0 +1,730 @@
+/*
+ * ORACLE / TEST INFRASTRUCTURE ONLY (see oracle/README.md).  Only tests/,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg load this; the
+ * product never does.
+ *
+ * CPU restatement of the reference's photon transport for voxelized media
+ * (bulk method 2) and of its two-phase fluorescence driver, written from the
+ * reference's behaviour:
+ *   launch_photon          LaunchPhoton          CUDAMCFLtransport.cu:460-562
+ *   step                   MCd3D loop body       CUDAMCFLtransport.cu:286-447
+ *   move_to_first_boundary MoveToFirstBoundary   CUDAMCFLtransport.cu:702-847
+ *   reflect                Reflect (method 2)    CUDAMCFLtransport.cu:628-700
+ *   spin                   Spin                  CUDAMCFLtransport.cu:585-625
+ *   photon_survive         PhotonSurvive         CUDAMCFLtransport.cu:850-864
+ *   Rng                    rand_MWC_co/oc        CUDAMCFLrng.cu:17-29
+ *   init_rng_streams       init_RNG              CUDAMCFLrng.cu:31-90
+ *   run_refstream          DoOneSimulation(Fl) + voxel loop  CUDAMCFLmain.cu:60-288,409-652
+ *
+ * Every floating-point expression keeps the reference's operand order and
+ * types (including its double-precision literals), so each rounding happens
+ * where it happens in the reference.  The file is compiled without
+ * contraction.  Two knobs:
+ *   math   libm         __logf/__cosf/__sincosf as the C library computes them
+ *                       (what the host build of the reference uses), or
+ *          portable     the series of portable_math.h (what the CUDA engine's
+ *                       exact-math kernel uses);
+ *   rng    refstream    32768 per-thread streams and the reference's
+ *                       relaunch schedule, or
+ *          photon       one stream per photon index (the engine's scheme).
+ * refstream+libm reproduces the host build of the reference bit for bit;
+ * photon+portable reproduces the engine's exact-math kernel bit for bit.
+ *
+ * Where the reference indexes past an array when a coordinate rounds onto the
+ * far edge of the grid or detector, the linear index is clamped to the last
+ * element (the engine does the same).  The reference's transport of the time
+ * of flight only feeds the time-resolved detectors, which this oracle does not
+ * tally.
+ */
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <atomic>
+#include <thread>
+#include <vector>
+
+#include "oracle_api.h"
+#include "portable_math.h"
+
+namespace {
+
+const unsigned kThreadsPerBlock = 256;   /* CUDAMCFL.h:18 */
+const unsigned kBlocks = 128;            /* CUDAMCFL.h:19 */
+const unsigned kThreads = kThreadsPerBlock * kBlocks;
+const unsigned kStepsPerLaunch = 80000;  /* CUDAMCFL.h:21 */
+const float kPi = 3.141592654f;          /* CUDAMCFL.h:22 */
+const unsigned kWeightRoulette = 429497u; /* CUDAMCFL.h:33 */
+const float kChance = 0.1f;              /* CUDAMCFL.h:34 */
+
+struct LibmMath {
+  static float log(float x) { return logf(x); }
+  static float cos(float x) { return cosf(x); }
+  static void sincos(float x, float *s, float *c) { *s = sinf(x); *c = cosf(x); }
+};
+
+struct PortableMath {
+  static float log(float x) { return mcfl_plogf(x); }
+  static float cos(float x) { return mcfl_pcosf(x); }
+  static void sincos(float x, float *s, float *c) { mcfl_psincosf(x, s, c); }
+};
+
+struct Rng {
+  uint64_t x;
+  uint32_t a;
+  float co() { /* [0,1) */
+    x = (x & 0xffffffffull) * a + (x >> 32);
+    return mcfl_u2f_rz((uint32_t)x) / 4294967296.0f;
+  }
+  float oc() { return 1.0f - co(); } /* (0,1] */
+};
+
+struct Prop {
+  float mutr, mua, g, n;
+};
+
+struct Photon {
+  float x, y, z, dx, dy, dz;
+  uint32_t weight;
+  uint32_t bulkpos;
+};
+
+/* Everything one transport phase reads (the reference's __constant__ set). */
+struct Phase {
+  float esp;
+  unsigned grid;
+  unsigned num_x, num_y, num_z;
+  unsigned total;
+  float size_x, size_y;
+  float det_dx, det_dy, det_x0, det_y0;
+  int det_nx;
+  unsigned xy_size;
+  unsigned last_bulk;
+  Prop prop[ORACLE_MAX_BULKS + 2];
+  const short *labels;
+  int fhd_on;
+  float xi, yi, zi, dir;
+  uint32_t start_weight;
+  int guard; /* reproduce the reference's non-atomic overflow guards */
+};
+
+inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
+  const float gf = mcfl_i2f_rn((int)ph.grid);
+  unsigned idx = mcfl_f2u_rz((x + 2 * ph.esp) * gf) +
+                 ph.num_x * (mcfl_f2u_rz((y + 2 * ph.esp) * gf) + ph.num_y * mcfl_f2u_rz(z * gf));
+  return idx < ph.total ? idx : ph.total - 1;
+}
+
+inline unsigned pixel_index(const Phase &ph, float x, float y) {
+  unsigned idx = mcfl_f2u_rz((y - ph.det_y0 + ph.size_y) / ph.det_dy) * (unsigned)ph.det_nx +
+                 mcfl_f2u_rz((x - ph.det_x0 + ph.size_x) / ph.det_dx);
+  return idx < ph.xy_size ? idx : ph.xy_size - 1;
+}
+
+inline uint32_t start_label(const Phase &ph, const Photon &p) {
+  if (p.z < ph.esp) {
+    if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp) return (uint32_t)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
+    return 1;
+  }
+  return ph.last_bulk;
+}
+
+template <class M>
+void launch_photon(Photon &p, Rng &r, const Phase &ph, float xi, float yi, float zi) {
+  if (ph.dir == 0.0f) {
+    const float gf = mcfl_i2f_rn((int)ph.grid);
+    p.x = xi + (0.999999f / gf) * r.oc();
+    p.y = yi + (0.999999f / gf) * r.oc();
+    p.z = zi + (0.999999f / gf) * r.oc();
+    float costheta = (float)(1.0 - 2.0 * (double)r.oc());
+    float sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
+    float psi = (float)(2.0 * (double)kPi * (double)r.oc());
+    float cospsi = M::cos(psi);
+    float sinpsi;
+    if (psi < kPi)
+      sinpsi = sqrtf((float)(1.0 - (double)(cospsi * cospsi)));
+    else
+      sinpsi = -sqrtf((float)(1.0 - (double)(cospsi * cospsi)));
+    p.dx = sintheta * cospsi;
+    p.dy = sintheta * sinpsi;
+    p.dz = costheta;
+    p.weight = 0xFFFFFFFFu;
+  } else {
+    const float input_fibre_diameter = (float)0.03;
+    float sample_rad = input_fibre_diameter * sqrtf(-M::log(r.oc()));
+    float sample_phi = 2 * kPi * r.oc();
+    float sin_phi, cos_phi;
+    M::sincos(sample_phi, &sin_phi, &cos_phi);
+    p.x = xi + sample_rad * cos_phi;
+    p.y = yi + sample_rad * sin_phi;
+    p.z = zi;
+    p.dx = 0.0f;
+    p.dy = 0.0f;
+    p.dz = 1.0f;
+    p.weight = ph.start_weight;
+  }
+  p.bulkpos = start_label(ph, p);
+}
+
+template <class M>
+void spin(Photon &p, float g, Rng &r) {
+  float cost, sint, cosp, sinp, temp;
+  float tempdir = p.dx;
+  temp = (1.0f - g * g) / (1.0f - g + 2.0f * g * r.co());
+  cost = (1.0f + g * g - temp * temp) / (2.0f * g);
+  if (g == 0.0f) cost = 2.0f * r.co() - 1.0f;
+  sint = sqrtf(1.0f - cost * cost);
+  /* The reference passes (&cosp, &sinp) as (sin, cos) outputs
+   * (CUDAMCFLtransport.cu:603): cosp holds sin(psi), sinp holds cos(psi). */
+  M::sincos(2.0f * kPi * r.co(), &cosp, &sinp);
+  temp = sqrtf(1.0f - p.dz * p.dz);
+  if (temp == 0.0f) {
+    p.dx = sint * cosp;
+    p.dy = sint * sinp;
+    p.dz = copysignf(cost, p.dz * cost);
+  } else {
+    p.dx = (sint * (p.dx * p.dz * cosp - p.dy * sinp)) / temp + p.dx * cost;
+    p.dy = (sint * (p.dy * p.dz * cosp + tempdir * sinp)) / temp + p.dy * cost;
+    p.dz = -sint * cosp * temp + p.dz * cost;
+  }
+  temp = 1.0f / sqrtf(p.dx * p.dx + p.dy * p.dy + p.dz * p.dz);
+  p.dx = p.dx * temp;
+  p.dy = p.dy * temp;
+  p.dz = p.dz * temp;
+}
+
+/* Returns 1 when reflected. */
+inline unsigned reflect(Photon &p, uint32_t newlb, Rng &r, const Phase &ph) {
+  float n1 = ph.prop[p.bulkpos].n, n2 = ph.prop[newlb].n;
+  float rr;
+  float cos_angle_i = fabsf(p.dz);
+  if (n1 == n2) {
+    p.bulkpos = newlb;
+    return 0u;
+  }
+  if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
+    p.dz *= -1.0f;
+    return 1u;
+  }
+  if (cos_angle_i == 1.0f) {
+    rr = (n1 - n2) / (n1 + n2);
+    if (r.co() <= rr * rr) {
+      p.dz *= -1.0f;
+      return 1u;
+    }
+    p.bulkpos = newlb;
+    return 0u;
+  }
+  float e = (n1 * n1) / (n2 * n2) * (1.0f - cos_angle_i * cos_angle_i);
+  rr = 2 * sqrtf((1.0f - cos_angle_i * cos_angle_i) * (1.0f - e) * e * cos_angle_i * cos_angle_i);
+  e = e + (cos_angle_i * cos_angle_i) * (1.0f - 2.0f * e);
+  rr = e * ((1.0f - e - rr) / ((1.0f - e + rr) * (e + rr)));
+  if (r.co() <= rr) {
+    p.dz *= -1.0f;
+    return 1u;
+  }
+  rr = n1 / n2;
+  e = rr * rr * (1.0f - cos_angle_i * cos_angle_i);
+  p.dx *= rr;
+  p.dy *= rr;
+  p.dz = copysignf(sqrtf(1 - e), p.dz);
+  p.bulkpos = newlb;
+  return 0u;
+}
+
+/* March through a scattering-free ("glass") voxel in half-voxel steps until
+ * the label changes, then back-project onto the sphere of radius 0.707 voxel
+ * around the centre of the voxel reached. */
+inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase &ph, float max_s) {
+  const unsigned num_x = ph.num_x, num_y = ph.num_y;
+  const float gf = mcfl_i2f_rn((int)ph.grid);
+  float search_step = 1 / (2 * gf);
+  float total_move = 0;
+  int index = 1;
+  uint32_t present_bulk = old_bulk;
+  while (present_bulk == old_bulk && total_move < max_s) {
+    p.x += p.dx * search_step;
+    p.y += p.dy * search_step;
+    p.z += p.dz * search_step;
+    if (p.z + p.dz * search_step < 0.0f) {
+      present_bulk = 0;
+      index = -1;
+      search_step = (-p.z) / p.dz;
+    } else if (p.z + p.dz * search_step > ph.esp) {
+      present_bulk = ph.last_bulk;
+      index = -1;
+      search_step = (ph.esp - p.z) / p.dz;
+    } else if (fabsf(p.x + p.dx * search_step) >= 2 * ph.esp || fabsf(p.y + p.dy * search_step) >= 2 * ph.esp) {
+      present_bulk = 1;
+      index = -1;
+    } else {
+      index = (int)voxel_index(ph, p.x, p.y, p.z);
+      present_bulk = (uint32_t)(unsigned short)ph.labels[index];
+    }
+    total_move += search_step;
+  }
+  if (index >= 0 && present_bulk != old_bulk) {
+    unsigned uidx = (unsigned)index;
+    unsigned z_grid = uidx / (num_x * num_y);
+    uidx -= z_grid * num_x * num_y;
+    unsigned y_grid = uidx / num_x;
+    unsigned x_grid = uidx % num_x;
+    const double half = 1. / (2. * (double)ph.grid);
+    float y_voxel = (float)((double)(mcfl_i2f_rn((int)y_grid) / (float)ph.grid - 2 * ph.esp) + half);
+    float x_voxel = (float)((double)(mcfl_i2f_rn((int)x_grid) / (float)ph.grid - 2 * ph.esp) + half);
+    float z_voxel = (float)((double)(mcfl_i2f_rn((int)z_grid) / (float)ph.grid) + half);
+    const double rv = 0.707107 * (double)(1 / gf);
+    float r_voxel2 = (float)(rv * rv);
+    float pow_dx = p.dx * p.dx, pow_dy = p.dy * p.dy, pow_dz = p.dz * p.dz;
+    float pow_px = p.x * p.x, pow_py = p.y * p.y, pow_pz = p.z * p.z;
+    float pow_cx = x_voxel * x_voxel, pow_cy = y_voxel * y_voxel, pow_cz = z_voxel * z_voxel;
+    float disc = 2 * x_voxel * y_voxel * p.dx * p.dy - (pow_cy + pow_cz) * pow_dx - (pow_cx + pow_cz) * pow_dy -
+                 (pow_cx + pow_cy) * pow_dz - (pow_dy + pow_dz) * pow_px - (pow_dx + pow_dz) * pow_py -
+                 (pow_dx + pow_dy) * pow_pz + (pow_dx + pow_dy + pow_dz) * r_voxel2 +
+                 2 * (x_voxel * z_voxel * p.dx + y_voxel * z_voxel * p.dy) * p.dz -
+                 2 * (y_voxel * p.dx * p.dy - x_voxel * pow_dy + z_voxel * p.dx * p.dz - x_voxel * pow_dz) * p.x +
+                 2 * (y_voxel * pow_dx - x_voxel * p.dx * p.dy - z_voxel * p.dy * p.dz + y_voxel * pow_dz +
+                      p.dx * p.dy * p.x) * p.y +
+                 2 * (z_voxel * pow_dx + z_voxel * pow_dy + p.dx * p.dz * p.x + p.dy * p.dz * p.y -
+                      (x_voxel * p.dx + y_voxel * p.dy) * p.dz) * p.z;
+    float root = sqrtf(disc);
+    float lin = x_voxel * p.dx + y_voxel * p.dy + z_voxel * p.dz - p.dx * p.x - p.dy * p.y - p.dz * p.z;
+    float den = pow_dx + pow_dy + pow_dz;
+    float back_step1 = -(lin + root) / den;
+    float back_step2 = -(lin - root) / den;
+    float new_px1 = p.x - p.dx * back_step1, new_py1 = p.y - p.dy * back_step1, new_pz1 = p.z - p.dz * back_step1;
+    float new_px2 = p.x - p.dx * back_step2, new_py2 = p.y - p.dy * back_step2, new_pz2 = p.z - p.dz * back_step2;
+    if (((new_px1 - x_voxel) * (new_px1 - x_voxel) + (new_py1 - y_voxel) * (new_py1 - y_voxel) +
+         (new_pz1 - z_voxel) * (new_pz1 - z_voxel)) <
+        ((new_px2 - x_voxel) * (new_px2 - x_voxel) + (new_py2 - y_voxel) * (new_py2 - y_voxel) +
+         (new_pz2 - z_voxel) * (new_pz2 - z_voxel))) {
+      p.x = new_px1; p.y = new_py1; p.z = new_pz1;
+    } else {
+      p.x = new_px2; p.y = new_py2; p.z = new_pz2;
+    }
+  }
+  return present_bulk;
+}
+
+inline unsigned photon_survive(Photon &p, Rng &r, uint64_t *gain, uint64_t *loss) {
+  if (p.weight > kWeightRoulette) return 1u;
+  if (p.weight == 0u) return 0u;
+  if (r.co() < kChance) {
+    uint32_t w0 = p.weight;
+    p.weight = mcfl_f2u_rn(mcfl_u2f_rn(p.weight) / kChance);
+    *gain += (uint64_t)(p.weight - w0);
+    return 1u;
+  }
+  *loss += p.weight;
+  return 0u;
+}
+
+inline void add_guarded(unsigned long long *t, uint32_t w, int guard) {
+  if (!guard) {
+    __atomic_fetch_add(t, (unsigned long long)w, __ATOMIC_RELAXED);
+  } else if (*t + w < (unsigned long long)LLONG_MAX) {
+    __atomic_fetch_add(t, (unsigned long long)w, __ATOMIC_RELAXED);
+  }
+}
+
+/* Where a phase's tallies go.  exit_img: image for an exit through the top
+ * (R) or the bottom (T); the emission phase of the photon-indexed variant
+ * weights exits with the emitting voxel's fixed-point factor instead. */
+struct Sink {
+  unsigned long long *Rd = nullptr, *Tt = nullptr, *fhd = nullptr;
+  unsigned long long *R128 = nullptr, *T128 = nullptr; /* lo,hi pairs */
+  uint64_t voxel_q = 0;
+  uint64_t absorbed = 0, exit_top = 0, exit_bottom = 0, r_loss = 0, r_gain = 0, w0_loss = 0, steps = 0;
+};
+
+inline void add128(unsigned long long *acc, uint32_t w, uint64_t q) {
+  unsigned __int128 prod = (unsigned __int128)w * q;
+  uint64_t lo = (uint64_t)prod, hi = (uint64_t)(prod >> 64);
+  uint64_t old = acc[0];
+  acc[0] = old + lo;
+  acc[1] += hi + (acc[0] < old ? 1u : 0u);
+}
+
+/* One pass of the MCd3D loop body up to the survival test.  Returns 1 while
+ * the photon lives. */
+template <class M>
+unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
+  float s;
+  uint32_t new_bulk;
+  const uint32_t last_bulk = ph.last_bulk;
+  sk.steps++;
+  if (ph.prop[p.bulkpos].mutr != FLT_MAX) {
+    s = -M::log(r.oc()) * ph.prop[p.bulkpos].mutr;
+    new_bulk = p.bulkpos;
+    if (p.z + s * p.dz < 0.0f) {
+      new_bulk = 0;
+      s = (-p.z) / p.dz;
+    }
+    if (p.z + s * p.dz > ph.esp) {
+      new_bulk = last_bulk;
+      s = (ph.esp - p.z) / p.dz;
+    }
+    p.x += p.dx * s;
+    p.y += p.dy * s;
+    p.z += p.dz * s;
+    if (new_bulk != 0 && new_bulk != last_bulk) {
+      if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp && p.z < ph.esp)
+        new_bulk = (uint32_t)(unsigned short)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
+      else
+        new_bulk = 1;
+    }
+  } else {
+    s = 100.0f;
+    new_bulk = move_to_first_boundary(p, p.bulkpos, ph, s);
+  }
+  if (new_bulk != p.bulkpos) reflect(p, new_bulk, r, ph);
+  if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp && p.z < ph.esp && ph.fhd_on == 1)
+    add_guarded(&sk.fhd[voxel_index(ph, p.x, p.y, p.z)], p.weight, ph.guard);
+  if (p.bulkpos == 0) {
+    if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
+      unsigned idx = pixel_index(ph, p.x, p.y);
+      if (sk.R128) add128(&sk.R128[2 * (size_t)idx], p.weight, sk.voxel_q);
+      else add_guarded(&sk.Rd[idx], p.weight, ph.guard);
+    }
+    sk.exit_top += p.weight;
+    p.weight = 0u;
+    s = 0.0f;
+  }
+  if (p.bulkpos == last_bulk) {
+    if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
+      unsigned idx = pixel_index(ph, p.x, p.y);
+      if (sk.T128) add128(&sk.T128[2 * (size_t)idx], p.weight, sk.voxel_q);
+      else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
+    }
+    sk.exit_bottom += p.weight;
+    p.weight = 0u;
+    s = 0.0f;
+  }
+  if (s > 0.0f) {
+    const Prop &pr = ph.prop[p.bulkpos];
+    uint32_t w = mcfl_f2u_ru(pr.mua * pr.mutr * mcfl_u2f_rn(p.weight));
+    if (w > 0) {
+      p.weight -= w;
+      sk.absorbed += w;
+    } else {
+      sk.w0_loss += p.weight;
+      p.weight = 0u;
+    }
+    spin<M>(p, pr.g, r);
+  }
+  return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+}
+
+/* ------------------------------------------------------------------------ */
+
+void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
+  memset(&ph, 0, sizeof(ph));
+  ph.esp = sim->esp;
+  ph.grid = (unsigned)sim->grid_size;
+  const float gf = mcfl_i2f_rn(sim->grid_size);
+  ph.num_x = mcfl_f2u_rn(4 * ph.esp * gf);
+  ph.num_y = mcfl_f2u_rn(4 * ph.esp * gf);
+  ph.num_z = (unsigned)(int)(sim->esp * (float)sim->grid_size);
+  ph.total = ph.num_x * ph.num_y * ph.num_z;
+  ph.det_dx = sim->det_dx; ph.det_dy = sim->det_dy;
+  ph.det_x0 = sim->det_x0; ph.det_y0 = sim->det_y0;
+  ph.det_nx = sim->det_nx;
+  ph.size_x = (sim->det_dx * mcfl_i2f_rn(sim->det_nx)) / 2.0f;
+  ph.size_y = (sim->det_dy * mcfl_i2f_rn(sim->det_ny)) / 2.0f;
+  ph.xy_size = (unsigned)(sim->det_nx + sim->det_ny * sim->det_nx);
+  ph.last_bulk = sim->n_bulks + 1;
+  for (unsigned i = 0; i < sim->n_bulks + 2; ++i) {
+    const oracle_bulk &b = sim->bulks[i];
+    ph.prop[i] = Prop{b.mutr, emission ? b.muaf : b.mua, b.g, b.n};
+  }
+  ph.labels = sim->bulk_info;
+  ph.fhd_on = emission ? 0 : sim->fhd_activated;
+  ph.xi = sim->xi; ph.yi = sim->yi; ph.zi = sim->zi;
+  ph.dir = emission ? 0.0f : sim->dir;
+  ph.start_weight = sim->start_weight;
+}
+
+/* init_RNG (CUDAMCFLrng.cu:31-90) restated.  Returns 0 on success. */
+int init_rng_streams(uint64_t *x, uint32_t *a, unsigned n, const char *path, uint64_t xinit) {
+  FILE *fp = fopen(path, "r");
+  if (!fp) return 1;
+  unsigned begin = 0, fora, t1, t2;
+  if (fscanf(fp, "%u %u %u", &begin, &t1, &t2) != 3) { fclose(fp); return 1; }
+  if ((xinit == 0ull) | (((unsigned)(xinit >> 32)) >= (begin - 1)) | (((unsigned)xinit) >= 0xfffffffful)) {
+    fclose(fp);
+    return 1;
+  }
+  for (unsigned i = 0; i < n; i++) {
+    if (fscanf(fp, "%u %u %u", &fora, &t1, &t2) != 3) { fclose(fp); return 1; }
+    a[i] = fora;
+    x[i] = 0;
+    while ((x[i] == 0) | (((unsigned)(x[i] >> 32)) >= (fora - 1)) | (((unsigned)x[i]) >= 0xfffffffful)) {
+      xinit = (xinit & 0xffffffffull) * (begin) + (xinit >> 32);
+      x[i] = (unsigned)floor((((double)((unsigned)xinit)) / (double)0x100000000) * fora);
+      x[i] = x[i] << 32;
+      xinit = (xinit & 0xffffffffull) * (begin) + (xinit >> 32);
+      x[i] += (unsigned)xinit;
+    }
+  }
+  fclose(fp);
+  return 0;
+}
+
+/* State of the 32768 virtual threads across relaunches. */
+struct ThreadBank {
+  std::vector<Photon> p;
+  std::vector<uint32_t> active;
+  std::vector<uint64_t> *x;
+  std::vector<uint32_t> *a;
+};
+
+/* DoOneSimulation(Fl)'s launch loop with the MCd3D thread body restated:
+ * one launch is 32768 virtual threads, each running up to 80000 passes; a
+ * terminated photon is replaced while fewer than N - 32768 photons have
+ * terminated.  Returns the number of terminated photons, 0 past the
+ * relaunch cap. */
+template <class M>
+unsigned long long run_threads(const Phase &ph, unsigned long long nphot, std::vector<uint64_t> &x,
+                               std::vector<uint32_t> &a, Sink &sk, int nthreads, long cap) {
+  std::vector<Photon> P(kThreads);
+  std::vector<uint32_t> active(kThreads, 1u);
+  std::atomic<unsigned long long> terminated(0);
+  /* LaunchPhoton_Global does not store the advanced RNG state back
+   * (CUDAMCFLtransport.cu:574-581): the first transport pass of every thread
+   * draws the same numbers its launch drew. */
+  for (unsigned t = 0; t < kThreads; ++t) {
+    Rng r{x[t], a[t]};
+    launch_photon<M>(P[t], r, ph, ph.xi, ph.yi, ph.zi);
+  }
+  const unsigned long long limit = nphot - kThreads; /* unsigned, as the reference */
+  auto body = [&](unsigned t, Sink &s) {
+    Rng r{x[t], a[t]};
+    Photon p = P[t];
+    unsigned ii = active[t] ? 0 : kStepsPerLaunch;
+    for (; ii < kStepsPerLaunch; ii++) {
+      if (!step<M>(p, r, ph, s)) {
+        if (terminated.fetch_add(1) < limit) {
+          launch_photon<M>(p, r, ph, ph.xi, ph.yi, ph.zi);
+        } else {
+          active[t] = 0u;
+          ii = kStepsPerLaunch;
+        }
+      }
+    }
+    P[t] = p;
+    x[t] = r.x;
+  };
+  long launches = 0;
+  for (;;) {
+    ++launches;
+    if (nthreads <= 1) {
+      for (unsigned t = 0; t < kThreads; ++t) body(t, sk);
+    } else {
+      std::vector<Sink> local(nthreads);
+      for (auto &l : local) { l.Rd = sk.Rd; l.Tt = sk.Tt; l.fhd = sk.fhd; l.R128 = sk.R128; l.T128 = sk.T128; }
+      std::vector<std::thread> pool;
+      for (int w = 0; w < nthreads; ++w)
+        pool.emplace_back([&, w] {
+          for (unsigned b = (unsigned)w; b < kBlocks; b += (unsigned)nthreads)
+            for (unsigned t = b * kThreadsPerBlock; t < (b + 1) * kThreadsPerBlock; ++t) body(t, local[w]);
+        });
+      for (auto &th : pool) th.join();
+      for (auto &l : local) {
+        sk.absorbed += l.absorbed; sk.exit_top += l.exit_top; sk.exit_bottom += l.exit_bottom;
+        sk.r_loss += l.r_loss; sk.r_gain += l.r_gain; sk.w0_loss += l.w0_loss; sk.steps += l.steps;
+      }
+    }
+    unsigned sum = 0;
+    for (unsigned t = 0; t < kThreads; ++t) sum += active[t];
+    if (sum == 0) break;
+    if (cap > 0 && launches > cap) return 0;
+  }
+  return terminated.load();
+}
+
+template <class M>
+int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uint64_t seed_fl, int nthreads,
+                   oracle_result *res) {
+  Phase ph;
+  make_phase(sim, ph, 0);
+  ph.guard = 1;
+  const int nx2 = sim->det_nx, ny2 = sim->det_ny;
+  const unsigned xy = ph.xy_size;
+  res->grid[0] = (int)ph.num_x; res->grid[1] = (int)ph.num_y; res->grid[2] = (int)ph.num_z;
+  res->image[0] = nx2; res->image[1] = ny2;
+  res->number_of_photons = sim->number_of_photons;
+  res->Rd = (unsigned long long *)calloc(xy, 8);
+  res->Tt = (unsigned long long *)calloc(xy, 8);
+  res->fhd = (unsigned long long *)calloc(ph.total ? ph.total : 1, 8);
+  res->flR = (double *)calloc(xy, 8);
+  res->flT = (double *)calloc(xy, 8);
+  std::vector<uint64_t> x(kThreads);
+  std::vector<uint32_t> a(kThreads);
+  if (init_rng_streams(x.data(), a.data(), kThreads, sp, seed_exc)) return -2;
+  Sink sk;
+  sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
+  unsigned long long done = run_threads<M>(ph, sim->number_of_photons, x, a, sk, nthreads, 0);
+  res->photons_exc = done;
+  res->steps_exc = sk.steps;
+  res->balance[0] = sk.absorbed; res->balance[1] = sk.exit_top; res->balance[2] = sk.exit_bottom;
+  res->balance[3] = sk.r_loss; res->balance[4] = sk.r_gain; res->balance[5] = sk.w0_loss;
+  std::vector<double> Fx(ph.total ? ph.total : 1);
+  for (unsigned v = 0; v < ph.total; v++) Fx[v] = ((double)res->fhd[v] / (0xFFFFFFFF * done));
+
+  if (init_rng_streams(x.data(), a.data(), kThreads, sp, seed_fl)) return -2;
+  if (sim->do_fl_sim == 0 || sim->bulk_method != 2) return 0;
+  Phase fl;
+  make_phase(sim, fl, 1);
+  fl.guard = 1;
+  const double dx = sim->det_dx, dy = sim->det_dy;
+  std::vector<unsigned long long> tR(xy), tT(xy);
+  for (unsigned ix = 0; ix < ph.num_x; ix++)
+    for (unsigned iy = 0; iy < ph.num_y; iy++)
+      for (unsigned iz = 0; iz < ph.num_z; iz++) {
+        unsigned index = ix + ph.num_x * (iy + iz * ph.num_y);
+        short bd = sim->bulk_info[index];
+        if (!(sim->bulks[bd].albedof < 1)) continue; /* adds 0 * image in the reference */
+        float xi = ((float)ix / (float)sim->grid_size) - 2 * sim->esp;
+        float yi = ((float)iy / (float)sim->grid_size) - 2 * sim->esp;
+        float zi = ((float)iz / (float)sim->grid_size);
+        fl.xi = xi; fl.yi = yi; fl.zi = zi;
+        std::fill(tR.begin(), tR.end(), 0ull);
+        std::fill(tT.begin(), tT.end(), 0ull);
+        Sink s2;
+        s2.Rd = tR.data(); s2.Tt = tT.data();
+        std::vector<uint64_t> x_before = x; /* a capped run does not copy its RNG state back */
+        unsigned long long st = run_threads<M>(fl, (unsigned long long)sim->number_of_photons_per_voxel, x, a, s2,
+                                               nthreads, 10000);
+        if (st == 0) x = x_before;
+        res->steps_fl += s2.steps;
+        res->fl_voxels += 1;
+        if (st == 0) res->failed_voxels += 1;
+        res->photons_fl += st;
+        double voxelw = ((double)sim->bulks[bd].eY * (double)(1 - sim->bulks[bd].albedof) * Fx[index]) /
+                        (double)(st * 0xFFFFFFFF);
+        for (unsigned ij = 0; ij < xy; ij++) {
+          double tempvwR = voxelw * (double)tR[ij];
+          double tempvwT = voxelw * (double)tT[ij];
+          if (res->flR[ij] + tempvwR < DBL_MAX) res->flR[ij] += tempvwR / (dx * dy);
+          if (res->flT[ij] + tempvwT < DBL_MAX) res->flT[ij] += tempvwT / (dx * dy);
+        }
+      }
+  return 0;
+}
+
+/* ------------------------- photon-indexed variant ------------------------ */
+
+template <class M>
+void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint64_t k0, uint64_t k1, Sink &sk,
+                      const uint32_t *vox, const uint64_t *voxq, unsigned nv) {
+  for (uint64_t k = k0; k < k1; ++k) {
+    Rng r;
+    mcfl_photon_stream(key, k, table, &r.x, &r.a);
+    Photon p;
+    if (vox) {
+      uint32_t v = vox[k / nv];
+      unsigned ix = v % ph.num_x, iy = (v / ph.num_x) % ph.num_y, iz = v / (ph.num_x * ph.num_y);
+      float xi = ((float)ix / (float)ph.grid) - 2 * ph.esp;
+      float yi = ((float)iy / (float)ph.grid) - 2 * ph.esp;
+      float zi = ((float)iz / (float)ph.grid);
+      sk.voxel_q = voxq[k / nv];
+      launch_photon<M>(p, r, ph, xi, yi, zi);
+    } else {
+      launch_photon<M>(p, r, ph, ph.xi, ph.yi, ph.zi);
+    }
+    while (step<M>(p, r, ph, sk)) {
+    }
+  }
+}
+
+template <class M>
+int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc, uint64_t seed_fl,
+                oracle_result *res) {
+  Phase ph;
+  make_phase(sim, ph, 0);
+  ph.guard = 0;
+  const unsigned xy = ph.xy_size;
+  res->grid[0] = (int)ph.num_x; res->grid[1] = (int)ph.num_y; res->grid[2] = (int)ph.num_z;
+  res->image[0] = sim->det_nx; res->image[1] = sim->det_ny;
+  res->number_of_photons = sim->number_of_photons;
+  res->Rd = (unsigned long long *)calloc(xy, 8);
+  res->Tt = (unsigned long long *)calloc(xy, 8);
+  res->fhd = (unsigned long long *)calloc(ph.total ? ph.total : 1, 8);
+  res->flR = (double *)calloc(xy, 8);
+  res->flT = (double *)calloc(xy, 8);
+  res->flR128 = (unsigned long long *)calloc(2 * (size_t)xy, 8);
+  res->flT128 = (unsigned long long *)calloc(2 * (size_t)xy, 8);
+  Sink sk;
+  sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
+  const unsigned long long N = sim->number_of_photons;
+  run_photon_range<M>(ph, mcfl_stream_key(seed_exc, 0), table, 0, N, sk, nullptr, nullptr, 1);
+  res->photons_exc = N;
+  res->steps_exc = sk.steps;
+  res->balance[0] = sk.absorbed; res->balance[1] = sk.exit_top; res->balance[2] = sk.exit_bottom;
+  res->balance[3] = sk.r_loss; res->balance[4] = sk.r_gain; res->balance[5] = sk.w0_loss;
+  if (sim->do_fl_sim == 0 || sim->bulk_method != 2) return 0;
+
+  /* Emitting voxels in increasing linear index, with fixed-point weights
+   * q_v = rint(eY (1 - albedof) PHD_v 2^40), PHD_v = fhd_v / ((2^32-1) N). */
+  std::vector<uint32_t> vox;
+  std::vector<uint64_t> q;
+  for (unsigned v = 0; v < ph.total; ++v) {
+    const oracle_bulk &b = sim->bulks[sim->bulk_info[v]];
+    if (!(b.albedof < 1)) continue;
+    double fx = (double)res->fhd[v] / (double)(0xFFFFFFFFull * N);
+    double wv = (double)b.eY * (double)(1 - b.albedof) * fx;
+    double qs = nearbyint(wv * 0x1p40);
+    uint64_t qv = qs >= 18446744073709551615.0 ? 0xFFFFFFFFFFFFFFFFull : (uint64_t)qs;
+    if (qv == 0) continue;
+    vox.push_back(v);
+    q.push_back(qv);
+  }
+  Phase fl;
+  make_phase(sim, fl, 1);
+  fl.guard = 0;
+  Sink s2;
+  s2.R128 = res->flR128; s2.T128 = res->flT128;
+  const unsigned nv = sim->number_of_photons_per_voxel;
+  const uint64_t M_total = (uint64_t)vox.size() * nv;
+  run_photon_range<M>(fl, mcfl_stream_key(seed_fl, 1), table, 0, M_total, s2, vox.data(), q.data(), nv);
+  res->steps_fl = s2.steps;
+  res->fl_voxels = (long)vox.size();
+  res->photons_fl = M_total;
+  const double norm = ((double)nv * 4294967295.0) * ((double)sim->det_dx * (double)sim->det_dy);
+  for (unsigned i = 0; i < xy; ++i) {
+    double r = (double)res->flR128[2 * i + 1] * 18446744073709551616.0 + (double)res->flR128[2 * i];
+    double t = (double)res->flT128[2 * i + 1] * 18446744073709551616.0 + (double)res->flT128[2 * i];
+    res->flR[i] = r * 0x1p-40 / norm;
+    res->flT[i] = t * 0x1p-40 / norm;
+  }
+  return 0;
+}
+
+} // namespace
+
+extern "C" int oracle_run_refstream(const oracle_sim *sim, const char *safeprimes_path, unsigned long long seed_exc,
+                                    unsigned long long seed_fl, int math_libm, int nthreads, oracle_result *res) {
+  memset(res, 0, sizeof(*res));
+  if (sim->bulk_method != 2 || sim->n_bulks > ORACLE_MAX_BULKS) return -1;
+  /* With N <= 32768 the reference's relaunch test compares against
+   * N - 32768 computed in unsigned 64-bit arithmetic, which wraps: every
+   * photon is replaced and the run never ends (the emission phase stops at
+   * its 10000-launch cap only after ~2.6e12 passes).  Refuse such inputs. */
+  if (sim->number_of_photons <= kThreads) return -4;
+  if (sim->do_fl_sim != 0 && sim->number_of_photons_per_voxel <= kThreads) return -4;
+  return math_libm ? refstream_impl<LibmMath>(sim, safeprimes_path, seed_exc, seed_fl, nthreads, res)
+                   : refstream_impl<PortableMath>(sim, safeprimes_path, seed_exc, seed_fl, nthreads, res);
+}
+
+extern "C" int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipliers, unsigned int n_multipliers,
+                                 unsigned long long seed_exc, unsigned long long seed_fl, int math_libm,
+                                 oracle_result *res) {
+  memset(res, 0, sizeof(*res));
+  if (sim->bulk_method != 2 || sim->n_bulks > ORACLE_MAX_BULKS || n_multipliers != 32768) return -1;
+  return math_libm ? photon_impl<LibmMath>(sim, multipliers, seed_exc, seed_fl, res)
+                   : photon_impl<PortableMath>(sim, multipliers, seed_exc, seed_fl, res);
+}

@@ -1,0 +1,104 @@
+/*
+ * Device-side job and launch descriptors of the transport engine, shared by
+ * the kernels and the host engine.
+ *
+ * A launch processes a list of jobs.  Every job owns a contiguous range of
+ * global photon tickets [ticket_begin, ticket_begin + photons); persistent
+ * threads draw tickets from one 64-bit counter, so jobs of any size, medium or
+ * source mix freely inside one launch.  Photon k of a job draws its random
+ * numbers from the MWC stream (key, rng_offset + k) of portable_math.h, so a
+ * photon's trajectory does not depend on which thread, launch or batch
+ * carries it, and the 64-bit integer tallies are therefore bit-identical for
+ * any schedule.
+ */
+#ifndef MCFL_ENGINE_TYPES_H
+#define MCFL_ENGINE_TYPES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define MCFL_ALIGN(n) alignas(n)
+#else
+#define MCFL_ALIGN(n)
+#endif
+
+/* Per-job statistics, 64-bit counters. */
+enum {
+  MCFL_ST_DONE = 0,        /* photons terminated */
+  MCFL_ST_STEPS = 1,       /* transport passes */
+  MCFL_ST_ABSORBED = 2,    /* weight deposited by absorption */
+  MCFL_ST_EXIT_TOP = 3,    /* weight that left through z = 0 (inside or outside the detector) */
+  MCFL_ST_EXIT_BOTTOM = 4, /* weight that left through z = thickness */
+  MCFL_ST_R_LOSS = 5,      /* weight of photons that lost the roulette */
+  MCFL_ST_R_GAIN = 6,      /* weight added to roulette survivors */
+  MCFL_ST_W0_LOSS = 7,     /* weight of photons killed by a zero weight drop (mu_a = 0) */
+  MCFL_ST_CAPPED = 8,      /* photons stopped by the per-photon pass cap */
+  MCFL_ST_COUNT = 9
+};
+
+/* Source kinds. */
+enum {
+  MCFL_SRC_GAUSS_BEAM = 1, /* collimated beam, radius 0.03 sqrt(-ln u) (reference dir=1) */
+  MCFL_SRC_VOXELS = 2,     /* isotropic, uniform inside voxels of a list (reference dir=0, per voxel) */
+  MCFL_SRC_WIDEFIELD = 3   /* collimated, uniform over a rectangle */
+};
+
+typedef struct MCFL_ALIGN(16) McflJob {
+  /* medium (bulk-descriptor voxel grid, x fastest) */
+  const uint8_t *labels;
+  const float *prop; /* 4 floats per label: 1/(mu_a+mu_s) (FLT_MAX = no scattering), mu_a, g, n */
+  float hx, hy, esp; /* |x| < hx, |y| < hy, 0 <= z < esp */
+  float gx, gy, gz;  /* voxels per cm */
+  uint32_t nx, ny, nz, total;
+  uint32_t last_label; /* label of the medium below the slab (labels + 1) */
+  uint32_t src_kind;
+  /* source */
+  float sx, sy, sz;
+  float src_w, src_h;
+  uint32_t start_weight;
+  const uint32_t *src_vox; /* MCFL_SRC_VOXELS: linear voxel indices */
+  const uint64_t *src_q;   /* MCFL_SRC_VOXELS: fixed-point exit weights per voxel (2^-40 units) */
+  uint32_t per_voxel;      /* MCFL_SRC_VOXELS: photons per voxel */
+  uint32_t fhd_on;
+  /* detector (R at z = 0, T at z = esp) */
+  float det_x0, det_y0, det_dx, det_dy, size_x, size_y;
+  uint32_t det_nx, xy_size;
+  /* tallies */
+  unsigned long long *R, *T;       /* 64-bit sums of 32-bit exit weights */
+  unsigned long long *R128, *T128; /* (lo, hi) sums of weight x src_q, MCFL_SRC_VOXELS */
+  unsigned long long *fhd;         /* photon hitting density, when fhd_on */
+  unsigned long long *stats;       /* MCFL_ST_COUNT counters */
+  /* photons */
+  uint64_t key;          /* stream family key */
+  uint64_t rng_offset;   /* stream index of the job's photon 0 */
+  uint64_t ticket_begin; /* first global ticket */
+  uint64_t photons;      /* photons in the job */
+} McflJob;
+
+/* Photon state carried between slices of a budgeted launch. */
+typedef struct MCFL_ALIGN(16) McflSaved {
+  float x, y, z, dx, dy, dz;
+  uint32_t weight, label;
+  uint64_t rng_x;
+  uint32_t rng_a, job;
+  uint64_t k;        /* photon index within the job */
+  uint32_t steps;    /* passes of this photon so far */
+  uint32_t alive;
+  uint32_t src_idx;  /* voxel-list entry (MCFL_SRC_VOXELS) */
+  uint32_t pad;
+} McflSaved;
+
+typedef struct McflLaunch {
+  const McflJob *jobs;
+  uint32_t n_jobs;
+  uint32_t max_iters; /* loop iterations per launch; 0 = run until no ticket is left */
+  unsigned long long *ticket_counter;
+  uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */
+  const unsigned long long *ticket_end_dev; /* ticket end written by an earlier kernel */
+  const uint32_t *mult; /* 32768 MWC multipliers */
+  McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
+  uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
+  uint32_t pad;
+} McflLaunch;
+
+#endif

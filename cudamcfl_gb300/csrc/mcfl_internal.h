@@ -1,0 +1,105 @@
+/*
+ * Internal declarations of libmcfl shared by the host translation units.
+ */
+#ifndef MCFL_INTERNAL_H
+#define MCFL_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "engine_types.h"
+#include "mcfl.h"
+
+namespace mcfl {
+
+constexpr size_t kMwcTableEntries = 32768;
+
+/* safeprimes.cpp */
+bool mwc_multiplier_valid(uint32_t a);
+std::vector<uint32_t> mwc_multipliers(size_t count);
+const std::vector<uint32_t> &mwc_table(); /* kMwcTableEntries + 1 entries */
+
+/* errors (thread-local message) */
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *where);
+
+/* Grow-only device buffer. */
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  cudaError_t reserve(size_t n);
+  void release();
+  template <class T> T *as() const { return static_cast<T *>(p); }
+  ~DevBuf() { release(); }
+};
+
+/* engine_kernels.cu */
+extern "C" cudaError_t mcfl_launch_emission_prep(const uint8_t *labels, const float2 *fl, const unsigned long long *fhd,
+                                                 const float *fmap, uint32_t total, unsigned long long photons_exc,
+                                                 uint32_t per_voxel, uint32_t *block_counts, uint32_t *vox,
+                                                 uint64_t *q, unsigned long long *list_len,
+                                                 McflJob *job, unsigned long long *ticket_end, cudaStream_t s);
+size_t emission_prep_blocks(uint32_t total);
+extern "C" cudaError_t mcfl_launch_normalize_u64(const unsigned long long *raw, double *out, size_t n, double scale,
+                                                 cudaStream_t s);
+extern "C" cudaError_t mcfl_launch_normalize_phd(const unsigned long long *raw, double *out, size_t n,
+                                                 unsigned long long photons, cudaStream_t s);
+extern "C" cudaError_t mcfl_launch_normalize_128(const unsigned long long *raw, double *out, size_t n, double norm,
+                                                 cudaStream_t s);
+
+/* transport kernels */
+extern "C" cudaError_t mcfl_launch_transport_exact(const McflLaunch *L, int grid, int block, cudaStream_t s);
+extern "C" cudaError_t mcfl_launch_transport_fast(const McflLaunch *L, int grid, int block, cudaStream_t s);
+extern "C" cudaError_t mcfl_attr_transport_exact(int block, int *blocks_per_sm, int *regs);
+extern "C" cudaError_t mcfl_attr_transport_fast(int block, int *blocks_per_sm, int *regs);
+
+/* engine.cpp: one emission run from one voxel with the medium's excitation
+ * table (DoOneSimulationFl), raw 64-bit images */
+int run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run, unsigned int voxel,
+                              unsigned long long *R, unsigned long long *T, unsigned long long *stats);
+
+/* mci.cpp */
+void simulation_geometry(const mcfl_simulation *sim, float *half_x, float *half_y, float *esp, float *g);
+
+} // namespace mcfl
+
+struct mcfl_medium {
+  mcfl_ctx *ctx = nullptr;
+  mcfl::DevBuf labels, prop_exc, prop_emi, fl, fmap;
+  int nx = 0, ny = 0, nz = 0;
+  uint32_t total = 0;
+  float hx = 0, hy = 0, esp = 0, gx = 0, gy = 0, gz = 0;
+  int n_bulks = 0;
+  bool has_fmap = false;
+  std::vector<mcfl_bulk> bulks;
+  size_t bytes = 0;
+};
+
+struct mcfl_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  mcfl::DevBuf mult;       /* 32768 multipliers */
+  mcfl::DevBuf jobs;       /* job table */
+  mcfl::DevBuf counters;   /* ticket counters and ticket ends */
+  mcfl::DevBuf saved;      /* parked photons of budgeted launches */
+  /* run workspace */
+  mcfl::DevBuf R, T, fhd, R128, T128, stats, vox, q, block_counts, outd;
+  int math = MCFL_MATH_EXACT;
+  int block = 256;
+  int blocks_per_sm = 0;
+  uint32_t step_cap = 1u << 24;
+  int l2_window = 0;
+  unsigned long long launches = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+  int grid_for(int block_size, int *bps_out = nullptr);
+  cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
+};
+
+#endif

@@ -1,0 +1,575 @@
+/*
+ * Persistent photon-transport kernel for voxelized (bulk-descriptor) turbid
+ * media, sm_103a.
+ *
+ * Included by two translation units that differ only in floating-point
+ * semantics:
+ *   transport_exact.cu  MCFL_EXACT_MATH=1, nvcc -fmad=false -prec-div=true
+ *                       -prec-sqrt=true -ftz=false: every float operation is
+ *                       rounded once, logarithm and sine/cosine come from
+ *                       portable_math.h, so the tallies equal those of the
+ *                       CPU oracle bit for bit;
+ *   transport_fast.cu   MCFL_EXACT_MATH=0, --use_fast_math: the hardware
+ *                       SFU intrinsics, i.e. the numerics of the reference's
+ *                       own GPU build (Compile750:1 -use_fast_math).
+ *
+ * Physics follows the reference's voxelized transport step by step and keeps
+ * its operand order (RefCompat):
+ *   photon launch      LaunchPhoton           CUDAMCFLtransport.cu:460-562
+ *   transport pass     MCd3D loop body        CUDAMCFLtransport.cu:286-447
+ *   glass voxels       MoveToFirstBoundary    CUDAMCFLtransport.cu:702-847
+ *   boundaries         Reflect                CUDAMCFLtransport.cu:628-700
+ *   scattering         Spin                   CUDAMCFLtransport.cu:585-625
+ *   roulette           PhotonSurvive          CUDAMCFLtransport.cu:850-864
+ *   random numbers     rand_MWC_co/oc         CUDAMCFLrng.cu:17-29
+ *
+ * What is designed for the GPU instead of translated:
+ *   - persistent threads draw photon tickets from one 64-bit counter, one
+ *     warp-aggregated atomic per refill, instead of relaunching a fixed
+ *     32768-thread grid from a host loop that copies 128 KB of flags back per
+ *     launch (CUDAMCFLmain.cu:125-165);
+ *   - each photon owns an MWC stream derived from (job key, photon index):
+ *     results do not depend on the schedule, so any batch or slice of a batch
+ *     reproduces the same tallies;
+ *   - a job table lets one launch carry many sources, media and budgets; a
+ *     step budget per launch lets a server slot new jobs in between slices
+ *     while photons in flight are parked in HBM;
+ *   - labels are uint8 in HBM (L2-resident: 4 MB for 200x200x100 voxels);
+ *     the optical properties of the photon's current label live in registers
+ *     and are reloaded (one 16-byte L1 load) only when the label changes;
+ *   - the photon-hitting-density tally is run-length aggregated per thread:
+ *     successive passes in the same voxel add up in a register and reach HBM
+ *     as one 64-bit atomic;
+ *   - per-job weight accounting (absorbed, left at each face, roulette) for
+ *     an exact integer energy balance.
+ */
+#include <float.h>
+#include <stdint.h>
+
+#include "engine_types.h"
+#include "portable_math.h"
+
+#if MCFL_EXACT_MATH
+#define MCFL_LOGF(x) mcfl_plogf(x)
+#define MCFL_SINCOSF(x, s, c) mcfl_psincosf((x), (s), (c))
+#define MCFL_COSF(x) mcfl_pcosf(x)
+#define MCFL_RSQRTF(x) (1.0f / sqrtf(x))
+#define MCFL_KERNEL_NAME mcfl_transport_exact
+#define MCFL_LAUNCHER mcfl_launch_transport_exact
+#define MCFL_ATTR_FN mcfl_attr_transport_exact
+#else
+#define MCFL_LOGF(x) __logf(x)
+#define MCFL_SINCOSF(x, s, c) __sincosf((x), (s), (c))
+#define MCFL_COSF(x) __cosf(x)
+#define MCFL_RSQRTF(x) rsqrtf(x)
+#define MCFL_KERNEL_NAME mcfl_transport_fast
+#define MCFL_LAUNCHER mcfl_launch_transport_fast
+#define MCFL_ATTR_FN mcfl_attr_transport_fast
+#endif
+
+namespace {
+
+constexpr float kPi = 3.141592654f;        /* CUDAMCFL.h:22 */
+constexpr uint32_t kWeightRoulette = 429497u; /* CUDAMCFL.h:33 */
+constexpr float kChance = 0.1f;            /* CUDAMCFL.h:34 */
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kEv = 6; /* event counters kept in shared memory: EXIT_TOP .. CAPPED */
+
+struct Rng {
+  uint64_t x;
+  uint32_t a;
+  __device__ __forceinline__ float co() {
+    x = (uint64_t)(uint32_t)x * a + (x >> 32);
+    return __uint2float_rz((uint32_t)x) * 0x1p-32f;
+  }
+  __device__ __forceinline__ float oc() { return 1.0f - co(); }
+};
+
+struct Photon {
+  float x, y, z, dx, dy, dz;
+  uint32_t weight, label;
+};
+
+/* The current job's medium, held in registers. */
+struct Med {
+  const uint8_t *labels;
+  const float4 *prop;
+  unsigned long long *fhd;
+  float hx, hy, esp, gx, gy, gz;
+  uint32_t nx, ny, total, last;
+};
+
+__device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
+  m.labels = (const uint8_t *)__ldg((const unsigned long long *)&J->labels);
+  m.prop = (const float4 *)__ldg((const unsigned long long *)&J->prop);
+  m.fhd = __ldg(&J->fhd_on) ? (unsigned long long *)__ldg((const unsigned long long *)&J->fhd) : nullptr;
+  m.hx = __ldg(&J->hx);
+  m.hy = __ldg(&J->hy);
+  m.esp = __ldg(&J->esp);
+  m.gx = __ldg(&J->gx);
+  m.gy = __ldg(&J->gy);
+  m.gz = __ldg(&J->gz);
+  m.nx = __ldg(&J->nx);
+  m.ny = __ldg(&J->ny);
+  m.total = __ldg(&J->total);
+  m.last = __ldg(&J->last_label);
+}
+
+__device__ __forceinline__ float4 load_prop(const Med &m, uint32_t label) { return __ldg(&m.prop[label]); }
+
+__device__ __forceinline__ uint32_t voxel_index(const Med &m, float x, float y, float z) {
+  uint32_t i = __float2uint_rz((x + m.hx) * m.gx) +
+               m.nx * (__float2uint_rz((y + m.hy) * m.gy) + m.ny * __float2uint_rz(z * m.gz));
+  return i < m.total ? i : m.total - 1u;
+}
+
+__device__ __forceinline__ uint32_t start_label(const Med &m, const Photon &p) {
+  if (p.z < m.esp) {
+    if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy) return (uint32_t)m.labels[voxel_index(m, p.x, p.y, p.z)];
+    return 1u;
+  }
+  return m.last;
+}
+
+/* Locates the job owning global ticket t (jobs sorted by ticket_begin). */
+__device__ __forceinline__ uint32_t find_job(const McflLaunch &L, uint64_t t) {
+  uint32_t lo = 0, hi = L.n_jobs - 1;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi + 1) >> 1;
+    if (__ldg((const unsigned long long *)&L.jobs[mid].ticket_begin) <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  const McflJob *J = &L.jobs[lo];
+  const uint64_t b = __ldg((const unsigned long long *)&J->ticket_begin);
+  const uint64_t n = __ldg((const unsigned long long *)&J->photons);
+  return (t >= b && t - b < n) ? lo : 0xffffffffu;
+}
+
+__device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,
+                                              Photon &p, Rng &r, uint32_t &src_idx) {
+  mcfl_photon_stream(__ldg((const unsigned long long *)&J->key),
+                     __ldg((const unsigned long long *)&J->rng_offset) + k, mult, &r.x, &r.a);
+  const uint32_t kind = __ldg(&J->src_kind);
+  if (kind == MCFL_SRC_VOXELS) {
+    const uint32_t per = __ldg(&J->per_voxel);
+    src_idx = (uint32_t)(k / per);
+    const uint32_t v = __ldg(&J->src_vox[src_idx]);
+    const uint32_t ix = v % m.nx, iy = (v / m.nx) % m.ny, iz = v / (m.nx * m.ny);
+    const float xi = ((float)ix / m.gx) - m.hx;
+    const float yi = ((float)iy / m.gy) - m.hy;
+    const float zi = ((float)iz / m.gz);
+    p.x = xi + (0.999999f / m.gx) * r.oc();
+    p.y = yi + (0.999999f / m.gy) * r.oc();
+    p.z = zi + (0.999999f / m.gz) * r.oc();
+    const float costheta = (float)(1.0 - 2.0 * (double)r.oc());
+    const float sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
+    const float psi = (float)(2.0 * (double)kPi * (double)r.oc());
+    const float cospsi = MCFL_COSF(psi);
+    float sinpsi = __fsqrt_rn((float)(1.0 - (double)(cospsi * cospsi)));
+    if (!(psi < kPi)) sinpsi = -sinpsi;
+    p.dx = sintheta * cospsi;
+    p.dy = sintheta * sinpsi;
+    p.dz = costheta;
+    p.weight = 0xFFFFFFFFu;
+  } else if (kind == MCFL_SRC_WIDEFIELD) {
+    p.x = __ldg(&J->sx) + (r.co() - 0.5f) * __ldg(&J->src_w);
+    p.y = __ldg(&J->sy) + (r.co() - 0.5f) * __ldg(&J->src_h);
+    p.z = __ldg(&J->sz);
+    p.dx = 0.0f;
+    p.dy = 0.0f;
+    p.dz = 1.0f;
+    p.weight = __ldg(&J->start_weight);
+  } else {
+    const float input_fibre_diameter = 0.03f;
+    const float sample_rad = input_fibre_diameter * __fsqrt_rn(-MCFL_LOGF(r.oc()));
+    const float sample_phi = 2 * kPi * r.oc();
+    float sin_phi, cos_phi;
+    MCFL_SINCOSF(sample_phi, &sin_phi, &cos_phi);
+    p.x = __ldg(&J->sx) + sample_rad * cos_phi;
+    p.y = __ldg(&J->sy) + sample_rad * sin_phi;
+    p.z = __ldg(&J->sz);
+    p.dx = 0.0f;
+    p.dy = 0.0f;
+    p.dz = 1.0f;
+    p.weight = __ldg(&J->start_weight);
+  }
+  p.label = start_label(m, p);
+}
+
+__device__ __forceinline__ void spin(Photon &p, float g, Rng &r) {
+  float cost, sint, cosp, sinp, temp;
+  const float tempdir = p.dx;
+  temp = (1.0f - g * g) / (1.0f - g + 2.0f * g * r.co());
+  cost = (1.0f + g * g - temp * temp) / (2.0f * g);
+  if (g == 0.0f) cost = 2.0f * r.co() - 1.0f;
+  sint = sqrtf(1.0f - cost * cost);
+  /* sin goes to cosp and cos to sinp, as in CUDAMCFLtransport.cu:603 */
+  MCFL_SINCOSF(2.0f * kPi * r.co(), &cosp, &sinp);
+  temp = sqrtf(1.0f - p.dz * p.dz);
+  if (temp == 0.0f) {
+    p.dx = sint * cosp;
+    p.dy = sint * sinp;
+    p.dz = copysignf(cost, p.dz * cost);
+  } else {
+    p.dx = (sint * (p.dx * p.dz * cosp - p.dy * sinp)) / temp + p.dx * cost;
+    p.dy = (sint * (p.dy * p.dz * cosp + tempdir * sinp)) / temp + p.dy * cost;
+    p.dz = -sint * cosp * temp + p.dz * cost;
+  }
+  temp = MCFL_RSQRTF(p.dx * p.dx + p.dy * p.dy + p.dz * p.dz);
+  p.dx = p.dx * temp;
+  p.dy = p.dy * temp;
+  p.dz = p.dz * temp;
+}
+
+/* Fresnel reflection / refraction with z as the interface normal.  On
+ * transmission the label and the cached properties change. */
+__device__ __forceinline__ void reflect(Photon &p, uint32_t newlb, Rng &r, const Med &m, float4 &pr) {
+  const float n1 = pr.w;
+  const float4 pn = load_prop(m, newlb);
+  const float n2 = pn.w;
+  float rr;
+  const float cos_angle_i = fabsf(p.dz);
+  if (n1 == n2) {
+    p.label = newlb;
+    pr = pn;
+    return;
+  }
+  if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
+    p.dz *= -1.0f;
+    return;
+  }
+  if (cos_angle_i == 1.0f) {
+    rr = (n1 - n2) / (n1 + n2);
+    if (r.co() <= rr * rr) {
+      p.dz *= -1.0f;
+    } else {
+      p.label = newlb;
+      pr = pn;
+    }
+    return;
+  }
+  float e = (n1 * n1) / (n2 * n2) * (1.0f - cos_angle_i * cos_angle_i);
+  rr = 2 * sqrtf((1.0f - cos_angle_i * cos_angle_i) * (1.0f - e) * e * cos_angle_i * cos_angle_i);
+  e = e + (cos_angle_i * cos_angle_i) * (1.0f - 2.0f * e);
+  rr = e * ((1.0f - e - rr) / ((1.0f - e + rr) * (e + rr)));
+  if (r.co() <= rr) {
+    p.dz *= -1.0f;
+    return;
+  }
+  rr = n1 / n2;
+  e = rr * rr * (1.0f - cos_angle_i * cos_angle_i);
+  p.dx *= rr;
+  p.dy *= rr;
+  p.dz = copysignf(sqrtf(1 - e), p.dz);
+  p.label = newlb;
+  pr = pn;
+}
+
+/* Scattering-free voxels: march in half-voxel steps to the next label, then
+ * back-project onto the sphere of radius 0.707 voxel around the centre of the
+ * voxel reached.  The march is bounded by max_s. */
+__device__ __noinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, float max_s) {
+  float search_step = 1 / (2 * m.gx);
+  float total_move = 0;
+  int index = 1;
+  const uint32_t old_bulk = p.label;
+  uint32_t present_bulk = old_bulk;
+  while (present_bulk == old_bulk && total_move < max_s) {
+    p.x += p.dx * search_step;
+    p.y += p.dy * search_step;
+    p.z += p.dz * search_step;
+    if (p.z + p.dz * search_step < 0.0f) {
+      present_bulk = 0;
+      index = -1;
+      search_step = (-p.z) / p.dz;
+    } else if (p.z + p.dz * search_step > m.esp) {
+      present_bulk = m.last;
+      index = -1;
+      search_step = (m.esp - p.z) / p.dz;
+    } else if (fabsf(p.x + p.dx * search_step) >= m.hx || fabsf(p.y + p.dy * search_step) >= m.hy) {
+      present_bulk = 1;
+      index = -1;
+    } else {
+      index = (int)voxel_index(m, p.x, p.y, p.z);
+      present_bulk = (uint32_t)m.labels[index];
+    }
+    total_move += search_step;
+  }
+  if (index >= 0 && present_bulk != old_bulk) {
+    uint32_t uidx = (uint32_t)index;
+    const uint32_t z_grid = uidx / (m.nx * m.ny);
+    uidx -= z_grid * m.nx * m.ny;
+    const uint32_t y_grid = uidx / m.nx;
+    const uint32_t x_grid = uidx % m.nx;
+    const double half = 1. / (2. * (double)m.gx);
+    const float y_voxel = (float)((double)(__int2float_rn((int)y_grid) / m.gy - m.hy) + half);
+    const float x_voxel = (float)((double)(__int2float_rn((int)x_grid) / m.gx - m.hx) + half);
+    const float z_voxel = (float)((double)(__int2float_rn((int)z_grid) / m.gz) + half);
+    const double rv = 0.707107 * (double)(1 / m.gx);
+    const float r_voxel2 = (float)(rv * rv);
+    const float pow_dx = p.dx * p.dx, pow_dy = p.dy * p.dy, pow_dz = p.dz * p.dz;
+    const float pow_px = p.x * p.x, pow_py = p.y * p.y, pow_pz = p.z * p.z;
+    const float pow_cx = x_voxel * x_voxel, pow_cy = y_voxel * y_voxel, pow_cz = z_voxel * z_voxel;
+    const float disc =
+        2 * x_voxel * y_voxel * p.dx * p.dy - (pow_cy + pow_cz) * pow_dx - (pow_cx + pow_cz) * pow_dy -
+        (pow_cx + pow_cy) * pow_dz - (pow_dy + pow_dz) * pow_px - (pow_dx + pow_dz) * pow_py -
+        (pow_dx + pow_dy) * pow_pz + (pow_dx + pow_dy + pow_dz) * r_voxel2 +
+        2 * (x_voxel * z_voxel * p.dx + y_voxel * z_voxel * p.dy) * p.dz -
+        2 * (y_voxel * p.dx * p.dy - x_voxel * pow_dy + z_voxel * p.dx * p.dz - x_voxel * pow_dz) * p.x +
+        2 * (y_voxel * pow_dx - x_voxel * p.dx * p.dy - z_voxel * p.dy * p.dz + y_voxel * pow_dz + p.dx * p.dy * p.x) *
+            p.y +
+        2 * (z_voxel * pow_dx + z_voxel * pow_dy + p.dx * p.dz * p.x + p.dy * p.dz * p.y -
+             (x_voxel * p.dx + y_voxel * p.dy) * p.dz) * p.z;
+    const float root = sqrtf(disc);
+    const float lin = x_voxel * p.dx + y_voxel * p.dy + z_voxel * p.dz - p.dx * p.x - p.dy * p.y - p.dz * p.z;
+    const float den = pow_dx + pow_dy + pow_dz;
+    const float back_step1 = -(lin + root) / den;
+    const float back_step2 = -(lin - root) / den;
+    const float npx1 = p.x - p.dx * back_step1, npy1 = p.y - p.dy * back_step1, npz1 = p.z - p.dz * back_step1;
+    const float npx2 = p.x - p.dx * back_step2, npy2 = p.y - p.dy * back_step2, npz2 = p.z - p.dz * back_step2;
+    if (((npx1 - x_voxel) * (npx1 - x_voxel) + (npy1 - y_voxel) * (npy1 - y_voxel) +
+         (npz1 - z_voxel) * (npz1 - z_voxel)) <
+        ((npx2 - x_voxel) * (npx2 - x_voxel) + (npy2 - y_voxel) * (npy2 - y_voxel) +
+         (npz2 - z_voxel) * (npz2 - z_voxel))) {
+      p.x = npx1; p.y = npy1; p.z = npz1;
+    } else {
+      p.x = npx2; p.y = npy2; p.z = npz2;
+    }
+  }
+  return present_bulk;
+}
+
+/* 128-bit accumulate of weight x q: low word with carry detection. */
+__device__ __forceinline__ void add128(unsigned long long *acc, uint32_t w, uint64_t q) {
+  const uint64_t lo = (uint64_t)w * (uint32_t)q;
+  const uint64_t mid = (uint64_t)w * (uint32_t)(q >> 32);
+  const uint64_t plo = lo + (mid << 32);
+  const uint64_t phi = (mid >> 32) + (plo < lo ? 1u : 0u);
+  const unsigned long long old = atomicAdd(&acc[0], (unsigned long long)plo);
+  const uint64_t carry = (old + plo < old) ? 1u : 0u;
+  if (phi + carry) atomicAdd(&acc[1], (unsigned long long)(phi + carry));
+}
+
+/* Exit through a face: image tally when the exit point is inside the
+ * detector.  top: R (z = 0), else T (z = esp). */
+__device__ __noinline__ void tally_exit(const McflJob *J, const Photon &p, bool top, uint32_t src_idx) {
+  const float x0 = __ldg(&J->det_x0), y0 = __ldg(&J->det_y0);
+  const float size_x = __ldg(&J->size_x), size_y = __ldg(&J->size_y);
+  if (!(fabsf(p.x - x0) < size_x && fabsf(p.y - y0) < size_y)) return;
+  uint32_t idx = __float2uint_rz((p.y - y0 + size_y) / __ldg(&J->det_dy)) * __ldg(&J->det_nx) +
+                 __float2uint_rz((p.x - x0 + size_x) / __ldg(&J->det_dx));
+  const uint32_t xy = __ldg(&J->xy_size);
+  if (idx >= xy) idx = xy - 1u;
+  if (__ldg(&J->src_kind) == MCFL_SRC_VOXELS) {
+    unsigned long long *img =
+        (unsigned long long *)__ldg((const unsigned long long *)(top ? &J->R128 : &J->T128));
+    add128(&img[2 * (size_t)idx], p.weight, __ldg((const unsigned long long *)&J->src_q[src_idx]));
+  } else {
+    unsigned long long *img = (unsigned long long *)__ldg((const unsigned long long *)(top ? &J->R : &J->T));
+    atomicAdd(&img[idx], (unsigned long long)p.weight);
+  }
+}
+
+} // namespace
+
+/* One warp-synchronous persistent loop per thread; see the file comment. */
+extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
+  extern __shared__ unsigned long long s_ev[]; /* kEv x blockDim.x */
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned tib = threadIdx.x;
+  const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (int e = 0; e < kEv; ++e) s_ev[e * blockDim.x + tib] = 0ull;
+
+  const uint64_t ticket_end = L.ticket_end_dev ? *L.ticket_end_dev : L.ticket_end;
+  bool alive = false, exhausted = false;
+  Photon p;
+  Rng r;
+  Med m = {};
+  float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, done = 0;
+  uint64_t k = 0, steps = 0, absorbed = 0;
+  uint32_t f_idx = 0xffffffffu;
+  unsigned long long f_acc = 0ull;
+  const McflJob *J = nullptr;
+
+  auto flush_stats = [&]() {
+    if (J == nullptr) return;
+    unsigned long long *st = (unsigned long long *)__ldg((const unsigned long long *)&J->stats);
+    if (done) atomicAdd(&st[MCFL_ST_DONE], (unsigned long long)done);
+    if (steps) atomicAdd(&st[MCFL_ST_STEPS], (unsigned long long)steps);
+    if (absorbed) atomicAdd(&st[MCFL_ST_ABSORBED], (unsigned long long)absorbed);
+    for (int e = 0; e < kEv; ++e) {
+      unsigned long long v = s_ev[e * blockDim.x + tib];
+      if (v) atomicAdd(&st[MCFL_ST_EXIT_TOP + e], v);
+      s_ev[e * blockDim.x + tib] = 0ull;
+    }
+    done = 0;
+    steps = 0;
+    absorbed = 0;
+    if (m.fhd && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
+    f_idx = 0xffffffffu;
+    f_acc = 0ull;
+  };
+  auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * blockDim.x + tib] += v; };
+
+  if (L.max_iters && L.saved) {
+    const McflSaved sv = L.saved[gtid];
+    if (sv.alive) {
+      job = sv.job;
+      J = &L.jobs[job];
+      load_med(J, m);
+      p = Photon{sv.x, sv.y, sv.z, sv.dx, sv.dy, sv.dz, sv.weight, sv.label};
+      r.x = sv.rng_x;
+      r.a = sv.rng_a;
+      k = sv.k;
+      pst = sv.steps;
+      src_idx = sv.src_idx;
+      pr = load_prop(m, p.label);
+      alive = true;
+    }
+  }
+
+  for (uint32_t it = 0;; ++it) {
+    if (L.max_iters && it >= L.max_iters) break;
+    const bool need = !alive && !exhausted;
+    const unsigned nm = __ballot_sync(kFull, need);
+    if (nm) {
+      const int leader = __ffs(nm) - 1;
+      unsigned long long base = 0ull;
+      if ((int)lane == leader) base = atomicAdd(L.ticket_counter, (unsigned long long)__popc(nm));
+      base = __shfl_sync(kFull, base, leader);
+      if (need) {
+        const uint64_t t = base + (uint64_t)__popc(nm & ((1u << lane) - 1u));
+        if (t < ticket_end) {
+          const uint32_t j = find_job(L, t);
+          if (j != 0xffffffffu) {
+            if (j != job) {
+              flush_stats();
+              job = j;
+              J = &L.jobs[j];
+              load_med(J, m);
+            }
+            k = t - __ldg((const unsigned long long *)&J->ticket_begin);
+            launch_photon(J, m, k, L.mult, p, r, src_idx);
+            pr = load_prop(m, p.label);
+            pst = 0;
+            alive = true;
+          }
+        } else {
+          exhausted = true;
+        }
+      }
+    }
+    if (__all_sync(kFull, !alive)) break;
+    if (!alive) continue;
+
+    /* ---- one transport pass (MCd3D loop body) ---- */
+    ++steps;
+    ++pst;
+    float s;
+    uint32_t new_bulk;
+    if (pr.x != FLT_MAX) {
+      s = -MCFL_LOGF(r.oc()) * pr.x;
+      new_bulk = p.label;
+      if (p.z + s * p.dz < 0.0f) {
+        new_bulk = 0;
+        s = (-p.z) / p.dz;
+      }
+      if (p.z + s * p.dz > m.esp) {
+        new_bulk = m.last;
+        s = (m.esp - p.z) / p.dz;
+      }
+      p.x += p.dx * s;
+      p.y += p.dy * s;
+      p.z += p.dz * s;
+      if (new_bulk != 0u && new_bulk != m.last) {
+        if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp)
+          new_bulk = (uint32_t)m.labels[voxel_index(m, p.x, p.y, p.z)];
+        else
+          new_bulk = 1u;
+      }
+    } else {
+      s = 100.0f;
+      new_bulk = move_to_first_boundary(p, m, s);
+    }
+    if (new_bulk != p.label) reflect(p, new_bulk, r, m, pr);
+    if (m.fhd && fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp) {
+      const uint32_t fi = voxel_index(m, p.x, p.y, p.z);
+      if (fi != f_idx) {
+        if (f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
+        f_idx = fi;
+        f_acc = 0ull;
+      }
+      f_acc += p.weight;
+    }
+    if (p.label == 0u || p.label == m.last) {
+      const bool top = p.label == 0u;
+      tally_exit(J, p, top, src_idx);
+      ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+      p.weight = 0u;
+      s = 0.0f;
+    }
+    if (s > 0.0f) {
+      const uint32_t w = __float2uint_ru(pr.y * pr.x * __uint2float_rn(p.weight));
+      if (w > 0u) {
+        p.weight -= w;
+        absorbed += w;
+      } else {
+        ev_add(MCFL_ST_W0_LOSS, p.weight);
+        p.weight = 0u;
+      }
+      spin(p, pr.z, r);
+    }
+    /* PhotonSurvive */
+    if (p.weight <= kWeightRoulette) {
+      if (p.weight == 0u) {
+        alive = false;
+      } else if (r.co() < kChance) {
+        const uint32_t w0 = p.weight;
+        p.weight = __float2uint_rn(__uint2float_rn(p.weight) / kChance);
+        ev_add(MCFL_ST_R_GAIN, (unsigned long long)(p.weight - w0));
+      } else {
+        ev_add(MCFL_ST_R_LOSS, p.weight);
+        alive = false;
+      }
+    }
+    if (alive && pst >= L.step_cap) {
+      ev_add(MCFL_ST_CAPPED, 1ull);
+      alive = false;
+    }
+    if (!alive) ++done;
+  }
+
+  if (L.max_iters && L.saved) {
+    McflSaved sv;
+    sv.alive = alive ? 1u : 0u;
+    if (alive) {
+      sv.x = p.x; sv.y = p.y; sv.z = p.z; sv.dx = p.dx; sv.dy = p.dy; sv.dz = p.dz;
+      sv.weight = p.weight;
+      sv.label = p.label;
+      sv.rng_x = r.x;
+      sv.rng_a = r.a;
+      sv.job = job;
+      sv.k = k;
+      sv.steps = pst;
+      sv.src_idx = src_idx;
+    }
+    L.saved[gtid] = sv;
+  }
+  flush_stats();
+}
+
+extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, cudaStream_t stream) {
+  const size_t smem = (size_t)kEv * block * sizeof(unsigned long long);
+  MCFL_KERNEL_NAME<<<grid, block, smem, stream>>>(*L);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t MCFL_ATTR_FN(int block, int *blocks_per_sm, int *regs) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME);
+  if (e != cudaSuccess) return e;
+  if (regs) *regs = a.numRegs;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME, block,
+                                                       (size_t)kEv * block * sizeof(unsigned long long));
+}

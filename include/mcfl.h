@@ -1,0 +1,287 @@
+/*
+ * mcfl.h — C ABI of the GB300 photon-transport engine for voxelized
+ * fluorescent turbid media (libmcfl.so).
+ *
+ * Two layers:
+ *
+ *  1. The reference's own host interface, as a drop-in.  CUDAMCFL has no
+ *     plugin or FFI layer; its boundary is the cuda_fl executable with its
+ *     .mci/bulk/output files, and the host routines of CUDAMCFLmain.cu and
+ *     CUDAMCFLio.cu.  Each function below names the reference routine it
+ *     replaces (file:line in the CUDAMCFL sources).
+ *
+ *  2. The engine: device-resident media, runs, batches of many sources in
+ *     one persistent launch, and a continuous-batching server.
+ *
+ * Conventions: functions return an int status (MCFL_OK = 0, negative on
+ * error) unless stated otherwise; mcfl_last_error() gives the message of the
+ * last failure on the calling thread.  The library never prints and never
+ * exits.  Buffers are caller-owned.  Images hold nx + nx*ny entries like the
+ * reference's (CUDAMCFLmem.cu:113); entry y*nx + x is pixel (x, y).
+ */
+#ifndef MCFL_H
+#define MCFL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  MCFL_OK = 0,
+  MCFL_E_ARG = -1,     /* invalid argument */
+  MCFL_E_CUDA = -2,    /* CUDA runtime error, or no usable GPU */
+  MCFL_E_IO = -3,      /* file could not be opened or written */
+  MCFL_E_PARSE = -4,   /* malformed .mci or bulk file */
+  MCFL_E_NOMEM = -5,   /* host or device allocation failed */
+  MCFL_E_STATE = -6,   /* call not valid in the current state */
+  MCFL_E_RANGE = -7,   /* size beyond a supported limit */
+  MCFL_E_BUSY = -8,    /* server full: retry later */
+  MCFL_E_TIMEOUT = -9, /* wait timed out */
+  MCFL_E_CAPPED = -10  /* photons stopped by the per-photon pass cap */
+};
+
+#define MCFL_STR_LEN 500
+#define MCFL_MAX_BULKS 253
+
+/* ---------------------------------------------------------------------- */
+/* Reference data types                                                    */
+/* ---------------------------------------------------------------------- */
+
+/* BulkStruct, CUDAMCFL.h:116-127.  Entry 0 is the medium above the slab,
+ * entry n_bulks+1 the medium below; mutr = 1/(mua + mus) or FLT_MAX when
+ * mus = 0.  mua is the excitation absorption (mua + flc*AbsCExi), muaf the
+ * emission absorption (mua + flc*AbsCEmi), albedof = mus/(flc*AbsCExi + mus). */
+typedef struct mcfl_bulk {
+  float mutr, mua, g, n, flc, muaf, eY, albedof;
+} mcfl_bulk;
+
+/* LayerStruct, CUDAMCFL.h:38-52 (bulk method 1). */
+typedef struct mcfl_layer {
+  float z_min, z_max, mutr, mua, g, n, flc, muaf, eY, albedof;
+} mcfl_layer;
+
+/* IncStruct, CUDAMCFL.h:98-114 (bulk method 1). */
+typedef struct mcfl_inclusion {
+  float x, y, z, r, mutr, mua, g, n, flc, muaf, eY, albedof;
+} mcfl_inclusion;
+
+/* DetStruct, CUDAMCFL.h:71-96. */
+typedef struct mcfl_det {
+  float dx, dy, dz;
+  int nx, ny, nz;
+  float x0, y0, sep;
+  float x0_temp_det, y0_temp_det;
+  unsigned int x_temp_numdets, y_temp_numdets;
+  float x_temp_sepdets, y_temp_sepdets, temp_det_r;
+  unsigned int temp_rort;
+  unsigned long temp_bins, max_temp;
+} mcfl_det;
+
+/* SimulationStruct, CUDAMCFL.h:129-170.  bulk_info holds one uint8 label
+ * per voxel (the reference stores short; its parser only produces 0-9). */
+typedef struct mcfl_simulation {
+  unsigned long long number_of_photons;
+  unsigned int number_of_photons_per_voxel;
+  unsigned int n_layers;
+  unsigned int n_bulks;
+  unsigned int start_weight;
+  char outp_filename[MCFL_STR_LEN];
+  char inp_filename[MCFL_STR_LEN];
+  long begin, end;
+  char AorB;
+  mcfl_det det;
+  mcfl_layer *layers;
+  mcfl_bulk *bulks;
+  mcfl_inclusion inclusion;
+  int grid_size;
+  float esp;
+  float xi, yi, zi, dir;
+  float n_down;
+  int fhd_activated;
+  int do_fl_sim;
+  int bulk_method;
+  unsigned char *bulk_info;
+  char bulkinfo_filename[MCFL_STR_LEN];
+  int do_temp_sim;
+  /* not in the reference: grid size as the transport computes it, and the
+   * number of labels the bulk file held */
+  int num_x, num_y, num_z;
+  long long bulk_values_read;
+} mcfl_simulation;
+
+/* ---------------------------------------------------------------------- */
+/* Reference host interface (drop-in)                                      */
+/* ---------------------------------------------------------------------- */
+
+/* read_simulation_data, CUDAMCFLio.cu:243-659: parses a .mci file (and the
+ * bulk matrix it names, relative to the working directory) into a malloc'ed
+ * array.  Returns the number of simulations read, 0 on failure. */
+int mcfl_read_simulation_data(const char *filename, mcfl_simulation **simulations, int ignoreAdetection);
+
+/* FreeSimulationStruct, CUDAMCFLmem.cu:219-223. */
+void mcfl_free_simulation_struct(mcfl_simulation *simulations, int n_simulations);
+
+/* interpret_arg, CUDAMCFLio.cu:30-55: "-S<seed>" and "-A".  Returns 0, or 1
+ * on an unknown argument. */
+int mcfl_interpret_arg(int argc, char *argv[], unsigned long long *seed, int *ignoreAdetection);
+
+/* init_RNG, CUDAMCFLrng.cu:31-90: per-stream MWC states and multipliers
+ * from a multiplier file.  Returns 0 on success, 1 on failure (as the
+ * reference). */
+int mcfl_init_RNG(unsigned long long *x, unsigned int *a, unsigned int n_rng, const char *safeprimes_file,
+                  unsigned long long xinit);
+
+/* Writes a multiplier file in the format init_RNG reads (the reference does
+ * not ship safeprimes_base32.txt): count lines of "a hi lo", a descending
+ * from 2^32-1 with a*2^32-1 and a*2^31-1 prime. */
+int mcfl_write_safeprimes(const char *path, unsigned int count);
+
+/* DoOneSimulation, CUDAMCFLmain.cu:60-193: excitation run of the .mci's
+ * photons with the photon hitting density, on the GPU.  The reference takes
+ * per-thread RNG arrays x/a; the engine derives one stream per photon from
+ * seed instead.  fhd_out (num_x*num_y*num_z, normalised per photon as
+ * CUDAMCFLmain.cu:181-183), Rd_out/Tt_out (raw, det.nx + det.nx*det.ny) may
+ * be NULL.  Returns the photons finished, 0 on failure. */
+unsigned long long mcfl_DoOneSimulation(const mcfl_simulation *simulation, unsigned long long seed, double *fhd_out,
+                                        unsigned long long *Rd_out, unsigned long long *Tt_out);
+
+/* DoOneSimulationFl, CUDAMCFLmain.cu:196-288: one emission run of
+ * number_of_photons_per_voxel photons from the voxel whose corner is
+ * (xi, yi, zi), isotropic, emission absorption.  Raw R/T images.  Returns
+ * the photons finished, 0 on failure. */
+unsigned long long mcfl_DoOneSimulationFl(const mcfl_simulation *simulation, unsigned long long seed,
+                                          unsigned long long *tempvoxelR, unsigned long long *tempvoxelT);
+
+/* Write_Simulation_Results, CUDAMCFLio.cu:57-191: <out>_param.dat,
+ * <out>_Trans.dat, <out>_Refl.dat from raw excitation images. */
+int mcfl_Write_Simulation_Results(const mcfl_simulation *sim, const unsigned long long *Rd_xy,
+                                  const unsigned long long *Tt_xy, double simulation_time_s);
+
+/* The PHD dump of CUDAMCFLmain.cu:368-392 (<out>_PHD-Ascii.dat). */
+int mcfl_write_phd(const mcfl_simulation *sim, const double *fhd);
+
+/* The emission images of CUDAMCFLmain.cu:604-647 (<out>_FlR.dat, _FlT.dat). */
+int mcfl_write_fl_images(const mcfl_simulation *sim, const double *flR, const double *flT);
+
+/* main, CUDAMCFLmain.cu:290-668: the whole two-phase run of a .mci file
+ * (bulk method 2) with every output file the reference writes, both phases
+ * seeded from seed (the reference seeds its emission phase from time(NULL),
+ * CUDAMCFLmain.cu:412).  Paths resolve against the working directory, as the
+ * reference's do. */
+int mcfl_run_mci(const char *mci_path, unsigned long long seed);
+
+/* ---------------------------------------------------------------------- */
+/* Engine                                                                   */
+/* ---------------------------------------------------------------------- */
+
+typedef struct mcfl_ctx mcfl_ctx;
+typedef struct mcfl_medium mcfl_medium;
+
+/* Kernel numerics. */
+enum {
+  MCFL_MATH_EXACT = 0, /* IEEE single precision, bit-identical to the CPU oracle */
+  MCFL_MATH_FAST = 1   /* hardware SFU intrinsics (the reference's GPU numerics) */
+};
+
+/* Source kinds. */
+enum {
+  MCFL_SOURCE_GAUSS_BEAM = 1, /* the reference's collimated source: radius 0.03 sqrt(-ln u) cm, +z */
+  MCFL_SOURCE_WIDEFIELD = 3   /* collimated, uniform over width x height centred on (x, y) */
+};
+
+typedef struct mcfl_source {
+  int kind;
+  float x, y, z;
+  float width, height;
+} mcfl_source;
+
+/* Voxel grid in the reference's frame: |x| < half_x, |y| < half_y,
+ * 0 <= z < thickness; voxel (ix, iy, iz) at index ix + nx*(iy + ny*iz). */
+typedef struct mcfl_medium_desc {
+  int nx, ny, nz;
+  float half_x, half_y, thickness;
+  float vox_per_cm[3];          /* inverse voxel sizes */
+  const unsigned char *labels;  /* host, nx*ny*nz */
+  const float *fluor_map;       /* optional per-voxel emission-strength factor (host, nx*ny*nz), or NULL */
+  int n_bulks;                  /* labels 1..n_bulks; 0 above, n_bulks+1 below */
+  const mcfl_bulk *bulks;       /* n_bulks + 2 entries */
+} mcfl_medium_desc;
+
+typedef struct mcfl_detector {
+  float x0, y0, dx, dy;
+  int nx, ny;
+} mcfl_detector;
+
+/* One two-phase run: excitation from a source, optionally the photon
+ * hitting density, optionally the emission phase (photons_per_voxel photons
+ * from every voxel whose label has albedof < 1 and whose weight
+ * eY (1 - albedof) PHD * fluor_map is non-zero). */
+typedef struct mcfl_run_desc {
+  unsigned long long photons;
+  unsigned int photons_per_voxel; /* 0: no emission phase */
+  int fluence;                    /* 1: tally the photon hitting density (forced on for emission) */
+  unsigned long long seed_exc, seed_fl;
+  unsigned int start_weight;      /* 0: (2^32-1)(1 - R_specular) from n of labels 0 and 1 */
+  mcfl_source source;
+  mcfl_detector det;
+} mcfl_run_desc;
+
+#define MCFL_NSTATS 9
+/* stats[]: photons done, passes, absorbed, left at z=0, left at z=esp,
+ * roulette loss, roulette gain, zero-drop loss, capped photons (weights in
+ * units of 2^-32 of one photon). */
+
+/* Results of a run.  Every pointer may be NULL; sizes in the comments. */
+typedef struct mcfl_run_out {
+  unsigned long long *Rd, *Tt;       /* raw excitation images (det nx + nx*ny) */
+  double *R, *T;                     /* normalised: Rd/((2^32-1) N dx dy) */
+  unsigned long long *fhd;           /* raw photon hitting density (voxels) */
+  double *phd;                       /* fhd/((2^32-1) N) */
+  double *flR, *flT;                 /* emission images, reference normalisation */
+  unsigned long long *flR128, *flT128; /* raw emission accumulators, (lo, hi) per pixel */
+  unsigned long long stats_exc[MCFL_NSTATS], stats_fl[MCFL_NSTATS];
+  unsigned long long photons_fl;     /* emission photons */
+  long long fl_voxels;               /* emitting voxels */
+  double energy_exc[4];              /* R_all, T_all, absorbed, residual as fractions of the launched weight */
+  float ms_exc, ms_fl;               /* GPU time of the two transport launches */
+} mcfl_run_out;
+
+/* Context on one GPU (device < 0: current device). */
+int mcfl_create(int device, mcfl_ctx **ctx);
+void mcfl_destroy(mcfl_ctx *ctx);
+const char *mcfl_last_error(void);
+
+/* Options: "math" (MCFL_MATH_*), "block" (threads per block), "blocks_per_sm"
+ * (0 = occupancy maximum), "step_cap" (passes per photon), "l2_window"
+ * (1: persisting L2 access window on the labels and tallies). */
+int mcfl_set_option(mcfl_ctx *ctx, const char *key, long long value);
+long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
+
+/* Uses a caller stream (cudaStream_t) for all work of this context; NULL
+ * restores the context's own stream. */
+int mcfl_set_stream(mcfl_ctx *ctx, void *stream);
+
+/* Uploads a medium; it stays resident until mcfl_medium_free. */
+int mcfl_medium_create(mcfl_ctx *ctx, const mcfl_medium_desc *desc, mcfl_medium **medium);
+void mcfl_medium_free(mcfl_medium *medium);
+size_t mcfl_medium_bytes(const mcfl_medium *medium);
+
+/* Builds the medium of a parsed .mci simulation (bulk method 2). */
+int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_medium **medium);
+
+/* Runs one two-phase simulation and copies the requested results. */
+int mcfl_run(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *run, mcfl_run_out *out);
+
+/* The run description a .mci simulation implies. */
+int mcfl_run_desc_from_simulation(const mcfl_simulation *sim, unsigned long long seed, mcfl_run_desc *run);
+
+/* Kernel launches and GPU time issued by this context so far. */
+unsigned long long mcfl_launch_count(const mcfl_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

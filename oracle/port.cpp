@@ -728,3 +728,36 @@ extern "C" int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipli
   return math_libm ? photon_impl<LibmMath>(sim, multipliers, seed_exc, seed_fl, res)
                    : photon_impl<PortableMath>(sim, multipliers, seed_exc, seed_fl, res);
 }
+
+/* ---------------------------------------------------------- test helpers */
+
+extern "C" float oracle_plogf(float x) { return mcfl_plogf(x); }
+extern "C" void oracle_psincosf(float x, float *s, float *c) { mcfl_psincosf(x, s, c); }
+
+/* The closed-form distances from p along d to the sphere (c, r) that
+ * move_to_first_boundary back-projects with (CUDAMCFLtransport.cu:792-812),
+ * evaluated with the same expression. */
+extern "C" void oracle_sphere_back_steps(const float *pp, const float *dd, const float *cc, float r2, float *out) {
+  const float px = pp[0], py = pp[1], pz = pp[2], dx = dd[0], dy = dd[1], dz = dd[2];
+  const float x_voxel = cc[0], y_voxel = cc[1], z_voxel = cc[2];
+  float pow_dx = dx * dx, pow_dy = dy * dy, pow_dz = dz * dz;
+  float pow_px = px * px, pow_py = py * py, pow_pz = pz * pz;
+  float pow_cx = x_voxel * x_voxel, pow_cy = y_voxel * y_voxel, pow_cz = z_voxel * z_voxel;
+  float disc = 2 * x_voxel * y_voxel * dx * dy - (pow_cy + pow_cz) * pow_dx - (pow_cx + pow_cz) * pow_dy -
+               (pow_cx + pow_cy) * pow_dz - (pow_dy + pow_dz) * pow_px - (pow_dx + pow_dz) * pow_py -
+               (pow_dx + pow_dy) * pow_pz + (pow_dx + pow_dy + pow_dz) * r2 +
+               2 * (x_voxel * z_voxel * dx + y_voxel * z_voxel * dy) * dz -
+               2 * (y_voxel * dx * dy - x_voxel * pow_dy + z_voxel * dx * dz - x_voxel * pow_dz) * px +
+               2 * (y_voxel * pow_dx - x_voxel * dx * dy - z_voxel * dy * dz + y_voxel * pow_dz + dx * dy * px) * py +
+               2 * (z_voxel * pow_dx + z_voxel * pow_dy + dx * dz * px + dy * dz * py -
+                    (x_voxel * dx + y_voxel * dy) * dz) * pz;
+  float root = sqrtf(disc);
+  float lin = x_voxel * dx + y_voxel * dy + z_voxel * dz - dx * px - dy * py - dz * pz;
+  float den = pow_dx + pow_dy + pow_dz;
+  out[0] = -(lin + root) / den;
+  out[1] = -(lin - root) / den;
+}
+
+extern "C" int oracle_init_rng(uint64_t *x, uint32_t *a, unsigned n, const char *path, uint64_t seed) {
+  return init_rng_streams(x, a, n, path, seed);
+}

@@ -308,3 +308,9 @@ extern "C" int ref_parse_mci(const char *mci_path, oracle_sim *out) {
   FreeSimulationStruct(simulations, n_sim);
   return 0;
 }
+
+/* The reference's own init_RNG (CUDAMCFLrng.cu:31-90). */
+extern "C" int ref_init_rng(unsigned long long *x, unsigned int *a, unsigned int n, const char *path,
+                            unsigned long long seed) {
+  return init_RNG(x, a, n, path, seed);
+}

@@ -1,0 +1,155 @@
+"""Small reference-expressible test media (cubic voxels of 1/grid cm, lateral
+extent 4*esp, labels 0-9) shared by the oracle and the GPU tests."""
+from __future__ import annotations
+
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+import cudamcfl_gb300 as mc
+from oracle import pyoracle
+
+
+@dataclass
+class Case:
+    name: str
+    esp: float
+    grid: int
+    labels: np.ndarray       # (nz, ny, nx) uint8
+    columns: list            # .mci columns per label 1..n: (n, mua, mus, flc, AbsCExi, AbsCEmi, eY, g)
+    n_out: float
+    photons: int
+    per_voxel: int
+    det: tuple               # dx, dy, nx, ny, x0, y0
+    source: tuple = (0.0, 0.0, 0.0)
+    do_fl: int = 1
+
+    @property
+    def dims(self):
+        n = int(round(4 * self.esp * self.grid))
+        return n, n, int(round(self.esp * self.grid))
+
+    def bulks(self):
+        b = [mc.outer_bulk(self.n_out)]
+        b += [mc.bulk_from_mci_columns(*c) for c in self.columns]
+        b.append(mc.outer_bulk(self.n_out))
+        return b
+
+    def start_weight(self) -> int:
+        n1 = np.float64(np.float32(self.n_out))
+        n2 = np.float64(np.float32(self.columns[0][0]))
+        r = (n1 - n2) / (n1 + n2)
+        return int(np.float64(0xFFFFFFFF) * (1 - r * r))
+
+    def oracle_sim(self):
+        """oracle_sim with the same floats as the engine medium."""
+        s = pyoracle.CSim()
+        s.bulk_method = 2
+        s.number_of_photons = self.photons
+        s.number_of_photons_per_voxel = self.per_voxel
+        s.grid_size = self.grid
+        s.esp = self.esp
+        s.do_fl_sim = self.do_fl
+        s.fhd_activated = 1 if self.do_fl in (1, 2) else 0
+        s.det_dx, s.det_dy, s.det_nx, s.det_ny, s.det_x0, s.det_y0 = self.det
+        s.xi, s.yi, s.zi = self.source
+        s.dir = 1.0
+        bl = self.bulks()
+        s.n_bulks = len(bl) - 2
+        for i, b in enumerate(bl):
+            s.bulks[i] = pyoracle.CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof)
+        s.start_weight = self.start_weight()
+        lab = np.ascontiguousarray(self.labels.astype(np.int16))
+        s.bulk_info = lab.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_short))
+        s._keep = lab
+        return s
+
+    def engine_medium(self, ctx):
+        nx, ny, nz = self.dims
+        e = np.float32(self.esp)
+        return ctx.medium(self.labels, self.bulks(), vox_per_cm=(float(self.grid),) * 3,
+                          half_x=float(np.float32(2) * e), half_y=float(np.float32(2) * e), thickness=float(e))
+
+    def run_desc(self, seed_exc, seed_fl, photons=None):
+        dx, dy, nx, ny, x0, y0 = self.det
+        return mc.run_desc(photons or self.photons, source=self.source, det=mc.Detector(x0, y0, dx, dy, nx, ny),
+                           photons_per_voxel=self.per_voxel if self.do_fl else 0,
+                           fluence=1 if self.do_fl in (1, 2) else 0, seed_exc=seed_exc, seed_fl=seed_fl,
+                           start_weight=self.start_weight())
+
+    def write_mci(self, d: str) -> str:
+        """Writes <d>/<name>.mci and its bulk file in the reference's grammar."""
+        nx, ny, nz = self.dims
+        bulk = os.path.join(d, self.name + ".bulk")
+        with open(bulk, "w") as f:
+            f.write(" ".join(str(int(v)) for v in self.labels.ravel()) + "\n")
+        dx, dy, dnx, dny, x0, y0 = self.det
+        lines = ["# test medium " + self.name, "1.0 # file version", "1 # runs", "2 # method",
+                 f"{self.name}-out A", f"{self.photons} # photons", f"{self.per_voxel} # photons per voxel",
+                 f"{self.grid} # grid", f"{self.do_fl} # fluorescence", f"{dx} {dy}", f"{dnx} {dny}", f"{x0} {y0}",
+                 "{} {} {}".format(*self.source), "0 # temporal", "0 0", "1 1", "1 1", "0.5", "0", "10", "1000",
+                 f"{len(self.columns)} # bulks", f"{self.esp} # thickness", f"{self.n_out}"]
+        for c in self.columns:
+            lines.append(" ".join(repr(float(v)) for v in c))
+        lines += [f"{self.n_out}", os.path.basename(bulk)]
+        path = os.path.join(d, self.name + ".mci")
+        with open(path, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        return path
+
+
+def _labels(esp, grid, fill=1):
+    n = int(round(4 * esp * grid))
+    return np.full((int(round(esp * grid)), n, n), fill, dtype=np.uint8)
+
+
+def tiny(photons=40000, per_voxel=40000) -> Case:
+    lab = _labels(0.5, 4)
+    lab[0, 3:5, 3:5] = 2
+    return Case("tiny", 0.5, 4, lab,
+                [(1.4, 0.1, 100.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.4, 0.1, 100.0, 1.0, 0.05, 0.02, 0.1, 0.9)],
+                1.0, photons, per_voxel, (0.1, 0.1, 20, 20, 0.0, 0.0))
+
+
+def mismatch(photons=40000, per_voxel=40000) -> Case:
+    """Internal index mismatch (Fresnel and total internal reflection at
+    label changes), absorbing inclusion, off-centre beam and detector."""
+    lab = _labels(0.5, 6)
+    nz, ny, nx = lab.shape
+    lab[1:, 4:8, 5:9] = 2
+    lab[0, 8:10, 2:5] = 3
+    return Case("mismatch", 0.5, 6, lab,
+                [(1.37, 0.2, 60.0, 0.0, 0.0, 0.0, 0.0, 0.8), (1.52, 0.5, 40.0, 2.0, 0.1, 0.04, 0.2, 0.7),
+                 (1.33, 1.0, 80.0, 0.5, 0.2, 0.1, 0.05, 0.0)],
+                1.0, photons, per_voxel, (0.08, 0.07, 24, 20, 0.1, -0.05), (0.13, -0.07, 0.0))
+
+
+def glass(photons=40000, per_voxel=40000) -> Case:
+    """A scattering-free label (mus = 0) crossed by the beam: the half-voxel
+    march and sphere back-projection of MoveToFirstBoundary."""
+    lab = _labels(0.5, 4)
+    lab[0, 3:5, 3:5] = 2
+    lab[1, 2:6, 2:6] = 3
+    return Case("glass", 0.5, 4, lab,
+                [(1.4, 0.1, 100.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.4, 0.05, 0.0, 0.0, 0.0, 0.0, 0.0, 0.9),
+                 (1.4, 0.2, 90.0, 1.0, 0.05, 0.02, 0.1, 0.85)],
+                1.0, photons, per_voxel, (0.1, 0.1, 20, 20, 0.0, 0.0))
+
+
+def sphere(photons=40000, per_voxel=33000) -> Case:
+    """Config-1-like: a fluorescent sphere r=0.25 under a centred beam."""
+    esp, grid = 1.0, 10
+    lab = _labels(esp, grid)
+    nz, ny, nx = lab.shape
+    z = (np.arange(nz) + 0.5) / grid
+    y = (np.arange(ny) + 0.5) / grid - 2 * esp
+    x = (np.arange(nx) + 0.5) / grid - 2 * esp
+    m = (x[None, None, :] ** 2 + y[None, :, None] ** 2 + (z[:, None, None] - 0.5) ** 2) <= 0.25 ** 2
+    lab[m] = 2
+    return Case("sphere", esp, grid, lab,
+                [(1.4, 0.1, 100.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.4, 0.1, 100.0, 1.0, 0.05, 0.05, 0.1, 0.9)],
+                1.0, photons, per_voxel, (0.04, 0.04, 50, 50, 0.0, 0.0))
+
+
+ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere}

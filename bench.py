@@ -1,0 +1,488 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 photon-transport engine.
+
+Headline workload (one "step"): the two-phase fluorescence simulation of the
+voxelized heterogeneous medium — 200 x 200 x 100 voxels of 0.02 cm, 8 labels,
+seeded spheres and cylinders with a fp32 fluorophore map — 1e8 excitation
+photons from a Gaussian beam with the 3D photon hitting density, then the
+emission phase with PHOTONS_PER_VOXEL photons from every emitting voxel, R/T
+images at both wavelengths.  The metric is photons per second (excitation +
+emission photons).
+
+  value       batched engine, medium and tallies resident in HBM, CUDA-event
+              timed per step on the engine's stream, L2 flushed between steps
+  e2e         the same through the C ABI with host buffers: medium upload,
+              run, every image and the fluence copied back, each step
+  plain       the same simulation with the emission phase as one launch per
+              emitting voxel (the reference's schedule), timed on a sample
+  batching    256 Gaussian beams on a 16 x 16 raster over the 4 x 4 x 2 cm
+              sphere medium, log-uniform budgets, one persistent launch vs
+              one launch per beam
+  serving     Poisson stream of requests with their own media (64^3 ..
+              256 x 256 x 128) and 1e5..1e8 photons at ~80 % load through the
+              continuous-batching server: p50/p99 latency, photons/s
+  cpu_baseline  the reference's transport algorithm (the oracle restatement in
+              reference-stream mode, bit-identical to the reference's code) on
+              the host cores, on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (the reference's own
+CUDA build cannot run here: it needs its missing multiplier file and a GPU
+build of sm_35/sm_50 era; the host build is its transport).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "photons/s, two-phase fluorescence MC (excitation + emission), voxelized heterogeneous medium"
+UNIT = "photons/s"
+EXC_PHOTONS = 100_000_000
+PHOTONS_PER_VOXEL = 1000
+WORKLOAD = ("voxelized heterogeneous bulk descriptor 200x200x100 @0.02cm, 8 labels, seeded spheres+cylinders "
+            "with fp32 fluorophore map; 1e8 excitation photons (Gaussian beam) with 3D photon hitting density, "
+            "emission phase 1000 photons per emitting voxel; R/T images 100x100 @0.04cm at both wavelengths")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples while running."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int = 0):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        busy = [s for s in sm if s > 0.5 * max(sm)] if sm else []
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# ------------------------------------------------------------------ CPU arm
+
+def cpu_reference_sample(nthreads: int, exc_photons: int = 2_000_000, fl_voxels: int = 8, per_voxel: int = 40_000):
+    """The reference's transport algorithm on host threads over the benchmark
+    medium (reference RNG streams and relaunch schedule, C-library math).
+    Returns (photons/s, photons, seconds, description)."""
+    from cudamcfl_gb300 import media
+    from oracle import pyoracle
+    pyoracle.build()
+    o = pyoracle.Oracle()
+    m = media.config2(seed=2)
+    nz, ny, nx = m.labels.shape
+    vc = m.voxel_cm
+    sim = pyoracle.sim_from_arrays(
+        m.labels, m.bulks, half_x=float(np.float32(nx * vc[0] / 2)), half_y=float(np.float32(ny * vc[1] / 2)),
+        thickness=float(np.float32(nz * vc[2])), vox_per_cm=[float(np.float32(1 / v)) for v in vc],
+        photons=exc_photons, per_voxel=per_voxel, det=(0.04, 0.04, 100, 100, 0.0, 0.0), fluor_map=m.fluor_map,
+        do_fl=1 if fl_voxels > 0 else 0)
+    sim.max_fl_voxels = fl_voxels
+    import tempfile
+    with tempfile.TemporaryDirectory() as d:
+        sp = os.path.join(d, "safeprimes_base32.txt")
+        o.write_safeprimes(sp, 32769)
+        t0 = time.perf_counter()
+        r = o.run_refstream(sim, sp, 12345, 777, libm=True, nthreads=nthreads)
+        dt = time.perf_counter() - t0
+    photons = r.photons_exc + r.photons_fl
+    desc = (f"config-2 medium, {r.photons_exc} excitation photons + {r.fl_voxels} emitting voxels x {per_voxel} "
+            f"emission photons; reference RNG streams (32768 MWC) and relaunch schedule, libm math")
+    return photons / dt, photons, dt, desc
+
+
+def run_reference_arm(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_reference_sample(nthreads, exc_photons=100_000, fl_voxels=1)
+    vals, tot_p, tot_t = [], 0, 0.0
+    desc = ""
+    for _ in range(args.steps):
+        v, p, t, desc = cpu_reference_sample(nthreads, exc_photons=600_000, fl_voxels=4)
+        vals.append(v)
+        tot_p += p
+        tot_t += t
+    value = tot_p / tot_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--math", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,batching,serving,cpu,e2e")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    import cudamcfl_gb300 as mc
+    from cudamcfl_gb300 import build, media
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    skip = set(s for s in args.skip.split(",") if s)
+    build.build()
+    math_mode = mc.MATH_FAST if args.math == "fast" else mc.MATH_EXACT
+    stream = torch.cuda.Stream()
+    ctx = mc.Context(device=local, math=math_mode)
+    ctx.set_stream(stream.cuda_stream)
+    lib = mc.load()
+
+    m = media.config2(seed=2)
+    med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
+    # replicas only: every rank simulates its own photon streams (seeded by rank)
+    rd = mc.run_desc(EXC_PHOTONS, det=m.det, photons_per_voxel=PHOTONS_PER_VOXEL, fluence=1,
+                     seed_exc=1 + 1000 * rank, seed_fl=2 + 1000 * rank)
+    stats_out = mc.RunOut()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+
+    def one_step():
+        return lib.mcfl_run(ctx.handle, med.handle, mc.ctypes.byref(rd), mc.ctypes.byref(stats_out))
+
+    for _ in range(args.warmup):
+        mc.check(one_step())
+    torch.cuda.synchronize()
+    launches0 = ctx.launches
+    clocks = ClockSampler(local).start()
+    if dist:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, photons_step, exc_ms, fl_ms = [], [], [], []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)  # L2 flush (512 MB > 129 MB L2) outside the timed events
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        mc.check(one_step())
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        photons_step.append(EXC_PHOTONS + stats_out.photons_fl)
+        exc_ms.append(stats_out.ms_exc)
+        fl_ms.append(stats_out.ms_fl)
+    torch.cuda.synchronize()
+    if dist:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    launches = ctx.launches - launches0
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * sum(photons_step) / (total_ms / 1e3)
+    se, sf = dict(zip(mc.STAT_NAMES, stats_out.stats_exc)), dict(zip(mc.STAT_NAMES, stats_out.stats_fl))
+    exc_steps_per_photon = se["steps"] / EXC_PHOTONS
+    fl_steps_per_photon = sf["steps"] / max(1, stats_out.photons_fl)
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "photons_per_step": photons_step[0], "excitation_photons": EXC_PHOTONS,
+                   "emitting_voxels": stats_out.fl_voxels, "emission_photons": stats_out.photons_fl,
+                   "math": args.math, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas only",
+                   "schedule": "batched: one persistent launch per phase, CUDA-graph replay"},
+        "phases": {"excitation_ms": statistics.mean(exc_ms), "emission_ms": statistics.mean(fl_ms),
+                   "excitation_photons_per_s": EXC_PHOTONS / (statistics.mean(exc_ms) / 1e3),
+                   "emission_photons_per_s": stats_out.photons_fl / (statistics.mean(fl_ms) / 1e3),
+                   "steps_per_photon": {"excitation": exc_steps_per_photon, "emission": fl_steps_per_photon},
+                   "transport_steps_per_s": (se["steps"] + sf["steps"]) / (statistics.mean(step_ms) / 1e3),
+                   "energy_residual": stats_out.energy_exc[3]},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+    if rank != 0:
+        if dist:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # --- roofline of the dominant kernel (the transport kernel) ---
+    # Algorithmic work unit: one transport step of the reference (SURVEY
+    # per-step op table: ~60 FP32 + 10 SFU + 8 conversion + 3 integer).
+    ops_per_step = 81
+    steps_s = result["phases"]["transport_steps_per_s"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    sm_mhz = peaks.get("sm_max_mhz", 2070.0)
+    n_sm = ctx.get_option("sm_count")
+    fp32_peak = n_sm * 128 * sm_mhz * 1e6  # FP32 lane operations per second
+    traffic = None
+    try:
+        prof = json.load(open(os.path.join(ROOT, "profiles", "transport_roofline.json")))
+        traffic = prof.get("dram_bytes_per_step", None)
+        if traffic is not None:
+            traffic = traffic * (se["steps"] + sf["steps"]) / 2
+    except (OSError, ValueError):
+        pass
+    result["roofline"] = {
+        "bound": "issue", "achieved": ops_per_step * steps_s / 1e12, "peak": fp32_peak / 1e12, "unit": "Top/s",
+        "frac": ops_per_step * steps_s / fp32_peak, "traffic": traffic,
+        "note": (f"algorithmic FP32/SFU/convert ops of one transport step ({ops_per_step}) x steps/s over "
+                 f"{n_sm} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); neither HBM "
+                 "nor tensor cores bound this kernel"),
+    }
+
+    # --- e2e through the C ABI with host buffers ---
+    if "e2e" not in skip:
+        nv = m.labels.size
+        xy = 100 + 100 * 100
+        bufs = {k: np.zeros(n, dtype=dt) for k, n, dt in (
+            ("Rd", xy, np.uint64), ("Tt", xy, np.uint64), ("R", xy, np.float64), ("T", xy, np.float64),
+            ("phd", nv, np.float64), ("flR", xy, np.float64), ("flT", xy, np.float64))}
+        out = mc.RunOut()
+        out.Rd, out.Tt = mc.u64ptr(bufs["Rd"]), mc.u64ptr(bufs["Tt"])
+        out.R, out.T, out.phd = mc.f64ptr(bufs["R"]), mc.f64ptr(bufs["T"]), mc.f64ptr(bufs["phd"])
+        out.flR, out.flT = mc.f64ptr(bufs["flR"]), mc.f64ptr(bufs["flT"])
+        d, keep = mc._medium_desc(m.labels, m.bulks, m.voxel_cm, m.fluor_map)
+        h2d = m.labels.nbytes + m.fluor_map.nbytes + 3 * 16 * len(m.bulks) + 2 * 256
+        d2h = sum(b.nbytes for b in bufs.values()) + 8 * (2 * mc.NSTATS + 4)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ph = 0
+        for _ in range(args.steps):
+            h = mc.ctypes.c_void_p()
+            mc.check(lib.mcfl_medium_create(ctx.handle, mc.ctypes.byref(d), mc.ctypes.byref(h)))
+            mc.check(lib.mcfl_run(ctx.handle, h, mc.ctypes.byref(rd), mc.ctypes.byref(out)))
+            lib.mcfl_medium_free(h)
+            ph += EXC_PHOTONS + out.photons_fl
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        result["e2e"] = {"value": ph / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                         "d2h_bytes_per_step": int(d2h)}
+
+    # --- plain schedule of the same simulation (emission: one launch per voxel) ---
+    if "plain" not in skip:
+        sample = 400
+        r = mc.run_plain(ctx, med, rd, max_voxels=sample)
+        per_voxel_ms = r["ms_fl"] / max(1, r["fl_voxels"])
+        plain_ms = r["ms_exc"] + per_voxel_ms * stats_out.fl_voxels
+        plain_value = (EXC_PHOTONS + stats_out.photons_fl) / (plain_ms / 1e3)
+        result["plain"] = {"value": plain_value, "unit": UNIT, "ms_per_step": plain_ms,
+                           "sample": f"excitation + first {r['fl_voxels']} of {stats_out.fl_voxels} emitting voxels, "
+                                     f"one launch + host wait per voxel; {per_voxel_ms:.3f} ms per voxel",
+                           "batched_over_plain": value / plain_value}
+
+    # --- batched sweep: 256 beams on the sphere medium ---
+    if "batching" not in skip:
+        c1 = media.config1()
+        med1 = ctx.medium(c1.labels, c1.bulks, voxel_cm=c1.voxel_cm)
+        scale = 0.1
+        pos, budgets = media.raster_sources(16, 4.0, seed=3, scale=scale)
+        runs = [mc.run_desc(b, source=(x, y, 0.0), det=c1.det, seed_exc=10_000 + i) for i, ((x, y), b)
+                in enumerate(zip(pos, budgets))]
+        mc.batch_run(ctx, med1, runs[:4], mc.SCHEDULE_BATCHED, images=False)
+        _, ms_b = mc.batch_run(ctx, med1, runs, mc.SCHEDULE_BATCHED, images=False)
+        _, ms_p = mc.batch_run(ctx, med1, runs, mc.SCHEDULE_PLAIN, images=False)
+        tot = sum(budgets)
+        result["batching"] = {
+            "workload": f"256 Gaussian beams on a 16x16 raster over the config-1 sphere medium (50^3 voxels, 4x4x2 cm), "
+                        f"log-uniform budgets 1e6..5e7 scaled by {scale} ({tot:.3g} photons), own R/T images each",
+            "batched_photons_per_s": tot / (ms_b / 1e3), "plain_photons_per_s": tot / (ms_p / 1e3),
+            "batched_over_plain": ms_p / ms_b, "batched_ms": ms_b, "plain_ms": ms_p}
+        med1.free()
+
+    # --- continuous-batching server ---
+    if "serving" not in skip:
+        result["serving"] = serve_stream(mc, ctx, local, duration_s=12.0)
+
+    # --- CPU baseline (reference algorithm on host cores) ---
+    if "cpu" not in skip:
+        nthreads = os.cpu_count() or 1
+        v, p, t, desc = cpu_reference_sample(nthreads)
+        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc,
+                                  "seconds": t}
+    med.free()
+    ctx.close()
+    print(json.dumps(result), flush=True)
+    if dist:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
+    """Poisson arrivals at ~80 % of the measured service rate."""
+    from cudamcfl_gb300 import media
+    rng = np.random.default_rng(seed)
+    sizes = [(64, 64, 64), (96, 96, 64), (128, 128, 64), (160, 160, 96), (192, 192, 128), (256, 256, 128)]
+    pool = []
+    for i, (nx, ny, nz) in enumerate(sizes):
+        vox = (4.0 / nx, 4.0 / ny, 2.0 / nz)
+        lab = np.ones((nz, ny, nx), dtype=np.uint8)
+        fmap = np.zeros(lab.shape, dtype=np.float32)
+        for j in range(int(rng.integers(2, 6))):
+            media.add_sphere(lab, vox, (rng.uniform(-1.2, 1.2), rng.uniform(-1.2, 1.2), rng.uniform(0.4, 1.6)),
+                             rng.uniform(0.15, 0.45), int(rng.integers(2, 4)), fmap, float(rng.uniform(0, 1)))
+        bulks = [mc.outer_bulk(1.0), mc.bulk_from_mci_columns(1.4, 0.1, 100.0, g=0.9),
+                 mc.bulk_from_mci_columns(1.4, 0.3, 80.0, 1.0, 0.05, 0.02, 0.1, 0.85),
+                 mc.bulk_from_mci_columns(1.4, 0.05, 120.0, 1.0, 0.08, 0.03, 0.15, 0.9), mc.outer_bulk(1.0)]
+        pool.append((lab, bulks, vox, fmap))
+    det = mc.Detector(0.0, 0.0, 0.04, 0.04, 100, 100)
+    # service rate from a calibration run (photons/s of a plain single run)
+    lab, bulks, vox, fmap = pool[2]
+    med = ctx_main.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
+    cal = ctx_main.run(med, mc.run_desc(5_000_000, det=det, seed_exc=9), images=False, raw=False)
+    med.free()
+    rate_photons = 5_000_000 / (cal.ms_exc / 1e3)
+    mean_photons = (1e8 - 1e5) / math.log(1e8 / 1e5)
+    lam = 0.8 * rate_photons / mean_photons
+    import cudamcfl_gb300 as mcm
+    sctx = mcm.Context(device=device, math=ctx_main.get_option("math"))
+    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048)
+    ids, plain_ms_est = [], 0.0
+    t_start = time.perf_counter()
+    t_next = t_start
+    n = 0
+    while True:
+        now = time.perf_counter()
+        if now - t_start > duration_s:
+            break
+        if now < t_next:
+            time.sleep(min(0.002, t_next - now))
+            continue
+        photons = int(math.exp(rng.uniform(math.log(1e5), math.log(1e8))))
+        lab, bulks, vox, fmap = pool[int(rng.integers(0, len(pool)))]
+        wide = rng.uniform() < 0.5
+        rd = mcm.run_desc(photons, det=det, seed_exc=20_000 + n, kind=mcm.SOURCE_WIDEFIELD if wide else
+                          mcm.SOURCE_GAUSS_BEAM, width=4.0, height=4.0, fluence=0)
+        ids.append((srv.submit(lab, bulks, vox, rd, fluor_map=fmap), photons))
+        n += 1
+        t_next += rng.exponential(1.0 / lam)
+    for rid, _ in ids:
+        srv.wait(rid, -1)
+    mtr = srv.metrics()
+    for rid, _ in ids:
+        srv.result(rid)
+    srv.close()
+    photons_total = sum(p for _, p in ids)
+    served = photons_total / mtr["span_s"] if mtr["span_s"] > 0 else None
+
+    # saturation: the same kind of requests all queued at once (served), and
+    # one request per launch after another (plain), same requests both ways
+    burst = []
+    for i in range(24):
+        photons = int(math.exp(rng.uniform(math.log(1e5), math.log(1e8))))
+        lab, bulks, vox, fmap = pool[int(rng.integers(0, len(pool)))]
+        wide = rng.uniform() < 0.5
+        burst.append((lab, bulks, vox, fmap, mcm.run_desc(photons, det=det, seed_exc=90_000 + i, width=4.0,
+                                                         height=4.0, kind=mcm.SOURCE_WIDEFIELD if wide else
+                                                         mcm.SOURCE_GAUSS_BEAM)))
+    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048)
+    t0 = time.perf_counter()
+    bids = [srv.submit(lab, bulks, vox, rd, fluor_map=fmap) for lab, bulks, vox, fmap, rd in burst]
+    for rid in bids:
+        srv.wait(rid, -1)
+    t_served = time.perf_counter() - t0
+    for rid in bids:
+        srv.result(rid)
+    srv.close()
+    t0 = time.perf_counter()
+    for lab, bulks, vox, fmap, rd in burst:
+        med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
+        sctx.run(med, rd, images=False, raw=True)
+        med.free()
+    t_plain = time.perf_counter() - t0
+    sctx.close()
+    burst_photons = sum(b[4].photons for b in burst)
+    return {"requests": len(ids), "arrival_rate_per_s": lam, "target_load": 0.8, "p50_ms": mtr["p50_ms"],
+            "p99_ms": mtr["p99_ms"], "max_ms": mtr["max_ms"], "photons_per_s": served,
+            "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
+            "slices": mtr["slices"],
+            "saturated": {"requests": len(burst), "photons": burst_photons,
+                          "served_photons_per_s": burst_photons / t_served,
+                          "plain_photons_per_s": burst_photons / t_plain, "served_over_plain": t_plain / t_served},
+            "workload": "Poisson requests at 80 % of the calibrated single-run rate, own media 64^3..256x256x128 "
+                        "(labels + fp32 map), 1e5..1e8 photons log-uniform, Gaussian beam or 4x4 cm wide field; "
+                        "saturated: 24 such requests queued at once vs run one per launch (upload, run, read back)"}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -120,6 +120,23 @@ class RunOut(ctypes.Structure):
                 ("energy_exc", ctypes.c_double * 4), ("ms_exc", ctypes.c_float), ("ms_fl", ctypes.c_float)]
 
 
+SCHEDULE_BATCHED = 0
+SCHEDULE_PLAIN = 1
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_ulonglong), ("max_jobs", ctypes.c_uint),
+                ("slice_passes", ctypes.c_uint)]
+
+
+class ServerMetrics(ctypes.Structure):
+    _fields_ = [("completed", ctypes.c_ulonglong), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("max_ms", ctypes.c_double), ("photons", ctypes.c_ulonglong), ("slices", ctypes.c_ulonglong),
+                ("busy_s", ctypes.c_double), ("span_s", ctypes.c_double), ("mean_inflight", ctypes.c_double),
+                ("max_inflight", ctypes.c_ulonglong), ("hbm_used", ctypes.c_ulonglong),
+                ("hbm_budget", ctypes.c_ulonglong)]
+
+
 # ----------------------------------------------------------------- loading
 
 _lib = None
@@ -162,6 +179,15 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mcfl_write_phd": (ctypes.c_int, [P(Simulation), _f64p]),
         "mcfl_write_fl_images": (ctypes.c_int, [P(Simulation), _f64p, _f64p]),
         "mcfl_run_mci": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_ulonglong]),
+        "mcfl_batch_run": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_int, ctypes.c_int, P(RunOut),
+                                          P(ctypes.c_float)]),
+        "mcfl_run_plain": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_longlong, P(RunOut)]),
+        "mcfl_server_create": (ctypes.c_int, [vp, P(ServerOpts), P(vp)]),
+        "mcfl_server_submit": (ctypes.c_int, [vp, P(MediumDesc), P(RunDesc), P(ctypes.c_ulonglong)]),
+        "mcfl_server_wait": (ctypes.c_int, [vp, ctypes.c_ulonglong, ctypes.c_int]),
+        "mcfl_server_result": (ctypes.c_int, [vp, ctypes.c_ulonglong, P(RunOut), P(ctypes.c_double)]),
+        "mcfl_server_metrics": (ctypes.c_int, [vp, P(ServerMetrics)]),
+        "mcfl_server_destroy": (None, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -365,6 +391,138 @@ class Context:
             stats_exc=dict(zip(STAT_NAMES, list(out.stats_exc))), stats_fl=dict(zip(STAT_NAMES, list(out.stats_fl))),
             photons_fl=int(out.photons_fl), fl_voxels=int(out.fl_voxels), energy_exc=tuple(out.energy_exc),
             ms_exc=float(out.ms_exc), ms_fl=float(out.ms_fl))
+
+
+def _medium_desc(labels, bulks, voxel_cm, fluor_map=None):
+    """MediumDesc over numpy arrays (kept alive by the returned tuple)."""
+    lab = np.ascontiguousarray(labels, dtype=np.uint8)
+    nz, ny, nx = lab.shape
+    vc = np.asarray(voxel_cm, dtype=np.float64)
+    d = MediumDesc()
+    d.nx, d.ny, d.nz = nx, ny, nz
+    d.half_x = float(np.float32(nx * vc[0] / 2))
+    d.half_y = float(np.float32(ny * vc[1] / 2))
+    d.thickness = float(np.float32(nz * vc[2]))
+    d.vox_per_cm[:] = [float(np.float32(1.0 / v)) for v in vc]
+    d.labels = lab.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte))
+    fm = None
+    if fluor_map is not None:
+        fm = np.ascontiguousarray(fluor_map, dtype=np.float32)
+        d.fluor_map = fm.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    barr = (Bulk * len(bulks))(*bulks)
+    d.n_bulks = len(bulks) - 2
+    d.bulks = barr
+    return d, (lab, fm, barr)
+
+
+def _alloc_out(xy, nv=0, images=True, fluence=False):
+    out = RunOut()
+    keep = {}
+    for name, n, dt, pf in (("Rd", xy, np.uint64, u64ptr), ("Tt", xy, np.uint64, u64ptr)):
+        a = np.zeros(n, dtype=dt)
+        keep[name] = a
+        setattr(out, name, pf(a))
+    if images:
+        for name in ("R", "T"):
+            a = np.zeros(xy, dtype=np.float64)
+            keep[name] = a
+            setattr(out, name, f64ptr(a))
+    if fluence:
+        a = np.zeros(nv, dtype=np.uint64)
+        keep["fhd"] = a
+        out.fhd = u64ptr(a)
+    return out, keep
+
+
+def batch_run(ctx: "Context", medium: "Medium", runs: list, schedule: int = SCHEDULE_BATCHED,
+              images: bool = True):
+    """Runs excitation-only simulations on one medium.  Returns (list of
+    dicts with Rd, Tt, R, T, stats; GPU ms)."""
+    n = len(runs)
+    arr = (RunDesc * n)(*runs)
+    outs = (RunOut * n)()
+    keeps = []
+    for i, r in enumerate(runs):
+        xy = r.det.nx + r.det.nx * r.det.ny
+        o, k = _alloc_out(xy, images=images)
+        outs[i] = o
+        keeps.append(k)
+    ms = ctypes.c_float()
+    check(load().mcfl_batch_run(ctx.handle, medium.handle, arr, n, schedule, outs, ctypes.byref(ms)))
+    res = []
+    for i in range(n):
+        d = dict(keeps[i])
+        d["stats"] = dict(zip(STAT_NAMES, list(outs[i].stats_exc)))
+        res.append(d)
+    return res, float(ms.value)
+
+
+def run_plain(ctx: "Context", medium: "Medium", rd: RunDesc, max_voxels: int = 0):
+    """Two-phase run with one emission launch per voxel."""
+    xy = rd.det.nx + rd.det.nx * rd.det.ny
+    out = RunOut()
+    keep = {}
+    for name, n in (("Rd", xy), ("Tt", xy), ("flR128", 2 * xy), ("flT128", 2 * xy)):
+        a = np.zeros(n, dtype=np.uint64)
+        keep[name] = a
+        setattr(out, name, u64ptr(a))
+    check(load().mcfl_run_plain(ctx.handle, medium.handle, ctypes.byref(rd), max_voxels, ctypes.byref(out)))
+    keep["flR128"] = keep["flR128"].reshape(xy, 2)
+    keep["flT128"] = keep["flT128"].reshape(xy, 2)
+    keep.update(stats_exc=dict(zip(STAT_NAMES, list(out.stats_exc))),
+                stats_fl=dict(zip(STAT_NAMES, list(out.stats_fl))), fl_voxels=int(out.fl_voxels),
+                photons_fl=int(out.photons_fl), ms_exc=float(out.ms_exc), ms_fl=float(out.ms_fl))
+    return keep
+
+
+class Server:
+    """Continuous-batching server over one context."""
+
+    def __init__(self, ctx: "Context", hbm_budget_bytes: int = 0, max_jobs: int = 0, slice_passes: int = 0):
+        o = ServerOpts(hbm_budget_bytes, max_jobs, slice_passes)
+        h = ctypes.c_void_p()
+        check(load().mcfl_server_create(ctx.handle, ctypes.byref(o), ctypes.byref(h)))
+        self.handle = h
+        self._keep = {}
+        self._shape = {}
+
+    def submit(self, labels, bulks, voxel_cm, rd: RunDesc, fluor_map=None) -> int:
+        d, keep = _medium_desc(labels, bulks, voxel_cm, fluor_map)
+        rid = ctypes.c_ulonglong()
+        check(load().mcfl_server_submit(self.handle, ctypes.byref(d), ctypes.byref(rd), ctypes.byref(rid)))
+        self._keep[rid.value] = (d, keep, rd)
+        self._shape[rid.value] = (rd.det.nx + rd.det.nx * rd.det.ny, int(np.prod(np.shape(labels))),
+                                  bool(rd.fluence))
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1) -> int:
+        return int(load().mcfl_server_wait(self.handle, rid, timeout_ms))
+
+    def result(self, rid: int):
+        xy, nv, fl = self._shape[rid]
+        out, keep = _alloc_out(xy, nv, images=False, fluence=fl)
+        lat = ctypes.c_double()
+        check(load().mcfl_server_result(self.handle, rid, ctypes.byref(out), ctypes.byref(lat)))
+        self._keep.pop(rid, None)
+        keep["stats"] = dict(zip(STAT_NAMES, list(out.stats_exc)))
+        keep["latency_ms"] = float(lat.value)
+        return keep
+
+    def metrics(self) -> dict:
+        m = ServerMetrics()
+        check(load().mcfl_server_metrics(self.handle, ctypes.byref(m)))
+        return {k: getattr(m, k) for k, _ in ServerMetrics._fields_}
+
+    def close(self) -> None:
+        if self.handle:
+            load().mcfl_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per_voxel: int = 0, fluence: int = 0,

@@ -34,7 +34,7 @@ CUDA_UNITS = {
     "transport_fast.cu": FAST,
     "engine_kernels.cu": EXACT,
 }
-HOST_UNITS = ["engine.cpp", "mci.cpp", "safeprimes.cpp", "batch.cpp", "server.cpp"]
+HOST_UNITS = ["engine.cpp", "run.cpp", "mci.cpp", "safeprimes.cpp", "server.cpp"]
 HEADERS = ["engine_types.h", "portable_math.h", "mcfl_internal.h", "transport.cuh"]
 
 

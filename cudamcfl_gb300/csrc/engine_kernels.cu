@@ -133,6 +133,13 @@ __global__ void normalize_u64(const unsigned long long *raw, double *out, size_t
     out[i] = (double)raw[i] / scale;
 }
 
+/* raw[i] / scales[i / seg_len]: one normalisation per job of a batch */
+__global__ void normalize_segments(const unsigned long long *raw, double *out, size_t seg_len, size_t n,
+                                   const double *scales) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (double)raw[i] / scales[i / seg_len];
+}
+
 __global__ void normalize_phd(const unsigned long long *raw, double *out, size_t n, unsigned long long photons) {
   const double den = (double)(0xFFFFFFFFull * photons);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
@@ -173,6 +180,13 @@ extern "C" cudaError_t mcfl_launch_emission_prep(const uint8_t *labels, const fl
 extern "C" cudaError_t mcfl_launch_normalize_u64(const unsigned long long *raw, double *out, size_t n, double scale,
                                                  cudaStream_t s) {
   normalize_u64<<<grid_for(n), 256, 0, s>>>(raw, out, n, scale);
+  return cudaGetLastError();
+}
+
+extern "C" cudaError_t mcfl_launch_normalize_segments(const unsigned long long *raw, double *out, size_t seg_len,
+                                                      size_t n_seg, const double *scales, cudaStream_t s) {
+  const size_t n = seg_len * n_seg;
+  normalize_segments<<<grid_for(n), 256, 0, s>>>(raw, out, seg_len, n, scales);
   return cudaGetLastError();
 }
 

@@ -89,8 +89,9 @@ typedef struct MCFL_ALIGN(16) McflSaved {
 } McflSaved;
 
 typedef struct McflLaunch {
-  const McflJob *jobs;
-  uint32_t n_jobs;
+  const McflJob *jobs;   /* job slots */
+  const uint32_t *order; /* slots sorted by ticket_begin, or NULL: slots 0..n_jobs-1 in order */
+  uint32_t n_jobs;       /* entries of order (or slots) */
   uint32_t max_iters; /* loop iterations per launch; 0 = run until no ticket is left */
   unsigned long long *ticket_counter;
   uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */

@@ -27,6 +27,12 @@ const std::vector<uint32_t> &mwc_table(); /* kMwcTableEntries + 1 entries */
 int fail(int code, const std::string &msg);
 int cuda_fail(cudaError_t e, const char *where);
 
+#define MCFL_CUDA_TRY(call)                                    \
+  do {                                                         \
+    cudaError_t e__ = (call);                                  \
+    if (e__ != cudaSuccess) return mcfl::cuda_fail(e__, #call); \
+  } while (0)
+
 /* Grow-only device buffer. */
 struct DevBuf {
   void *p = nullptr;
@@ -48,6 +54,8 @@ extern "C" cudaError_t mcfl_launch_normalize_u64(const unsigned long long *raw, 
                                                  cudaStream_t s);
 extern "C" cudaError_t mcfl_launch_normalize_phd(const unsigned long long *raw, double *out, size_t n,
                                                  unsigned long long photons, cudaStream_t s);
+extern "C" cudaError_t mcfl_launch_normalize_segments(const unsigned long long *raw, double *out, size_t seg_len,
+                                                      size_t n_seg, const double *scales, cudaStream_t s);
 extern "C" cudaError_t mcfl_launch_normalize_128(const unsigned long long *raw, double *out, size_t n, double norm,
                                                  cudaStream_t s);
 
@@ -90,6 +98,17 @@ struct mcfl_ctx {
   mcfl::DevBuf saved;      /* parked photons of budgeted launches */
   /* run workspace */
   mcfl::DevBuf R, T, fhd, R128, T128, stats, vox, q, block_counts, outd;
+  /* pinned staging for job tables and results read back after a launch */
+  McflJob *h_jobs = nullptr;
+  size_t h_jobs_cap = 0;
+  unsigned long long *h_out = nullptr;
+  size_t h_out_cap = 0;
+  /* recorded launch sequences replayed as CUDA graphs */
+  cudaGraphExec_t graph_run = nullptr, graph_batch = nullptr;
+  std::string graph_run_key, graph_batch_key;
+  unsigned graph_run_kernels = 0, graph_batch_kernels = 0;
+  int use_graphs = 1;
+  mcfl::DevBuf bR, bT, bstats, bcnt, seg_scale; /* batch workspace */
   int math = MCFL_MATH_EXACT;
   int block = 256;
   int blocks_per_sm = 0;

@@ -1,0 +1,452 @@
+/*
+ * Continuous-batching server.
+ *
+ * Requests (a medium and an excitation run) arrive on any thread.  A server
+ * thread owns the GPU context and loops:
+ *   1. admission: queued requests are admitted in arrival order while their
+ *      HBM footprint (labels, fluorophore map, property tables, R/T images,
+ *      photon hitting density) fits the budget and a job slot is free; the
+ *      medium is uploaded and the request becomes a job whose photon tickets
+ *      start where the running jobs' tickets end;
+ *   2. one slice: the persistent transport kernel runs a bounded number of
+ *      passes over every admitted job at once, drawing tickets from all of
+ *      them, and parks the photons still in flight in HBM when the budget is
+ *      spent;
+ *   3. completion: jobs whose photons have all terminated are copied out and
+ *      their memory and slot are released.
+ * New work therefore joins the running batch at the next slice (every few
+ * milliseconds) while earlier requests are still in flight, and a request's
+ * photons draw the same random streams whatever else shares the GPU, so its
+ * tallies equal those of running it alone bit for bit.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "mcfl_internal.h"
+#include "portable_math.h"
+
+using namespace mcfl;
+using Clock = std::chrono::steady_clock;
+
+namespace {
+
+struct Request {
+  unsigned long long id = 0;
+  mcfl_medium_desc desc{};
+  std::vector<mcfl_bulk> bulks;
+  mcfl_run_desc run{};
+  Clock::time_point t_submit, t_admit, t_done;
+  size_t footprint = 0;
+  /* device state while admitted */
+  mcfl_medium *medium = nullptr;
+  DevBuf R, T, fhd, stats;
+  int slot = -1;
+  uint64_t ticket_begin = 0;
+  /* results */
+  bool done = false;
+  int status = MCFL_OK;
+  std::vector<unsigned long long> Rd, Tt, fhd_host;
+  unsigned long long st[MCFL_ST_COUNT] = {0};
+};
+
+size_t footprint_of(const mcfl_medium_desc &d, const mcfl_run_desc &r) {
+  const size_t nv = (size_t)d.nx * d.ny * d.nz;
+  const size_t xy = (size_t)r.det.nx + (size_t)r.det.nx * r.det.ny;
+  size_t b = nv + (d.fluor_map ? nv * 4 : 0) + 3 * 16 * (size_t)(d.n_bulks + 2);
+  b += 2 * xy * 8 + MCFL_ST_COUNT * 8;
+  if (r.fluence) b += nv * 8;
+  return b;
+}
+
+} // namespace
+
+struct mcfl_server {
+  mcfl_ctx *ctx = nullptr;
+  size_t budget = 0, used = 0;
+  unsigned slots = 64;
+  uint32_t slice_iters = 2048;
+  std::mutex mu;
+  std::condition_variable cv, cv_done;
+  std::deque<std::shared_ptr<Request>> queue;
+  std::map<unsigned long long, std::shared_ptr<Request>> all;
+  std::vector<std::shared_ptr<Request>> active; /* by slot */
+  unsigned long long next_id = 1;
+  bool stop = false;
+  int fatal = MCFL_OK;
+  std::thread worker;
+  /* device state */
+  DevBuf slot_jobs, order, counter, parked, stats_all;
+  McflJob *h_jobs = nullptr;
+  uint32_t *h_order = nullptr;
+  unsigned long long *h_read = nullptr;
+  uint64_t tickets_end = 0;
+  int grid = 0;
+  /* metrics */
+  std::vector<double> latencies_ms;
+  unsigned long long photons_done = 0, slices = 0, max_inflight = 0, inflight_sum = 0;
+  double busy_s = 0;
+  Clock::time_point t_first, t_last;
+  bool any = false;
+
+  void loop();
+  int admit_locked(std::vector<std::shared_ptr<Request>> &to_upload);
+  int upload(Request &r);
+  void release(Request &r);
+};
+
+int mcfl_server::upload(Request &r) {
+  mcfl_medium *m = nullptr;
+  int rc = mcfl_medium_create(ctx, &r.desc, &m);
+  if (rc != MCFL_OK) return rc;
+  r.medium = m;
+  const size_t xy = (size_t)r.run.det.nx + (size_t)r.run.det.nx * r.run.det.ny;
+  const size_t nv = m->total;
+  cudaStream_t s = ctx->stream;
+  MCFL_CUDA_TRY(r.R.reserve(xy * 8));
+  MCFL_CUDA_TRY(r.T.reserve(xy * 8));
+  MCFL_CUDA_TRY(r.stats.reserve(MCFL_ST_COUNT * 8));
+  MCFL_CUDA_TRY(cudaMemsetAsync(r.R.p, 0, xy * 8, s));
+  MCFL_CUDA_TRY(cudaMemsetAsync(r.T.p, 0, xy * 8, s));
+  MCFL_CUDA_TRY(cudaMemsetAsync(r.stats.p, 0, MCFL_ST_COUNT * 8, s));
+  if (r.run.fluence) {
+    MCFL_CUDA_TRY(r.fhd.reserve(nv * 8));
+    MCFL_CUDA_TRY(cudaMemsetAsync(r.fhd.p, 0, nv * 8, s));
+  }
+  McflJob &j = h_jobs[r.slot];
+  std::memset(&j, 0, sizeof(j));
+  j.labels = m->labels.as<uint8_t>();
+  j.prop = m->prop_exc.as<float>();
+  j.hx = m->hx; j.hy = m->hy; j.esp = m->esp;
+  j.gx = m->gx; j.gy = m->gy; j.gz = m->gz;
+  j.nx = (uint32_t)m->nx; j.ny = (uint32_t)m->ny; j.nz = (uint32_t)m->nz; j.total = m->total;
+  j.last_label = (uint32_t)m->n_bulks + 1u;
+  j.src_kind = r.run.source.kind == MCFL_SOURCE_WIDEFIELD ? MCFL_SRC_WIDEFIELD : MCFL_SRC_GAUSS_BEAM;
+  j.sx = r.run.source.x; j.sy = r.run.source.y; j.sz = r.run.source.z;
+  j.src_w = r.run.source.width; j.src_h = r.run.source.height;
+  if (r.run.start_weight) {
+    j.start_weight = r.run.start_weight;
+  } else {
+    const double n1 = m->bulks[0].n, n2 = m->bulks[1].n;
+    double q = (n1 - n2) / (n1 + n2);
+    q = q * q;
+    j.start_weight = (unsigned int)((double)0xFFFFFFFF * (1 - q));
+  }
+  const mcfl_detector &d = r.run.det;
+  j.det_x0 = d.x0; j.det_y0 = d.y0; j.det_dx = d.dx; j.det_dy = d.dy;
+  j.size_x = (d.dx * (float)d.nx) / 2.0f;
+  j.size_y = (d.dy * (float)d.ny) / 2.0f;
+  j.det_nx = (uint32_t)d.nx;
+  j.xy_size = (uint32_t)xy;
+  j.R = r.R.as<unsigned long long>();
+  j.T = r.T.as<unsigned long long>();
+  j.fhd_on = r.run.fluence ? 1u : 0u;
+  j.fhd = r.run.fluence ? r.fhd.as<unsigned long long>() : nullptr;
+  j.stats = r.stats.as<unsigned long long>();
+  j.key = mcfl_stream_key(r.run.seed_exc, 0);
+  j.rng_offset = 0;
+  j.ticket_begin = r.ticket_begin;
+  j.photons = r.run.photons;
+  return MCFL_OK;
+}
+
+void mcfl_server::release(Request &r) {
+  if (r.medium) mcfl_medium_free(r.medium);
+  r.medium = nullptr;
+  r.R.release();
+  r.T.release();
+  r.fhd.release();
+  r.stats.release();
+}
+
+int mcfl_server::admit_locked(std::vector<std::shared_ptr<Request>> &to_upload) {
+  while (!queue.empty()) {
+    auto r = queue.front();
+    if (r->footprint > budget) {
+      r->status = MCFL_E_RANGE;
+      r->done = true;
+      queue.pop_front();
+      cv_done.notify_all();
+      continue;
+    }
+    if (used + r->footprint > budget) break;
+    int slot = -1;
+    for (unsigned i = 0; i < slots; ++i)
+      if (!active[i]) {
+        slot = (int)i;
+        break;
+      }
+    if (slot < 0) break;
+    queue.pop_front();
+    r->slot = slot;
+    active[slot] = r;
+    used += r->footprint;
+    to_upload.push_back(r);
+  }
+  return MCFL_OK;
+}
+
+void mcfl_server::loop() {
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  unsigned long long counter_now = 0;
+  for (;;) {
+    std::vector<std::shared_ptr<Request>> fresh;
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      bool have_active = false;
+      for (auto &a : active) have_active |= (bool)a;
+      if (!have_active && queue.empty()) {
+        if (stop) return;
+        cv.wait_for(lk, std::chrono::milliseconds(2));
+        continue;
+      }
+      admit_locked(fresh);
+    }
+    for (auto &r : fresh) {
+      r->t_admit = Clock::now();
+      r->ticket_begin = std::max<uint64_t>(tickets_end, counter_now);
+      tickets_end = r->ticket_begin + r->run.photons;
+      int rc = upload(*r);
+      if (rc != MCFL_OK) {
+        std::lock_guard<std::mutex> lk(mu);
+        r->status = rc;
+        r->done = true;
+        active[r->slot] = nullptr;
+        used -= r->footprint;
+        release(*r);
+        cv_done.notify_all();
+      }
+    }
+    /* slots in ticket order */
+    unsigned n = 0;
+    for (unsigned i = 0; i < slots; ++i)
+      if (active[i]) h_order[n++] = i;
+    if (n == 0) continue;
+    std::sort(h_order, h_order + n, [&](uint32_t a, uint32_t b) { return h_jobs[a].ticket_begin < h_jobs[b].ticket_begin; });
+    const auto t0 = Clock::now();
+    cudaMemcpyAsync(slot_jobs.p, h_jobs, slots * sizeof(McflJob), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(order.p, h_order, n * 4, cudaMemcpyHostToDevice, s);
+    McflLaunch L;
+    std::memset(&L, 0, sizeof(L));
+    L.jobs = slot_jobs.as<McflJob>();
+    L.order = order.as<uint32_t>();
+    L.n_jobs = n;
+    L.max_iters = slice_iters;
+    L.ticket_counter = counter.as<unsigned long long>();
+    L.ticket_end = tickets_end;
+    L.mult = ctx->mult.as<uint32_t>();
+    L.saved = parked.as<McflSaved>();
+    L.step_cap = ctx->step_cap;
+    cudaError_t e = ctx->launch_transport(L, grid, ctx->block);
+    cudaMemcpyAsync(h_read, counter.p, 8, cudaMemcpyDeviceToHost, s);
+    for (unsigned i = 0; i < n; ++i) {
+      Request &r = *active[h_order[i]];
+      cudaMemcpyAsync(h_read + 1 + (size_t)i * MCFL_ST_COUNT, r.stats.p, MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, s);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    const auto t1 = Clock::now();
+    busy_s += std::chrono::duration<double>(t1 - t0).count();
+    ++slices;
+    inflight_sum += n;
+    max_inflight = std::max<unsigned long long>(max_inflight, n);
+    if (e != cudaSuccess) {
+      std::lock_guard<std::mutex> lk(mu);
+      fatal = cuda_fail(e, "server slice");
+      for (auto &a : active)
+        if (a) {
+          a->status = MCFL_E_CUDA;
+          a->done = true;
+          a = nullptr;
+        }
+      for (auto &q : queue) {
+        q->status = MCFL_E_CUDA;
+        q->done = true;
+      }
+      queue.clear();
+      cv_done.notify_all();
+      return;
+    }
+    counter_now = h_read[0];
+    for (unsigned i = 0; i < n; ++i) {
+      const uint32_t slot = h_order[i];
+      std::shared_ptr<Request> r = active[slot];
+      const unsigned long long *st = h_read + 1 + (size_t)i * MCFL_ST_COUNT;
+      if (st[MCFL_ST_DONE] < r->run.photons) continue;
+      const size_t xy = (size_t)r->run.det.nx + (size_t)r->run.det.nx * r->run.det.ny;
+      r->Rd.resize(xy);
+      r->Tt.resize(xy);
+      cudaMemcpyAsync(r->Rd.data(), r->R.p, xy * 8, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(r->Tt.data(), r->T.p, xy * 8, cudaMemcpyDeviceToHost, s);
+      if (r->run.fluence) {
+        r->fhd_host.resize(r->medium->total);
+        cudaMemcpyAsync(r->fhd_host.data(), r->fhd.p, (size_t)r->medium->total * 8, cudaMemcpyDeviceToHost, s);
+      }
+      std::memcpy(r->st, st, sizeof(r->st));
+      cudaStreamSynchronize(s);
+      release(*r);
+      std::lock_guard<std::mutex> lk(mu);
+      r->t_done = Clock::now();
+      r->status = r->st[MCFL_ST_CAPPED] ? MCFL_E_CAPPED : MCFL_OK;
+      r->done = true;
+      const double lat = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+      latencies_ms.push_back(lat);
+      photons_done += r->run.photons;
+      if (!any) t_first = r->t_submit;
+      any = true;
+      t_last = r->t_done;
+      active[slot] = nullptr;
+      used -= r->footprint;
+      cv_done.notify_all();
+    }
+  }
+}
+
+extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, mcfl_server **out) {
+  if (!ctx || !out) return fail(MCFL_E_ARG, "mcfl_server_create: null argument");
+  *out = nullptr;
+  auto *sv = new mcfl_server();
+  sv->ctx = ctx;
+  size_t free_b = 0, total_b = 0;
+  cudaSetDevice(ctx->device);
+  cudaMemGetInfo(&free_b, &total_b);
+  sv->budget = opts && opts->hbm_budget_bytes ? (size_t)opts->hbm_budget_bytes : free_b / 2;
+  sv->slots = opts && opts->max_jobs ? (unsigned)opts->max_jobs : 64u;
+  sv->slice_iters = opts && opts->slice_passes ? (uint32_t)opts->slice_passes : 2048u;
+  if (sv->slots > 4096) {
+    delete sv;
+    return fail(MCFL_E_RANGE, "max_jobs above 4096");
+  }
+  sv->active.assign(sv->slots, nullptr);
+  sv->grid = ctx->grid_for(ctx->block);
+  const size_t threads = (size_t)sv->grid * ctx->block;
+  cudaError_t e = sv->slot_jobs.reserve(sv->slots * sizeof(McflJob));
+  if (!e) e = sv->order.reserve(sv->slots * 4);
+  if (!e) e = sv->counter.reserve(8);
+  if (!e) e = sv->parked.reserve(threads * sizeof(McflSaved));
+  if (!e) e = cudaMemset(sv->counter.p, 0, 8);
+  if (!e) e = cudaMemset(sv->parked.p, 0, threads * sizeof(McflSaved));
+  if (!e) e = cudaHostAlloc((void **)&sv->h_jobs, sv->slots * sizeof(McflJob), cudaHostAllocDefault);
+  if (!e) e = cudaHostAlloc((void **)&sv->h_order, sv->slots * 4, cudaHostAllocDefault);
+  if (!e) e = cudaHostAlloc((void **)&sv->h_read, (1 + (size_t)sv->slots * MCFL_ST_COUNT) * 8, cudaHostAllocDefault);
+  if (e) {
+    mcfl_server_destroy(sv);
+    return cuda_fail(e, "mcfl_server_create");
+  }
+  std::memset(sv->h_jobs, 0, sv->slots * sizeof(McflJob));
+  sv->worker = std::thread([sv] { sv->loop(); });
+  *out = sv;
+  return MCFL_OK;
+}
+
+extern "C" int mcfl_server_submit(mcfl_server *sv, const mcfl_medium_desc *medium, const mcfl_run_desc *run,
+                                  unsigned long long *id) {
+  if (!sv || !medium || !run || !id) return fail(MCFL_E_ARG, "mcfl_server_submit: null argument");
+  if (run->photons_per_voxel) return fail(MCFL_E_ARG, "server requests are excitation runs (photons_per_voxel = 0)");
+  if (run->photons == 0 || run->det.nx <= 0 || run->det.ny <= 0) return fail(MCFL_E_ARG, "bad run");
+  if (!medium->labels || !medium->bulks || medium->n_bulks < 1 || medium->n_bulks > MCFL_MAX_BULKS)
+    return fail(MCFL_E_ARG, "bad medium");
+  auto r = std::make_shared<Request>();
+  r->desc = *medium;
+  r->bulks.assign(medium->bulks, medium->bulks + medium->n_bulks + 2);
+  r->desc.bulks = r->bulks.data();
+  r->run = *run;
+  r->footprint = footprint_of(*medium, *run);
+  r->t_submit = Clock::now();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  if (sv->fatal != MCFL_OK) return fail(MCFL_E_STATE, "server stopped after a CUDA error");
+  r->id = sv->next_id++;
+  sv->queue.push_back(r);
+  sv->all[r->id] = r;
+  *id = r->id;
+  sv->cv.notify_all();
+  return MCFL_OK;
+}
+
+extern "C" int mcfl_server_wait(mcfl_server *sv, unsigned long long id, int timeout_ms) {
+  if (!sv) return fail(MCFL_E_ARG, "null server");
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto it = sv->all.find(id);
+  if (it == sv->all.end()) return fail(MCFL_E_ARG, "unknown request");
+  auto r = it->second;
+  auto pred = [&] { return r->done; };
+  if (timeout_ms < 0) sv->cv_done.wait(lk, pred);
+  else if (!sv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+    return fail(MCFL_E_TIMEOUT, "request not finished");
+  return r->status;
+}
+
+extern "C" int mcfl_server_result(mcfl_server *sv, unsigned long long id, mcfl_run_out *out, double *latency_ms) {
+  if (!sv) return fail(MCFL_E_ARG, "null server");
+  std::shared_ptr<Request> r;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    auto it = sv->all.find(id);
+    if (it == sv->all.end()) return fail(MCFL_E_ARG, "unknown request");
+    r = it->second;
+    if (!r->done) return fail(MCFL_E_STATE, "request not finished");
+    sv->all.erase(it);
+  }
+  if (r->status != MCFL_OK) return fail(r->status, "request failed");
+  if (out) {
+    if (out->Rd) std::memcpy(out->Rd, r->Rd.data(), r->Rd.size() * 8);
+    if (out->Tt) std::memcpy(out->Tt, r->Tt.data(), r->Tt.size() * 8);
+    if (out->fhd && !r->fhd_host.empty()) std::memcpy(out->fhd, r->fhd_host.data(), r->fhd_host.size() * 8);
+    std::memcpy(out->stats_exc, r->st, sizeof(r->st));
+  }
+  if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+  return MCFL_OK;
+}
+
+extern "C" int mcfl_server_metrics(mcfl_server *sv, mcfl_server_metrics_t *m) {
+  if (!sv || !m) return fail(MCFL_E_ARG, "null argument");
+  std::lock_guard<std::mutex> lk(sv->mu);
+  std::memset(m, 0, sizeof(*m));
+  std::vector<double> l = sv->latencies_ms;
+  std::sort(l.begin(), l.end());
+  auto pct = [&](double p) {
+    if (l.empty()) return 0.0;
+    const double pos = p * (double)(l.size() - 1);
+    const size_t i = (size_t)pos;
+    const double f = pos - (double)i;
+    return i + 1 < l.size() ? l[i] * (1 - f) + l[i + 1] * f : l[i];
+  };
+  m->completed = l.size();
+  m->p50_ms = pct(0.50);
+  m->p99_ms = pct(0.99);
+  m->max_ms = l.empty() ? 0.0 : l.back();
+  m->photons = sv->photons_done;
+  m->slices = sv->slices;
+  m->busy_s = sv->busy_s;
+  m->mean_inflight = sv->slices ? (double)sv->inflight_sum / (double)sv->slices : 0.0;
+  m->max_inflight = sv->max_inflight;
+  m->span_s = sv->any ? std::chrono::duration<double>(sv->t_last - sv->t_first).count() : 0.0;
+  m->hbm_used = sv->used;
+  m->hbm_budget = sv->budget;
+  return MCFL_OK;
+}
+
+extern "C" void mcfl_server_destroy(mcfl_server *sv) {
+  if (!sv) return;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+    sv->cv.notify_all();
+  }
+  if (sv->worker.joinable()) sv->worker.join();
+  for (auto &a : sv->active)
+    if (a) sv->release(*a);
+  if (sv->h_jobs) cudaFreeHost(sv->h_jobs);
+  if (sv->h_order) cudaFreeHost(sv->h_order);
+  if (sv->h_read) cudaFreeHost(sv->h_read);
+  delete sv;
+}

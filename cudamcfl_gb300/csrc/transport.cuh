@@ -131,18 +131,23 @@ __device__ __forceinline__ uint32_t start_label(const Med &m, const Photon &p) {
   return m.last;
 }
 
-/* Locates the job owning global ticket t (jobs sorted by ticket_begin). */
+__device__ __forceinline__ uint32_t slot_at(const McflLaunch &L, uint32_t i) { return L.order ? __ldg(&L.order[i]) : i; }
+
+/* Locates the job slot owning global ticket t (binary search over the slots
+ * in ticket order). */
 __device__ __forceinline__ uint32_t find_job(const McflLaunch &L, uint64_t t) {
+  if (L.n_jobs == 0) return 0xffffffffu;
   uint32_t lo = 0, hi = L.n_jobs - 1;
   while (lo < hi) {
     uint32_t mid = (lo + hi + 1) >> 1;
-    if (__ldg((const unsigned long long *)&L.jobs[mid].ticket_begin) <= t) lo = mid;
+    if (__ldg((const unsigned long long *)&L.jobs[slot_at(L, mid)].ticket_begin) <= t) lo = mid;
     else hi = mid - 1;
   }
-  const McflJob *J = &L.jobs[lo];
+  const uint32_t slot = slot_at(L, lo);
+  const McflJob *J = &L.jobs[slot];
   const uint64_t b = __ldg((const unsigned long long *)&J->ticket_begin);
   const uint64_t n = __ldg((const unsigned long long *)&J->photons);
-  return (t >= b && t - b < n) ? lo : 0xffffffffu;
+  return (t >= b && t - b < n) ? slot : 0xffffffffu;
 }
 
 __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,

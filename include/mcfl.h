@@ -278,7 +278,77 @@ int mcfl_run(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *run,
 /* The run description a .mci simulation implies. */
 int mcfl_run_desc_from_simulation(const mcfl_simulation *sim, unsigned long long seed, mcfl_run_desc *run);
 
-/* Kernel launches and GPU time issued by this context so far. */
+/* Schedules of many simulations. */
+enum {
+  MCFL_SCHEDULE_BATCHED = 0, /* all simulations in one persistent launch, replayed as a CUDA graph */
+  MCFL_SCHEDULE_PLAIN = 1    /* one launch (and host wait) per simulation, as the reference */
+};
+
+/* Runs n excitation-only simulations (sources, budgets, seeds) on one medium,
+ * each with its own R/T images; detectors must share nx, ny.  Both schedules
+ * give bit-identical images.  outs (n entries, may be NULL) receive the
+ * requested images and per-simulation stats; gpu_ms the GPU time of the
+ * transport launches. */
+int mcfl_batch_run(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *runs, int n, int schedule,
+                   mcfl_run_out *outs, float *gpu_ms);
+
+/* The two-phase run with its emission phase scheduled as the reference's
+ * voxel loop does it (CUDAMCFLmain.cu:471-594): one launch and host wait per
+ * emitting voxel.  With max_voxels > 0 only the first max_voxels emitting
+ * voxels are simulated (to time the schedule on a sample).  Over all voxels
+ * the images equal those of mcfl_run bit for bit. */
+int mcfl_run_plain(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *run, long long max_voxels,
+                   mcfl_run_out *out);
+
+/* ---------------------------------------------------------------------- */
+/* Continuous-batching server                                              */
+/* ---------------------------------------------------------------------- */
+
+typedef struct mcfl_server mcfl_server;
+
+typedef struct mcfl_server_opts {
+  unsigned long long hbm_budget_bytes; /* admission budget (0: half the free HBM) */
+  unsigned int max_jobs;               /* concurrent jobs (0: 64) */
+  unsigned int slice_passes;           /* transport passes per thread per slice (0: 2048) */
+} mcfl_server_opts;
+
+typedef struct mcfl_server_metrics_t {
+  unsigned long long completed;     /* requests finished */
+  double p50_ms, p99_ms, max_ms;    /* submit-to-completion latency */
+  unsigned long long photons;       /* photons of finished requests */
+  unsigned long long slices;        /* persistent-kernel slices launched */
+  double busy_s;                    /* wall time spent in slices */
+  double span_s;                    /* first submit to last completion */
+  double mean_inflight;             /* jobs per slice, mean */
+  unsigned long long max_inflight;  /* jobs per slice, maximum */
+  unsigned long long hbm_used, hbm_budget;
+} mcfl_server_metrics_t;
+
+/* Starts the server thread; it owns ctx (and its stream) until
+ * mcfl_server_destroy. */
+int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, mcfl_server **server);
+
+/* Queues one request: an excitation run (photons_per_voxel = 0, fluence
+ * optional) on its own medium.  Thread-safe.  The medium's host arrays must
+ * stay valid until mcfl_server_wait reports the request finished.  Requests
+ * larger than the HBM budget finish with MCFL_E_RANGE. */
+int mcfl_server_submit(mcfl_server *server, const mcfl_medium_desc *medium, const mcfl_run_desc *run,
+                       unsigned long long *id);
+
+/* Waits for a request (timeout_ms < 0: no limit).  Returns its status, or
+ * MCFL_E_TIMEOUT. */
+int mcfl_server_wait(mcfl_server *server, unsigned long long id, int timeout_ms);
+
+/* Copies a finished request's raw R/T images, photon hitting density and
+ * stats, and forgets the request. */
+int mcfl_server_result(mcfl_server *server, unsigned long long id, mcfl_run_out *out, double *latency_ms);
+
+int mcfl_server_metrics(mcfl_server *server, mcfl_server_metrics_t *metrics);
+
+/* Finishes the admitted and queued requests, then stops the thread. */
+void mcfl_server_destroy(mcfl_server *server);
+
+/* Kernel launches issued by this context so far. */
 unsigned long long mcfl_launch_count(const mcfl_ctx *ctx);
 
 #ifdef __cplusplus

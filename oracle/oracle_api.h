@@ -62,6 +62,15 @@ typedef struct oracle_sim {
   float det_x0, det_y0;
   oracle_bulk bulks[ORACLE_MAX_BULKS + 2];
   const short *bulk_info; /* num_x*num_y*num_z labels, x fastest */
+  /* Optional general geometry (not expressible in a .mci file): when nx > 0
+   * the grid is nx*ny*nz voxels, |x| < half_x, |y| < half_y, 0 <= z < esp,
+   * with vox_per_cm voxels per cm per axis.  Otherwise the reference's
+   * geometry: half extents 2*esp and grid_size voxels per cm. */
+  int nx, ny, nz;
+  float half_x, half_y;
+  float vox_per_cm[3];
+  const float *fluor_map; /* optional emission-strength factor per voxel */
+  long max_fl_voxels;     /* refstream only: stop after this many emitting voxels (0: all) */
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);

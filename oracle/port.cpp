@@ -96,7 +96,8 @@ struct Photon {
 /* Everything one transport phase reads (the reference's __constant__ set). */
 struct Phase {
   float esp;
-  unsigned grid;
+  float hx, hy;     /* half lateral extents (2*esp in the reference) */
+  float gx, gy, gz; /* voxels per cm (grid_size in the reference) */
   unsigned num_x, num_y, num_z;
   unsigned total;
   float size_x, size_y;
@@ -113,9 +114,8 @@ struct Phase {
 };
 
 inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
-  const float gf = mcfl_i2f_rn((int)ph.grid);
-  unsigned idx = mcfl_f2u_rz((x + 2 * ph.esp) * gf) +
-                 ph.num_x * (mcfl_f2u_rz((y + 2 * ph.esp) * gf) + ph.num_y * mcfl_f2u_rz(z * gf));
+  unsigned idx = mcfl_f2u_rz((x + ph.hx) * ph.gx) +
+                 ph.num_x * (mcfl_f2u_rz((y + ph.hy) * ph.gy) + ph.num_y * mcfl_f2u_rz(z * ph.gz));
   return idx < ph.total ? idx : ph.total - 1;
 }
 
@@ -127,7 +127,7 @@ inline unsigned pixel_index(const Phase &ph, float x, float y) {
 
 inline uint32_t start_label(const Phase &ph, const Photon &p) {
   if (p.z < ph.esp) {
-    if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp) return (uint32_t)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
+    if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy) return (uint32_t)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
     return 1;
   }
   return ph.last_bulk;
@@ -136,10 +136,9 @@ inline uint32_t start_label(const Phase &ph, const Photon &p) {
 template <class M>
 void launch_photon(Photon &p, Rng &r, const Phase &ph, float xi, float yi, float zi) {
   if (ph.dir == 0.0f) {
-    const float gf = mcfl_i2f_rn((int)ph.grid);
-    p.x = xi + (0.999999f / gf) * r.oc();
-    p.y = yi + (0.999999f / gf) * r.oc();
-    p.z = zi + (0.999999f / gf) * r.oc();
+    p.x = xi + (0.999999f / ph.gx) * r.oc();
+    p.y = yi + (0.999999f / ph.gy) * r.oc();
+    p.z = zi + (0.999999f / ph.gz) * r.oc();
     float costheta = (float)(1.0 - 2.0 * (double)r.oc());
     float sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
     float psi = (float)(2.0 * (double)kPi * (double)r.oc());
@@ -241,7 +240,7 @@ inline unsigned reflect(Photon &p, uint32_t newlb, Rng &r, const Phase &ph) {
  * around the centre of the voxel reached. */
 inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase &ph, float max_s) {
   const unsigned num_x = ph.num_x, num_y = ph.num_y;
-  const float gf = mcfl_i2f_rn((int)ph.grid);
+  const float gf = ph.gx;
   float search_step = 1 / (2 * gf);
   float total_move = 0;
   int index = 1;
@@ -258,7 +257,7 @@ inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase
       present_bulk = ph.last_bulk;
       index = -1;
       search_step = (ph.esp - p.z) / p.dz;
-    } else if (fabsf(p.x + p.dx * search_step) >= 2 * ph.esp || fabsf(p.y + p.dy * search_step) >= 2 * ph.esp) {
+    } else if (fabsf(p.x + p.dx * search_step) >= ph.hx || fabsf(p.y + p.dy * search_step) >= ph.hy) {
       present_bulk = 1;
       index = -1;
     } else {
@@ -273,10 +272,10 @@ inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase
     uidx -= z_grid * num_x * num_y;
     unsigned y_grid = uidx / num_x;
     unsigned x_grid = uidx % num_x;
-    const double half = 1. / (2. * (double)ph.grid);
-    float y_voxel = (float)((double)(mcfl_i2f_rn((int)y_grid) / (float)ph.grid - 2 * ph.esp) + half);
-    float x_voxel = (float)((double)(mcfl_i2f_rn((int)x_grid) / (float)ph.grid - 2 * ph.esp) + half);
-    float z_voxel = (float)((double)(mcfl_i2f_rn((int)z_grid) / (float)ph.grid) + half);
+    const double half = 1. / (2. * (double)ph.gx);
+    float y_voxel = (float)((double)(mcfl_i2f_rn((int)y_grid) / ph.gy - ph.hy) + half);
+    float x_voxel = (float)((double)(mcfl_i2f_rn((int)x_grid) / ph.gx - ph.hx) + half);
+    float z_voxel = (float)((double)(mcfl_i2f_rn((int)z_grid) / ph.gz) + half);
     const double rv = 0.707107 * (double)(1 / gf);
     float r_voxel2 = (float)(rv * rv);
     float pow_dx = p.dx * p.dx, pow_dy = p.dy * p.dy, pow_dz = p.dz * p.dz;
@@ -372,7 +371,7 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
     p.y += p.dy * s;
     p.z += p.dz * s;
     if (new_bulk != 0 && new_bulk != last_bulk) {
-      if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp && p.z < ph.esp)
+      if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy && p.z < ph.esp)
         new_bulk = (uint32_t)(unsigned short)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
       else
         new_bulk = 1;
@@ -382,7 +381,7 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
     new_bulk = move_to_first_boundary(p, p.bulkpos, ph, s);
   }
   if (new_bulk != p.bulkpos) reflect(p, new_bulk, r, ph);
-  if (fabsf(p.x) < 2 * ph.esp && fabsf(p.y) < 2 * ph.esp && p.z < ph.esp && ph.fhd_on == 1)
+  if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy && p.z < ph.esp && ph.fhd_on == 1)
     add_guarded(&sk.fhd[voxel_index(ph, p.x, p.y, p.z)], p.weight, ph.guard);
   if (p.bulkpos == 0) {
     if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
@@ -424,11 +423,23 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
 void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
   memset(&ph, 0, sizeof(ph));
   ph.esp = sim->esp;
-  ph.grid = (unsigned)sim->grid_size;
-  const float gf = mcfl_i2f_rn(sim->grid_size);
-  ph.num_x = mcfl_f2u_rn(4 * ph.esp * gf);
-  ph.num_y = mcfl_f2u_rn(4 * ph.esp * gf);
-  ph.num_z = (unsigned)(int)(sim->esp * (float)sim->grid_size);
+  if (sim->nx > 0) {
+    ph.hx = sim->half_x;
+    ph.hy = sim->half_y;
+    ph.gx = sim->vox_per_cm[0];
+    ph.gy = sim->vox_per_cm[1];
+    ph.gz = sim->vox_per_cm[2];
+    ph.num_x = (unsigned)sim->nx;
+    ph.num_y = (unsigned)sim->ny;
+    ph.num_z = (unsigned)sim->nz;
+  } else {
+    const float gf = mcfl_i2f_rn(sim->grid_size);
+    ph.hx = ph.hy = 2 * ph.esp;
+    ph.gx = ph.gy = ph.gz = gf;
+    ph.num_x = mcfl_f2u_rn(4 * ph.esp * gf);
+    ph.num_y = mcfl_f2u_rn(4 * ph.esp * gf);
+    ph.num_z = (unsigned)(int)(sim->esp * (float)sim->grid_size);
+  }
   ph.total = ph.num_x * ph.num_y * ph.num_z;
   ph.det_dx = sim->det_dx; ph.det_dy = sim->det_dy;
   ph.det_x0 = sim->det_x0; ph.det_y0 = sim->det_y0;
@@ -588,9 +599,10 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
         unsigned index = ix + ph.num_x * (iy + iz * ph.num_y);
         short bd = sim->bulk_info[index];
         if (!(sim->bulks[bd].albedof < 1)) continue; /* adds 0 * image in the reference */
-        float xi = ((float)ix / (float)sim->grid_size) - 2 * sim->esp;
-        float yi = ((float)iy / (float)sim->grid_size) - 2 * sim->esp;
-        float zi = ((float)iz / (float)sim->grid_size);
+        if (sim->max_fl_voxels > 0 && res->fl_voxels >= sim->max_fl_voxels) return 0;
+        float xi = ((float)ix / ph.gx) - ph.hx;
+        float yi = ((float)iy / ph.gy) - ph.hy;
+        float zi = ((float)iz / ph.gz);
         fl.xi = xi; fl.yi = yi; fl.zi = zi;
         std::fill(tR.begin(), tR.end(), 0ull);
         std::fill(tT.begin(), tT.end(), 0ull);
@@ -628,9 +640,9 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
     if (vox) {
       uint32_t v = vox[k / nv];
       unsigned ix = v % ph.num_x, iy = (v / ph.num_x) % ph.num_y, iz = v / (ph.num_x * ph.num_y);
-      float xi = ((float)ix / (float)ph.grid) - 2 * ph.esp;
-      float yi = ((float)iy / (float)ph.grid) - 2 * ph.esp;
-      float zi = ((float)iz / (float)ph.grid);
+      float xi = ((float)ix / ph.gx) - ph.hx;
+      float yi = ((float)iy / ph.gy) - ph.hy;
+      float zi = ((float)iz / ph.gz);
       sk.voxel_q = voxq[k / nv];
       launch_photon<M>(p, r, ph, xi, yi, zi);
     } else {
@@ -677,6 +689,7 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
     if (!(b.albedof < 1)) continue;
     double fx = (double)res->fhd[v] / (double)(0xFFFFFFFFull * N);
     double wv = (double)b.eY * (double)(1 - b.albedof) * fx;
+    if (sim->fluor_map) wv = wv * (double)sim->fluor_map[v];
     double qs = nearbyint(wv * 0x1p40);
     uint64_t qv = qs >= 18446744073709551615.0 ? 0xFFFFFFFFFFFFFFFFull : (uint64_t)qs;
     if (qv == 0) continue;

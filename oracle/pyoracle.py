@@ -79,6 +79,14 @@ class CSim(ctypes.Structure):
         ("det_y0", ctypes.c_float),
         ("bulks", CBulk * (MAX_BULKS + 2)),
         ("bulk_info", ctypes.POINTER(ctypes.c_short)),
+        ("nx", ctypes.c_int),
+        ("ny", ctypes.c_int),
+        ("nz", ctypes.c_int),
+        ("half_x", ctypes.c_float),
+        ("half_y", ctypes.c_float),
+        ("vox_per_cm", ctypes.c_float * 3),
+        ("fluor_map", ctypes.POINTER(ctypes.c_float)),
+        ("max_fl_voxels", ctypes.c_long),
     ]
 
 
@@ -269,3 +277,43 @@ def sim_from_fields(labels: np.ndarray, bulks: list[dict], *, esp: float, grid_s
     lab = np.ascontiguousarray(labels, dtype=np.int16)
     s.bulk_info = lab.ctypes.data_as(ctypes.POINTER(ctypes.c_short))
     return s, lab
+
+
+def sim_from_arrays(labels: np.ndarray, bulks, *, half_x: float, half_y: float, thickness: float, vox_per_cm,
+                    photons: int, per_voxel: int, det: tuple, source=(0.0, 0.0, 0.0), start_weight: int = 0,
+                    fluor_map: np.ndarray | None = None, do_fl: int = 1) -> "CSim":
+    """A general-geometry simulation over (nz, ny, nx) labels with the same
+    floats the engine uses for its medium.  bulks: objects with the fields of
+    mcfl_bulk (mutr, mua, g, n, flc, muaf, eY, albedof), n+2 entries.  The
+    returned structure keeps its arrays alive."""
+    s = CSim()
+    s.bulk_method = 2
+    s.number_of_photons = photons
+    s.number_of_photons_per_voxel = per_voxel
+    s.esp = thickness
+    s.grid_size = 0
+    s.do_fl_sim = do_fl
+    s.fhd_activated = 1 if do_fl in (1, 2) else 0
+    s.det_dx, s.det_dy, s.det_nx, s.det_ny, s.det_x0, s.det_y0 = det
+    s.xi, s.yi, s.zi = source
+    s.dir = 1.0
+    s.n_bulks = len(bulks) - 2
+    for i, b in enumerate(bulks):
+        s.bulks[i] = CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof)
+    if start_weight == 0:
+        n1, n2 = np.float64(np.float32(bulks[0].n)), np.float64(np.float32(bulks[1].n))
+        r = (n1 - n2) / (n1 + n2)
+        start_weight = int(np.float64(0xFFFFFFFF) * (1 - r * r))
+    s.start_weight = start_weight
+    lab = np.ascontiguousarray(labels.astype(np.int16))
+    s.bulk_info = lab.ctypes.data_as(ctypes.POINTER(ctypes.c_short))
+    s.nz, s.ny, s.nx = lab.shape
+    s.half_x, s.half_y = half_x, half_y
+    s.vox_per_cm[:] = list(vox_per_cm)
+    keep = [lab]
+    if fluor_map is not None:
+        fm = np.ascontiguousarray(fluor_map, dtype=np.float32)
+        s.fluor_map = fm.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        keep.append(fm)
+    s._keep = keep
+    return s

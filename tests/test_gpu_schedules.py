@@ -1,0 +1,134 @@
+"""Batching, the plain schedule, graph replay and the continuous-batching
+server.  Every schedule must reproduce the tallies of the same simulation run
+alone, bit for bit: photon k of a simulation always draws stream
+(key, offset + k) and all tallies are integer sums."""
+import numpy as np
+import pytest
+
+import cudamcfl_gb300 as mc
+from cudamcfl_gb300 import media
+from tests import cases
+
+
+def _alone(ctx, med, rd):
+    return ctx.run(med, rd, images=True, raw=True)
+
+
+@pytest.mark.gpu
+def test_batched_equals_plain_equals_alone(gpu_ctx):
+    case = cases.sphere()
+    med = case.engine_medium(gpu_ctx)
+    dx, dy, nx, ny, x0, y0 = case.det
+    det = mc.Detector(x0, y0, dx, dy, nx, ny)
+    srcs = [(-0.3, 0.1), (0.0, 0.0), (0.25, -0.2), (0.5, 0.5), (-0.6, -0.4)]
+    budgets = [3000, 20000, 7000, 12000, 500]
+    runs = [mc.run_desc(b, source=(x, y, 0.0), det=det, seed_exc=100 + i, start_weight=case.start_weight())
+            for i, ((x, y), b) in enumerate(zip(srcs, budgets))]
+    bat, _ = mc.batch_run(gpu_ctx, med, runs, mc.SCHEDULE_BATCHED)
+    pla, _ = mc.batch_run(gpu_ctx, med, runs, mc.SCHEDULE_PLAIN)
+    for i, rd in enumerate(runs):
+        one = _alone(gpu_ctx, med, rd)
+        for r in (bat[i], pla[i]):
+            assert np.array_equal(r["Rd"], one.Rd) and np.array_equal(r["Tt"], one.Tt)
+            assert np.array_equal(r["R"], one.R) and np.array_equal(r["T"], one.T)
+            assert r["stats"]["done"] == budgets[i]
+            assert r["stats"]["absorbed"] == one.stats_exc["absorbed"]
+    # replaying the recorded batch graph reproduces it
+    bat2, _ = mc.batch_run(gpu_ctx, med, runs, mc.SCHEDULE_BATCHED)
+    for a, b in zip(bat, bat2):
+        assert np.array_equal(a["Rd"], b["Rd"]) and np.array_equal(a["Tt"], b["Tt"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tiny", "sphere"])
+def test_plain_per_voxel_emission_equals_batched(name, gpu_ctx):
+    case = cases.ALL[name](photons=20000, per_voxel=300)
+    med = case.engine_medium(gpu_ctx)
+    rd = case.run_desc(31, 32)
+    bat = gpu_ctx.run(med, rd)
+    pla = mc.run_plain(gpu_ctx, med, rd)
+    assert pla["fl_voxels"] == bat.fl_voxels > 0
+    assert np.array_equal(pla["Rd"], bat.Rd) and np.array_equal(pla["Tt"], bat.Tt)
+    assert np.array_equal(pla["flR128"], bat.flR128) and np.array_equal(pla["flT128"], bat.flT128)
+    assert pla["stats_fl"]["steps"] == bat.stats_fl["steps"]
+
+
+@pytest.mark.gpu
+def test_graph_replay_follows_new_seeds(gpu_ctx):
+    case = cases.mismatch(photons=20000, per_voxel=100)
+    med = case.engine_medium(gpu_ctx)
+    a1 = gpu_ctx.run(med, case.run_desc(1, 2))
+    b = gpu_ctx.run(med, case.run_desc(3, 4))
+    a2 = gpu_ctx.run(med, case.run_desc(1, 2))
+    assert np.array_equal(a1.Rd, a2.Rd) and np.array_equal(a1.flR128, a2.flR128)
+    assert not np.array_equal(a1.Rd, b.Rd)
+    gpu_ctx.set_option("graphs", 0)
+    try:
+        a3 = gpu_ctx.run(med, case.run_desc(1, 2))
+    finally:
+        gpu_ctx.set_option("graphs", 1)
+    assert np.array_equal(a1.Rd, a3.Rd) and np.array_equal(a1.fhd, a3.fhd)
+
+
+def _request_media(seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i, (nx, ny, nz) in enumerate([(32, 32, 16), (48, 40, 24), (64, 64, 32), (24, 24, 24)]):
+        vox = (0.05, 0.05, 0.05)
+        lab = np.ones((nz, ny, nx), dtype=np.uint8)
+        media.add_sphere(lab, vox, (rng.uniform(-0.3, 0.3), rng.uniform(-0.3, 0.3), nz * 0.05 / 2), 0.3, 2)
+        bulks = [mc.outer_bulk(1.0), mc.bulk_from_mci_columns(1.4, 0.1 + 0.05 * i, 80.0 + 10 * i, g=0.85),
+                 mc.bulk_from_mci_columns(1.33, 0.5, 50.0, g=0.7), mc.outer_bulk(1.0)]
+        out.append((lab, bulks, vox))
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("slice_passes", [64, 4096])
+def test_server_results_equal_alone(slice_passes, gpu_ctx):
+    meds = _request_media(7)
+    det = mc.Detector(0.0, 0.0, 0.05, 0.05, 30, 30)
+    reqs = []
+    for i in range(10):
+        lab, bulks, vox = meds[i % len(meds)]
+        kind = mc.SOURCE_WIDEFIELD if i % 3 == 0 else mc.SOURCE_GAUSS_BEAM
+        rd = mc.run_desc(2000 + 1500 * i, source=(0.05 * i - 0.2, 0.0, 0.0), det=det, fluence=i % 2,
+                         seed_exc=500 + i, kind=kind, width=1.0, height=0.8)
+        reqs.append((lab, bulks, vox, rd))
+    ctx2 = mc.Context(math=mc.MATH_EXACT)
+    srv = mc.Server(ctx2, hbm_budget_bytes=64 << 20, max_jobs=4, slice_passes=slice_passes)
+    try:
+        ids = [srv.submit(lab, bulks, vox, rd) for lab, bulks, vox, rd in reqs]
+        results = []
+        for rid in ids:
+            assert srv.wait(rid, 120000) == 0
+            results.append(srv.result(rid))
+        m = srv.metrics()
+        assert m["completed"] == len(reqs) and m["max_inflight"] > 1
+    finally:
+        srv.close()
+        ctx2.close()
+    for (lab, bulks, vox, rd), res in zip(reqs, results):
+        med = gpu_ctx.medium(lab, bulks, voxel_cm=vox)
+        one = gpu_ctx.run(med, rd)
+        assert np.array_equal(res["Rd"], one.Rd) and np.array_equal(res["Tt"], one.Tt)
+        assert res["stats"]["absorbed"] == one.stats_exc["absorbed"]
+        assert res["stats"]["steps"] == one.stats_exc["steps"]
+        if rd.fluence:
+            assert np.array_equal(res["fhd"], one.fhd)
+        med.free()
+
+
+@pytest.mark.gpu
+def test_server_rejects_request_above_budget(gpu_ctx):
+    lab = np.ones((64, 64, 64), dtype=np.uint8)
+    bulks = [mc.outer_bulk(1.0), mc.bulk_from_mci_columns(1.4, 0.1, 100.0), mc.outer_bulk(1.0)]
+    det = mc.Detector(0.0, 0.0, 0.05, 0.05, 10, 10)
+    ctx2 = mc.Context()
+    srv = mc.Server(ctx2, hbm_budget_bytes=1 << 16, max_jobs=2)
+    try:
+        rid = srv.submit(lab, bulks, (0.05, 0.05, 0.05), mc.run_desc(1000, det=det))
+        assert srv.wait(rid, 60000) == mc.E_RANGE
+    finally:
+        srv.close()
+        ctx2.close()

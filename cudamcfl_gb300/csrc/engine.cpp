@@ -172,6 +172,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;
   if (k == "graphs") return c->use_graphs;
+  if (k == "graph_failed") return c->graph_error.empty() ? 0 : 1;
   if (k == "sm_count") return c->sm_count;
   if (k == "grid") return c->grid_for(c->block);
   if (k == "regs") {

@@ -108,6 +108,7 @@ struct mcfl_ctx {
   std::string graph_run_key, graph_batch_key;
   unsigned graph_run_kernels = 0, graph_batch_kernels = 0;
   int use_graphs = 1;
+  std::string graph_error; /* why graphs were switched off, if they were */
   mcfl::DevBuf bR, bT, bstats, bcnt, seg_scale; /* batch workspace */
   int math = MCFL_MATH_EXACT;
   int block = 256;

@@ -105,43 +105,68 @@ cudaError_t ensure_pinned(mcfl_ctx *c, size_t jobs, size_t outs) {
   return cudaSuccess;
 }
 
+/* Event record that becomes a timing node when the stream is being
+ * captured into a graph. */
+cudaError_t record_event(cudaEvent_t ev, cudaStream_t s) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &cs);
+  if (e != cudaSuccess) return e;
+  return cs == cudaStreamCaptureStatusActive ? cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal)
+                                             : cudaEventRecord(ev, s);
+}
+
 /* Replays a recorded launch sequence as a CUDA graph, recording it again when
  * the key (every pointer and size the sequence bakes in) changes.  On the
- * legacy default stream, or with graphs off, the sequence runs directly. */
-cudaError_t replay(mcfl_ctx *c, cudaGraphExec_t *exec, std::string *cur_key, unsigned *kernels,
-                   const std::string &key, const std::function<cudaError_t(cudaStream_t, unsigned *)> &record) {
+ * legacy default stream, with graphs off, or when a capture cannot be made,
+ * the sequence runs directly. */
+int replay(mcfl_ctx *c, cudaGraphExec_t *exec, std::string *cur_key, unsigned *kernels, const std::string &key,
+           const std::function<cudaError_t(cudaStream_t, unsigned *)> &record) {
   cudaStream_t s = c->stream;
-  if (!c->use_graphs || s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) {
+  auto direct = [&]() -> int {
     unsigned k = 0;
     cudaError_t e = record(s, &k);
     c->launches += k;
-    return e;
-  }
+    return e == cudaSuccess ? MCFL_OK : cuda_fail(e, "launch sequence");
+  };
+  if (!c->use_graphs || s == nullptr || s == cudaStreamLegacy || s == cudaStreamPerThread) return direct();
   if (*exec == nullptr || *cur_key != key) {
     if (*exec) cudaGraphExecDestroy(*exec);
     *exec = nullptr;
+    cur_key->clear();
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
-    if (e != cudaSuccess) return e;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamBeginCapture");
     unsigned k = 0;
     cudaError_t er = record(s, &k);
     e = cudaStreamEndCapture(s, &g);
-    if (er != cudaSuccess) {
-      if (g) cudaGraphDestroy(g);
-      return er;
-    }
-    if (e != cudaSuccess) return e;
-    e = cudaGraphInstantiate(exec, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) {
+    if (er == cudaSuccess && e == cudaSuccess) e = cudaGraphInstantiate(exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (er != cudaSuccess || e != cudaSuccess) {
+      /* not capturable here: keep the context working without graphs */
+      cudaGetLastError();
       *exec = nullptr;
-      return e;
+      c->use_graphs = 0;
+      c->graph_error = std::string(cudaGetErrorString(er != cudaSuccess ? er : e));
+      return direct();
     }
     *cur_key = key;
     *kernels = k;
   }
   c->launches += *kernels;
-  return cudaGraphLaunch(*exec, s);
+  cudaError_t e = cudaGraphLaunch(*exec, s);
+  return e == cudaSuccess ? MCFL_OK : cuda_fail(e, "cudaGraphLaunch");
+}
+
+/* GPU time between two events; 0 when they hold no record.  Clears the
+ * runtime's last-error slot so a failed query cannot leak into a later
+ * launch check. */
+float elapsed_ms(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();
+    ms = 0.f;
+  }
+  return ms;
 }
 
 std::string ptr_key(std::initializer_list<const void *> ps, std::initializer_list<unsigned long long> vs) {
@@ -173,10 +198,12 @@ McflLaunch base_launch(mcfl_ctx *c) {
 extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run, mcfl_run_out *out) {
   int rc = check_run(c, m, run);
   if (rc) return rc;
+  cudaGetLastError();
   const mcfl_detector &det = run->det;
   const bool emission = run->photons_per_voxel > 0;
   const bool fluence = emission || run->fluence;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
+  cudaGetLastError();
   cudaStream_t s = c->stream;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   const size_t nv = m->total;
@@ -249,11 +276,11 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.n_jobs = 1;
     L.ticket_counter = cnt + 0;
     L.ticket_end = photons;
-    REC(cudaEventRecord(c->ev[0], st));
+    REC(record_event(c->ev[0], st));
     REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
                                   : mcfl_launch_transport_exact(&L, grid, block, st));
     ++*k;
-    REC(cudaEventRecord(c->ev[1], st));
+    REC(record_event(c->ev[1], st));
     if (emission) {
       REC(mcfl_launch_emission_prep(m->labels.as<uint8_t>(), m->fl.as<float2>(), c->fhd.as<unsigned long long>(),
                                     m->has_fmap ? m->fmap.as<float>() : nullptr, m->total, photons, per_voxel,
@@ -264,11 +291,11 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       Lf.jobs = c->jobs.as<McflJob>() + 1;
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
-      REC(cudaEventRecord(c->ev[2], st));
+      REC(record_event(c->ev[2], st));
       REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&Lf, grid, block, st)
                                     : mcfl_launch_transport_exact(&Lf, grid, block, st));
       ++*k;
-      REC(cudaEventRecord(c->ev[3], st));
+      REC(record_event(c->ev[3], st));
     }
     REC(cudaMemcpyAsync(c->h_out, c->stats.p, 2 * MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, st));
     REC(cudaMemcpyAsync(c->h_out + 2 * MCFL_ST_COUNT, c->counters.p, 4 * 8, cudaMemcpyDeviceToHost, st));
@@ -280,7 +307,8 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                   {xy, nv, (unsigned long long)emission, (unsigned long long)fluence, photons,
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
                                    (unsigned long long)block, c->step_cap});
-  MCFL_CUDA_TRY(replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record));
+  rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
+  if (rc != MCFL_OK) return rc;
 
   /* FP64 normalisation of the requested images on the GPU */
   std::vector<std::pair<double *, std::pair<double *, size_t>>> pend;
@@ -333,9 +361,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     out->energy_exc[1] = tb / launched;
     out->energy_exc[2] = a / launched;
     out->energy_exc[3] = (launched - (a + rt + tb + lost)) / launched;
-    cudaEventElapsedTime(&out->ms_exc, c->ev[0], c->ev[1]);
+    out->ms_exc = elapsed_ms(c->ev[0], c->ev[1]);
     out->ms_fl = 0.f;
-    if (emission) cudaEventElapsedTime(&out->ms_fl, c->ev[2], c->ev[3]);
+    if (emission) out->ms_fl = elapsed_ms(c->ev[2], c->ev[3]);
   }
   if (st[MCFL_ST_CAPPED] || st[MCFL_ST_COUNT + MCFL_ST_CAPPED])
     return fail(MCFL_E_CAPPED, "photons reached the per-photon pass cap");
@@ -359,6 +387,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     if (d.nx != det.nx || d.ny != det.ny) return fail(MCFL_E_ARG, "mcfl_batch_run: detectors must share a size");
   }
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
+  cudaGetLastError();
   cudaStream_t s = c->stream;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   const size_t N = (size_t)n;
@@ -400,21 +429,22 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = (uint32_t)n;
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
-      if ((e = cudaEventRecord(c->ev[0], st))) return e;
+      if ((e = record_event(c->ev[0], st))) return e;
       if ((e = c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
                                          : mcfl_launch_transport_exact(&L, grid, block, st)))
         return e;
       ++*k;
-      if ((e = cudaEventRecord(c->ev[1], st))) return e;
+      if ((e = record_event(c->ev[1], st))) return e;
       return cudaMemcpyAsync(c->h_out, c->bstats.p, N * MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, st);
     };
     const std::string key =
         ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
                  c->step_cap});
-    MCFL_CUDA_TRY(replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record));
+    const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
+    if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    ms = elapsed_ms(c->ev[0], c->ev[1]);
   } else {
     MCFL_CUDA_TRY(cudaMemsetAsync(c->bR.p, 0, N * xy * 8, s));
     MCFL_CUDA_TRY(cudaMemsetAsync(c->bT.p, 0, N * xy * 8, s));
@@ -434,7 +464,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     MCFL_CUDA_TRY(cudaEventRecord(c->ev[1], s));
     MCFL_CUDA_TRY(cudaMemcpyAsync(c->h_out, c->bstats.p, N * MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, s));
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
-    cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]);
+    ms = elapsed_ms(c->ev[0], c->ev[1]);
   }
   if (gpu_ms) *gpu_ms = ms;
   bool capped = false;
@@ -483,6 +513,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   if (run->photons_per_voxel == 0) return mcfl_run(c, m, run, out);
   const mcfl_detector &det = run->det;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
+  cudaGetLastError();
   cudaStream_t s = c->stream;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   const size_t nv = m->total;
@@ -564,8 +595,8 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     std::memcpy(out->stats_fl, c->h_out + MCFL_ST_COUNT, MCFL_ST_COUNT * 8);
     out->fl_voxels = (long long)NL;
     out->photons_fl = (unsigned long long)NL * run->photons_per_voxel;
-    cudaEventElapsedTime(&out->ms_exc, c->ev[0], c->ev[1]);
-    cudaEventElapsedTime(&out->ms_fl, c->ev[2], c->ev[3]);
+    out->ms_exc = elapsed_ms(c->ev[0], c->ev[1]);
+    out->ms_fl = elapsed_ms(c->ev[2], c->ev[3]);
   }
   return MCFL_OK;
 }
@@ -578,6 +609,7 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   cudaStream_t s = c->stream;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
+  cudaGetLastError();
   MCFL_CUDA_TRY(c->R128.reserve(xy * 16));
   MCFL_CUDA_TRY(c->T128.reserve(xy * 16));
   MCFL_CUDA_TRY(c->vox.reserve(64));

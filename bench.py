@@ -189,9 +189,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
     ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,batching,serving,cpu,e2e")
+    ap.add_argument("--profile", action="store_true",
+                    help="small case for ncu: the benchmark medium, --photons excitation photons and 20 emission "
+                         "photons per voxel, --warmup runs then one run (2 transport launches per run)")
+    ap.add_argument("--photons", type=int, default=2_000_000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.profile:
+        return profile_case(args)
 
     import torch
     import cudamcfl_gb300 as mc
@@ -385,6 +391,25 @@ def main():
     print(json.dumps(result), flush=True)
     if dist:
         torch.distributed.destroy_process_group()
+    return 0
+
+
+def profile_case(args):
+    import cudamcfl_gb300 as mc
+    from cudamcfl_gb300 import build, media
+    build.build()
+    ctx = mc.Context(device=0, math=mc.MATH_FAST if args.math == "fast" else mc.MATH_EXACT)
+    m = media.config2(seed=2)
+    med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
+    rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=20, fluence=1, seed_exc=1, seed_fl=2)
+    for _ in range(args.warmup + 1):
+        r = ctx.run(med, rd, images=False, raw=False)
+    print(json.dumps({"profile_case": "config2", "math": args.math, "photons": args.photons,
+                      "emission_photons": r.photons_fl, "steps_exc": r.stats_exc["steps"],
+                      "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
+                      "regs": ctx.get_option("regs"), "grid": ctx.get_option("grid")}), flush=True)
+    med.free()
+    ctx.close()
     return 0
 
 

@@ -64,10 +64,15 @@ void DevBuf::release() {
 using namespace mcfl;
 
 
-int mcfl_ctx::grid_for(int block_size, int *bps_out) {
+int mcfl_ctx::grid_for(int block_size, int *bps_out, bool uniform) {
   int bps = 0, regs = 0;
-  cudaError_t e = math == MCFL_MATH_FAST ? mcfl_attr_transport_fast(block_size, &bps, &regs)
-                                         : mcfl_attr_transport_exact(block_size, &bps, &regs);
+  cudaError_t e;
+  if (uniform)
+    e = math == MCFL_MATH_FAST ? mcfl_attr_transport_fast_uniform(block_size, &bps, &regs)
+                               : mcfl_attr_transport_exact_uniform(block_size, &bps, &regs);
+  else
+    e = math == MCFL_MATH_FAST ? mcfl_attr_transport_fast(block_size, &bps, &regs)
+                               : mcfl_attr_transport_exact(block_size, &bps, &regs);
   if (e != cudaSuccess || bps <= 0) bps = 1;
   if (blocks_per_sm > 0 && blocks_per_sm < bps) bps = blocks_per_sm;
   if (bps_out) *bps_out = bps;
@@ -174,11 +179,13 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "graphs") return c->use_graphs;
   if (k == "graph_failed") return c->graph_error.empty() ? 0 : 1;
   if (k == "sm_count") return c->sm_count;
-  if (k == "grid") return c->grid_for(c->block);
-  if (k == "regs") {
+  if (k == "grid") return c->grid_for(c->block, nullptr, true);
+  if (k == "grid_general") return c->grid_for(c->block, nullptr, false);
+  if (k == "regs" || k == "regs_general") {
     int bps = 0, regs = 0;
-    if (c->math == MCFL_MATH_FAST) mcfl_attr_transport_fast(c->block, &bps, &regs);
-    else mcfl_attr_transport_exact(c->block, &bps, &regs);
+    const bool u = k == "regs";
+    if (c->math == MCFL_MATH_FAST) (u ? mcfl_attr_transport_fast_uniform : mcfl_attr_transport_fast)(c->block, &bps, &regs);
+    else (u ? mcfl_attr_transport_exact_uniform : mcfl_attr_transport_exact)(c->block, &bps, &regs);
     return regs;
   }
   return -1;

@@ -88,6 +88,15 @@ typedef struct MCFL_ALIGN(16) McflSaved {
   uint32_t pad;
 } McflSaved;
 
+/* Medium of a launch whose jobs all share it (kernel parameters). */
+typedef struct McflMedium {
+  const uint8_t *labels;
+  const float *prop;
+  unsigned long long *fhd; /* NULL when no job tallies the photon hitting density */
+  float hx, hy, esp, gx, gy, gz;
+  uint32_t nx, ny, total, last_label;
+} McflMedium;
+
 typedef struct McflLaunch {
   const McflJob *jobs;   /* job slots */
   const uint32_t *order; /* slots sorted by ticket_begin, or NULL: slots 0..n_jobs-1 in order */
@@ -99,7 +108,8 @@ typedef struct McflLaunch {
   const uint32_t *mult; /* 32768 MWC multipliers */
   McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
-  uint32_t pad;
+  uint32_t uniform_medium; /* 1: every job uses med (and fhd_on agrees with med.fhd) */
+  McflMedium med;
 } McflLaunch;
 
 #endif

@@ -64,6 +64,8 @@ extern "C" cudaError_t mcfl_launch_transport_exact(const McflLaunch *L, int grid
 extern "C" cudaError_t mcfl_launch_transport_fast(const McflLaunch *L, int grid, int block, cudaStream_t s);
 extern "C" cudaError_t mcfl_attr_transport_exact(int block, int *blocks_per_sm, int *regs);
 extern "C" cudaError_t mcfl_attr_transport_fast(int block, int *blocks_per_sm, int *regs);
+extern "C" cudaError_t mcfl_attr_transport_exact_uniform(int block, int *blocks_per_sm, int *regs);
+extern "C" cudaError_t mcfl_attr_transport_fast_uniform(int block, int *blocks_per_sm, int *regs);
 
 /* engine.cpp: one emission run from one voxel with the medium's excitation
  * table (DoOneSimulationFl), raw 64-bit images */
@@ -118,7 +120,7 @@ struct mcfl_ctx {
   unsigned long long launches = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
-  int grid_for(int block_size, int *bps_out = nullptr);
+  int grid_for(int block_size, int *bps_out = nullptr, bool uniform = false);
   cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
 };
 

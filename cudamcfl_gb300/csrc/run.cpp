@@ -191,6 +191,26 @@ McflLaunch base_launch(mcfl_ctx *c) {
   return L;
 }
 
+/* Every job of the launch uses medium m with one photon-hitting-density
+ * tally (or none): the medium travels in the kernel parameters. */
+void set_uniform(McflLaunch &L, const mcfl_medium *m, bool emission, unsigned long long *fhd) {
+  L.uniform_medium = 1;
+  McflMedium &u = L.med;
+  u.labels = m->labels.as<uint8_t>();
+  u.prop = emission ? m->prop_emi.as<float>() : m->prop_exc.as<float>();
+  u.fhd = fhd;
+  u.hx = m->hx;
+  u.hy = m->hy;
+  u.esp = m->esp;
+  u.gx = m->gx;
+  u.gy = m->gy;
+  u.gz = m->gz;
+  u.nx = (uint32_t)m->nx;
+  u.ny = (uint32_t)m->ny;
+  u.total = m->total;
+  u.last_label = (uint32_t)m->n_bulks + 1u;
+}
+
 } // namespace
 
 /* ------------------------------------------------------------------ run */
@@ -252,7 +272,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
 
   unsigned long long *cnt = c->counters.as<unsigned long long>();
-  const int grid = c->grid_for(c->block);
+  const int grid = c->grid_for(c->block, nullptr, true);
   const int block = c->block;
   const unsigned long long photons = run->photons;
   const unsigned per_voxel = run->photons_per_voxel;
@@ -276,6 +296,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.n_jobs = 1;
     L.ticket_counter = cnt + 0;
     L.ticket_end = photons;
+    set_uniform(L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
     REC(record_event(c->ev[0], st));
     REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
                                   : mcfl_launch_transport_exact(&L, grid, block, st));
@@ -291,6 +312,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       Lf.jobs = c->jobs.as<McflJob>() + 1;
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
+      set_uniform(Lf, m, true, nullptr);
       REC(record_event(c->ev[2], st));
       REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&Lf, grid, block, st)
                                     : mcfl_launch_transport_exact(&Lf, grid, block, st));
@@ -413,7 +435,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     j.photons = runs[i].photons;
     tickets += runs[i].photons;
   }
-  const int grid = c->grid_for(c->block);
+  const int grid = c->grid_for(c->block, nullptr, true);
   const int block = c->block;
   float ms = 0.f;
   if (schedule == MCFL_SCHEDULE_BATCHED) {
@@ -429,6 +451,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = (uint32_t)n;
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
+      set_uniform(L, m, false, nullptr);
       if ((e = record_event(c->ev[0], st))) return e;
       if ((e = c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
                                          : mcfl_launch_transport_exact(&L, grid, block, st)))
@@ -458,6 +481,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = 1;
       L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
       L.ticket_end = runs[i].photons;
+      set_uniform(L, m, false, nullptr);
       MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
     }
@@ -569,7 +593,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   }
   MCFL_CUDA_TRY(cudaMemcpyAsync(c->jobs.p, c->h_jobs, NL * sizeof(McflJob), cudaMemcpyHostToDevice, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(c->bcnt.p, 0, NL * 8 + 8, s));
-  const int grid = c->grid_for(c->block);
+  const int grid = c->grid_for(c->block, nullptr, true);
   MCFL_CUDA_TRY(cudaEventRecord(c->ev[2], s));
   for (size_t i = 0; i < NL; ++i) {
     McflLaunch L = base_launch(c);
@@ -577,6 +601,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     L.n_jobs = 1;
     L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
     L.ticket_end = run->photons_per_voxel;
+    set_uniform(L, m, true, nullptr);
     MCFL_CUDA_TRY(c->launch_transport(L, grid, c->block));
     MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulationFl */
   }
@@ -642,7 +667,8 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   L.n_jobs = 1;
   L.ticket_counter = c->counters.as<unsigned long long>();
   L.ticket_end = run->photons;
-  MCFL_CUDA_TRY(c->launch_transport(L, c->grid_for(c->block), c->block));
+  set_uniform(L, m, false, nullptr);
+  MCFL_CUDA_TRY(c->launch_transport(L, c->grid_for(c->block, nullptr, true), c->block));
   std::vector<unsigned long long> r(2 * xy), t(2 * xy);
   MCFL_CUDA_TRY(cudaMemcpyAsync(r.data(), c->R128.p, xy * 16, cudaMemcpyDeviceToHost, s));
   MCFL_CUDA_TRY(cudaMemcpyAsync(t.data(), c->T128.p, xy * 16, cudaMemcpyDeviceToHost, s));

@@ -57,6 +57,7 @@
 #define MCFL_KERNEL_NAME mcfl_transport_exact
 #define MCFL_LAUNCHER mcfl_launch_transport_exact
 #define MCFL_ATTR_FN mcfl_attr_transport_exact
+#define MCFL_ATTR_FN_U mcfl_attr_transport_exact_uniform
 #else
 #define MCFL_LOGF(x) __logf(x)
 #define MCFL_SINCOSF(x, s, c) __sincosf((x), (s), (c))
@@ -65,6 +66,7 @@
 #define MCFL_KERNEL_NAME mcfl_transport_fast
 #define MCFL_LAUNCHER mcfl_launch_transport_fast
 #define MCFL_ATTR_FN mcfl_attr_transport_fast
+#define MCFL_ATTR_FN_U mcfl_attr_transport_fast_uniform
 #endif
 
 namespace {
@@ -273,7 +275,7 @@ __device__ __forceinline__ void reflect(Photon &p, uint32_t newlb, Rng &r, const
 /* Scattering-free voxels: march in half-voxel steps to the next label, then
  * back-project onto the sphere of radius 0.707 voxel around the centre of the
  * voxel reached.  The march is bounded by max_s. */
-__device__ __noinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, float max_s) {
+__device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, float max_s) {
   float search_step = 1 / (2 * m.gx);
   float total_move = 0;
   int index = 1;
@@ -357,28 +359,32 @@ __device__ __forceinline__ void add128(unsigned long long *acc, uint32_t w, uint
 
 /* Exit through a face: image tally when the exit point is inside the
  * detector.  top: R (z = 0), else T (z = esp). */
-__device__ __noinline__ void tally_exit(const McflJob *J, const Photon &p, bool top, uint32_t src_idx) {
+__device__ __noinline__ void tally_exit(const McflJob *J, float px, float py, uint32_t weight, bool top,
+                                        uint32_t src_idx) {
   const float x0 = __ldg(&J->det_x0), y0 = __ldg(&J->det_y0);
   const float size_x = __ldg(&J->size_x), size_y = __ldg(&J->size_y);
-  if (!(fabsf(p.x - x0) < size_x && fabsf(p.y - y0) < size_y)) return;
-  uint32_t idx = __float2uint_rz((p.y - y0 + size_y) / __ldg(&J->det_dy)) * __ldg(&J->det_nx) +
-                 __float2uint_rz((p.x - x0 + size_x) / __ldg(&J->det_dx));
+  if (!(fabsf(px - x0) < size_x && fabsf(py - y0) < size_y)) return;
+  uint32_t idx = __float2uint_rz((py - y0 + size_y) / __ldg(&J->det_dy)) * __ldg(&J->det_nx) +
+                 __float2uint_rz((px - x0 + size_x) / __ldg(&J->det_dx));
   const uint32_t xy = __ldg(&J->xy_size);
   if (idx >= xy) idx = xy - 1u;
   if (__ldg(&J->src_kind) == MCFL_SRC_VOXELS) {
     unsigned long long *img =
         (unsigned long long *)__ldg((const unsigned long long *)(top ? &J->R128 : &J->T128));
-    add128(&img[2 * (size_t)idx], p.weight, __ldg((const unsigned long long *)&J->src_q[src_idx]));
+    add128(&img[2 * (size_t)idx], weight, __ldg((const unsigned long long *)&J->src_q[src_idx]));
   } else {
     unsigned long long *img = (unsigned long long *)__ldg((const unsigned long long *)(top ? &J->R : &J->T));
-    atomicAdd(&img[idx], (unsigned long long)p.weight);
+    atomicAdd(&img[idx], (unsigned long long)weight);
   }
 }
 
 } // namespace
 
-/* One warp-synchronous persistent loop per thread; see the file comment. */
-extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
+/* One warp-synchronous persistent loop per thread; see the file comment.
+ * kUniform: the medium comes from the launch parameters (constant bank)
+ * instead of per-lane registers loaded from the job. */
+template <bool kUniform>
+__global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
   extern __shared__ unsigned long long s_ev[]; /* kEv x blockDim.x */
   const unsigned lane = threadIdx.x & 31u;
   const unsigned tib = threadIdx.x;
@@ -390,9 +396,24 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
   Photon p;
   Rng r;
   Med m = {};
+  if (kUniform) {
+    m.labels = L.med.labels;
+    m.prop = (const float4 *)L.med.prop;
+    m.fhd = L.med.fhd;
+    m.hx = L.med.hx;
+    m.hy = L.med.hy;
+    m.esp = L.med.esp;
+    m.gx = L.med.gx;
+    m.gy = L.med.gy;
+    m.gz = L.med.gz;
+    m.nx = L.med.nx;
+    m.ny = L.med.ny;
+    m.total = L.med.total;
+    m.last = L.med.last_label;
+  }
   float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, done = 0;
-  uint64_t k = 0, steps = 0, absorbed = 0;
+  uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, done = 0, steps = 0;
+  uint64_t k = 0, absorbed = 0;
   uint32_t f_idx = 0xffffffffu;
   unsigned long long f_acc = 0ull;
   const McflJob *J = nullptr;
@@ -411,9 +432,11 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
     done = 0;
     steps = 0;
     absorbed = 0;
-    if (m.fhd && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
-    f_idx = 0xffffffffu;
-    f_acc = 0ull;
+    if (!kUniform) {
+      if (m.fhd && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
+      f_idx = 0xffffffffu;
+      f_acc = 0ull;
+    }
   };
   auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * blockDim.x + tib] += v; };
 
@@ -422,7 +445,7 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
     if (sv.alive) {
       job = sv.job;
       J = &L.jobs[job];
-      load_med(J, m);
+      if (!kUniform) load_med(J, m);
       p = Photon{sv.x, sv.y, sv.z, sv.dx, sv.dy, sv.dz, sv.weight, sv.label};
       r.x = sv.rng_x;
       r.a = sv.rng_a;
@@ -452,7 +475,7 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
               flush_stats();
               job = j;
               J = &L.jobs[j];
-              load_med(J, m);
+              if (!kUniform) load_med(J, m);
             }
             k = t - __ldg((const unsigned long long *)&J->ticket_begin);
             launch_photon(J, m, k, L.mult, p, r, src_idx);
@@ -473,6 +496,7 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
     ++pst;
     float s;
     uint32_t new_bulk;
+    uint32_t vi = 0xffffffffu; /* voxel of the end point, when looked up */
     if (pr.x != FLT_MAX) {
       s = -MCFL_LOGF(r.oc()) * pr.x;
       new_bulk = p.label;
@@ -488,18 +512,22 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
       p.y += p.dy * s;
       p.z += p.dz * s;
       if (new_bulk != 0u && new_bulk != m.last) {
-        if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp)
-          new_bulk = (uint32_t)m.labels[voxel_index(m, p.x, p.y, p.z)];
-        else
+        if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp) {
+          vi = voxel_index(m, p.x, p.y, p.z);
+          new_bulk = (uint32_t)m.labels[vi];
+        } else {
           new_bulk = 1u;
+        }
       }
     } else {
       s = 100.0f;
       new_bulk = move_to_first_boundary(p, m, s);
     }
     if (new_bulk != p.label) reflect(p, new_bulk, r, m, pr);
-    if (m.fhd && fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp) {
-      const uint32_t fi = voxel_index(m, p.x, p.y, p.z);
+    /* the hitting density is tallied at the end point, where the label was
+     * looked up unless the pass was clipped to a face */
+    if (m.fhd && (vi != 0xffffffffu || (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp))) {
+      const uint32_t fi = vi != 0xffffffffu ? vi : voxel_index(m, p.x, p.y, p.z);
       if (fi != f_idx) {
         if (f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
         f_idx = fi;
@@ -509,7 +537,7 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
     }
     if (p.label == 0u || p.label == m.last) {
       const bool top = p.label == 0u;
-      tally_exit(J, p, top, src_idx);
+      tally_exit(J, p.x, p.y, p.weight, top, src_idx);
       ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
       p.weight = 0u;
       s = 0.0f;
@@ -562,19 +590,34 @@ extern "C" __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L)
     L.saved[gtid] = sv;
   }
   flush_stats();
+  if (kUniform && m.fhd && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 }
 
 extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, cudaStream_t stream) {
   const size_t smem = (size_t)kEv * block * sizeof(unsigned long long);
-  MCFL_KERNEL_NAME<<<grid, block, smem, stream>>>(*L);
+  if (L->uniform_medium)
+    MCFL_KERNEL_NAME<true><<<grid, block, smem, stream>>>(*L);
+  else
+    MCFL_KERNEL_NAME<false><<<grid, block, smem, stream>>>(*L);
   return cudaGetLastError();
 }
 
+/* Occupancy of the general (per-lane medium) instantiation, the larger of
+ * the two, so one grid size serves both. */
 extern "C" cudaError_t MCFL_ATTR_FN(int block, int *blocks_per_sm, int *regs) {
   cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME);
+  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME<false>);
   if (e != cudaSuccess) return e;
   if (regs) *regs = a.numRegs;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME, block,
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME<false>, block,
+                                                       (size_t)kEv * block * sizeof(unsigned long long));
+}
+
+extern "C" cudaError_t MCFL_ATTR_FN_U(int block, int *blocks_per_sm, int *regs) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME<true>);
+  if (e != cudaSuccess) return e;
+  if (regs) *regs = a.numRegs;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME<true>, block,
                                                        (size_t)kEv * block * sizeof(unsigned long long));
 }

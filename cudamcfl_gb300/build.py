@@ -33,6 +33,7 @@ CUDA_UNITS = {
     "transport_exact.cu": EXACT,
     "transport_fast.cu": FAST,
     "engine_kernels.cu": EXACT,
+    "noalloc.cu": EXACT,
 }
 HOST_UNITS = ["engine.cpp", "run.cpp", "mci.cpp", "safeprimes.cpp", "server.cpp"]
 HEADERS = ["engine_types.h", "portable_math.h", "mcfl_internal.h", "transport.cuh"]

@@ -1,0 +1,167 @@
+/*
+ * Allocation-free batched excitation run (mcfl_batch_run_noalloc).
+ *
+ * Some callers cannot allocate device memory: code that runs inside another
+ * framework's memory pool or arena, that must not trigger the implicit
+ * synchronisation of cudaMalloc/cudaFree, or that is only handed device
+ * buffers it may read and write.  This entry point serves them: the caller
+ * passes the medium and the output images on the device, and the scratch the
+ * persistent kernel needs (its ticket counter, its job table and the MWC
+ * multiplier table) lives in one file-scope __device__ array of fixed size,
+ * which every GPU that loads the library holds until the process exits.
+ *
+ * Limits and rules:
+ *   - at most MCFL_NOALLOC_MAX_JOBS simulations per call (the job table's
+ *     size); more is rejected with MCFL_E_RANGE;
+ *   - the first call on a device, with that device current, resolves the
+ *     array's device address (cudaGetSymbolAddress) and writes the multiplier
+ *     table into it; make that first call before any stream capture;
+ *   - every call shares the array and leaves its contents behind; the ticket
+ *     counter is cleared at the start of each call, so calls that run one after
+ *     another are independent, but calls that overlap on the GPU (other
+ *     streams, other host threads) race on the array;
+ *   - the output images and stats are cleared by the call, then accumulated
+ *     by the kernel; the call is asynchronous on the given stream.
+ * Nothing here calls cudaMalloc, cudaFree or any allocating library routine.
+ */
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstring>
+#include <mutex>
+
+#include "mcfl_internal.h"
+#include "portable_math.h"
+
+using namespace mcfl;
+
+namespace {
+
+struct NoallocScratch {
+  unsigned long long counter;
+  unsigned long long pad[31]; /* jobs start 256 bytes in */
+  McflJob jobs[MCFL_NOALLOC_MAX_JOBS];
+  uint32_t mult[32768];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocScratch)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+NoallocScratch *g_scratch[kMaxDevices] = {nullptr};
+
+/* Device address of the scratch array on the current device, set up on the
+ * first call. */
+int scratch_for_current_device(NoallocScratch **out) {
+  int dev = 0;
+  MCFL_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return mcfl::fail(MCFL_E_RANGE, "noalloc: device index beyond 63");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!g_scratch[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return mcfl::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+    const std::vector<uint32_t> &tab = mcfl::mwc_table();
+    if (tab.size() != mcfl::kMwcTableEntries + 1) return mcfl::fail(MCFL_E_STATE, "multiplier table incomplete");
+    e = cudaMemcpy((char *)p + offsetof(NoallocScratch, mult), tab.data() + 1, mcfl::kMwcTableEntries * 4,
+                   cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return mcfl::cuda_fail(e, "noalloc multiplier upload");
+    g_scratch[dev] = (NoallocScratch *)p;
+  }
+  *out = g_scratch[dev];
+  return MCFL_OK;
+}
+
+} // namespace
+
+extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, const float *d_prop, int nx, int ny,
+                                      int nz, float half_x, float half_y, float thickness, const float *vox_per_cm,
+                                      int n_bulks, const mcfl_run_desc *runs, int n, unsigned long long *d_R,
+                                      unsigned long long *d_T, unsigned long long *d_stats, void *stream) {
+  using mcfl::fail;
+  if (n < 1) return fail(MCFL_E_ARG, "noalloc: at least one simulation");
+  if (n > MCFL_NOALLOC_MAX_JOBS) return fail(MCFL_E_RANGE, "noalloc: more than MCFL_NOALLOC_MAX_JOBS simulations");
+  if (!d_labels || !d_prop || !runs || !d_R || !d_T || !d_stats || !vox_per_cm)
+    return fail(MCFL_E_ARG, "noalloc: null pointer");
+  if (math != MCFL_MATH_EXACT && math != MCFL_MATH_FAST) return fail(MCFL_E_ARG, "noalloc: unknown math");
+  if (nx <= 0 || ny <= 0 || nz <= 0 || (unsigned long long)nx * ny * nz >= 0xFFFFFFFFull)
+    return fail(MCFL_E_ARG, "noalloc: bad grid");
+  if (n_bulks < 1 || n_bulks > MCFL_MAX_BULKS) return fail(MCFL_E_RANGE, "noalloc: n_bulks out of range");
+  const mcfl_detector det = runs[0].det;
+  if (det.nx <= 0 || det.ny <= 0 || !(det.dx > 0) || !(det.dy > 0)) return fail(MCFL_E_ARG, "noalloc: bad detector");
+  for (int i = 0; i < n; ++i) {
+    const mcfl_run_desc &r = runs[i];
+    if (r.photons == 0 || r.photons_per_voxel || r.fluence) return fail(MCFL_E_ARG, "noalloc: excitation images only");
+    if (r.start_weight == 0) return fail(MCFL_E_ARG, "noalloc: start_weight must be given");
+    if (r.det.nx != det.nx || r.det.ny != det.ny) return fail(MCFL_E_ARG, "noalloc: detectors must share a size");
+    if (r.source.kind != MCFL_SOURCE_GAUSS_BEAM && r.source.kind != MCFL_SOURCE_WIDEFIELD)
+      return fail(MCFL_E_ARG, "noalloc: unknown source kind");
+  }
+  NoallocScratch *sc = nullptr;
+  int rc = scratch_for_current_device(&sc);
+  if (rc != MCFL_OK) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaGetLastError();
+  const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
+  McflJob jobs[MCFL_NOALLOC_MAX_JOBS];
+  std::memset(jobs, 0, sizeof(McflJob) * (size_t)n);
+  unsigned long long tickets = 0;
+  for (int i = 0; i < n; ++i) {
+    const mcfl_run_desc &r = runs[i];
+    McflJob &j = jobs[i];
+    j.labels = d_labels;
+    j.prop = d_prop;
+    j.hx = half_x; j.hy = half_y; j.esp = thickness;
+    j.gx = vox_per_cm[0]; j.gy = vox_per_cm[1]; j.gz = vox_per_cm[2];
+    j.nx = (uint32_t)nx; j.ny = (uint32_t)ny; j.nz = (uint32_t)nz;
+    j.total = (uint32_t)nx * (uint32_t)ny * (uint32_t)nz;
+    j.last_label = (uint32_t)n_bulks + 1u;
+    j.src_kind = r.source.kind == MCFL_SOURCE_WIDEFIELD ? MCFL_SRC_WIDEFIELD : MCFL_SRC_GAUSS_BEAM;
+    j.sx = r.source.x; j.sy = r.source.y; j.sz = r.source.z;
+    j.src_w = r.source.width; j.src_h = r.source.height;
+    j.start_weight = r.start_weight;
+    j.det_x0 = r.det.x0; j.det_y0 = r.det.y0; j.det_dx = r.det.dx; j.det_dy = r.det.dy;
+    j.size_x = (r.det.dx * (float)r.det.nx) / 2.0f;
+    j.size_y = (r.det.dy * (float)r.det.ny) / 2.0f;
+    j.det_nx = (uint32_t)r.det.nx;
+    j.xy_size = (uint32_t)xy;
+    j.R = d_R + (size_t)i * xy;
+    j.T = d_T + (size_t)i * xy;
+    j.stats = d_stats + (size_t)i * MCFL_ST_COUNT;
+    j.key = mcfl_stream_key(r.seed_exc, 0);
+    j.ticket_begin = tickets;
+    j.photons = r.photons;
+    tickets += r.photons;
+  }
+  MCFL_CUDA_TRY(cudaMemsetAsync(&sc->counter, 0, sizeof(unsigned long long), s));
+  MCFL_CUDA_TRY(cudaMemcpyAsync(sc->jobs, jobs, sizeof(McflJob) * (size_t)n, cudaMemcpyHostToDevice, s));
+  MCFL_CUDA_TRY(cudaMemsetAsync(d_R, 0, (size_t)n * xy * 8, s));
+  MCFL_CUDA_TRY(cudaMemsetAsync(d_T, 0, (size_t)n * xy * 8, s));
+  MCFL_CUDA_TRY(cudaMemsetAsync(d_stats, 0, (size_t)n * MCFL_ST_COUNT * 8, s));
+  McflLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.jobs = sc->jobs;
+  L.n_jobs = (uint32_t)n;
+  L.ticket_counter = &sc->counter;
+  L.ticket_end = tickets;
+  L.mult = sc->mult;
+  L.step_cap = 1u << 24;
+  L.uniform_medium = 1;
+  L.med.labels = d_labels;
+  L.med.prop = d_prop;
+  L.med.fhd = nullptr;
+  L.med.hx = half_x; L.med.hy = half_y; L.med.esp = thickness;
+  L.med.gx = vox_per_cm[0]; L.med.gy = vox_per_cm[1]; L.med.gz = vox_per_cm[2];
+  L.med.nx = (uint32_t)nx; L.med.ny = (uint32_t)ny; L.med.total = jobs[0].total;
+  L.med.last_label = (uint32_t)n_bulks + 1u;
+  const int block = 256;
+  int dev = 0, sms = 0, bps = 0, regs = 0;
+  MCFL_CUDA_TRY(cudaGetDevice(&dev));
+  MCFL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  MCFL_CUDA_TRY(math == MCFL_MATH_FAST ? mcfl_attr_transport_fast_uniform(block, &bps, &regs)
+                                       : mcfl_attr_transport_exact_uniform(block, &bps, &regs));
+  if (bps < 1) bps = 1;
+  MCFL_CUDA_TRY(math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, bps * sms, block, s)
+                                       : mcfl_launch_transport_exact(&L, bps * sms, block, s));
+  return MCFL_OK;
+}

@@ -348,6 +348,33 @@ int mcfl_server_metrics(mcfl_server *server, mcfl_server_metrics_t *metrics);
 /* Finishes the admitted and queued requests, then stops the thread. */
 void mcfl_server_destroy(mcfl_server *server);
 
+/* ---------------------------------------------------------------------- */
+/* Allocation-free batch                                                    */
+/* ---------------------------------------------------------------------- */
+
+#define MCFL_NOALLOC_MAX_JOBS 64
+
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory (code running inside another framework's memory pool or arena, code
+ * that must avoid the synchronisation of cudaMalloc/cudaFree, or code that is
+ * only handed device buffers): runs n <= MCFL_NOALLOC_MAX_JOBS excitation
+ * simulations on one medium in one persistent launch, like mcfl_batch_run,
+ * without allocating anything.  The caller passes the medium on the device
+ * (labels, nx*ny*nz bytes; d_prop, 4 floats per label: 1/(mua+mus), mua, g, n
+ * for labels 0..n_bulks+1) and the outputs on the device (d_R, d_T: n images
+ * of det.nx + det.nx*det.ny 64-bit sums; d_stats: n x MCFL_NSTATS), which
+ * the call clears.  Every run must give start_weight.  The kernel's scratch
+ * (ticket counter, job table, multiplier table, about 145 KB) is one static
+ * device array that every GPU loading the library holds until exit; the
+ * first call on a device sets it up (make it before any stream capture);
+ * calls share it, so calls that overlap on the GPU race.  Asynchronous on
+ * stream (a cudaStream_t, NULL for the default stream).  More than
+ * MCFL_NOALLOC_MAX_JOBS runs: MCFL_E_RANGE. */
+int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, const float *d_prop, int nx, int ny, int nz,
+                           float half_x, float half_y, float thickness, const float *vox_per_cm, int n_bulks,
+                           const mcfl_run_desc *runs, int n, unsigned long long *d_R, unsigned long long *d_T,
+                           unsigned long long *d_stats, void *stream);
+
 /* Kernel launches issued by this context so far. */
 unsigned long long mcfl_launch_count(const mcfl_ctx *ctx);
 

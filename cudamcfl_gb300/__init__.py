@@ -105,7 +105,7 @@ class Detector(ctypes.Structure):
 class RunDesc(ctypes.Structure):
     _fields_ = [("photons", ctypes.c_ulonglong), ("photons_per_voxel", ctypes.c_uint), ("fluence", ctypes.c_int),
                 ("seed_exc", ctypes.c_ulonglong), ("seed_fl", ctypes.c_ulonglong), ("start_weight", ctypes.c_uint),
-                ("source", Source), ("det", Detector)]
+                ("source", Source), ("det", Detector), ("launch_rng_reuse", ctypes.c_int)]
 
 
 _u64p = ctypes.POINTER(ctypes.c_ulonglong)
@@ -527,7 +527,7 @@ class Server:
 
 def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per_voxel: int = 0, fluence: int = 0,
              seed_exc: int = 1, seed_fl: int = 2, start_weight: int = 0, kind: int = SOURCE_GAUSS_BEAM,
-             width: float = 0.0, height: float = 0.0) -> RunDesc:
+             width: float = 0.0, height: float = 0.0, launch_rng_reuse: int = 0) -> RunDesc:
     r = RunDesc()
     r.photons = photons
     r.photons_per_voxel = photons_per_voxel
@@ -537,6 +537,7 @@ def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per
     r.start_weight = start_weight
     r.source = Source(kind, *[float(v) for v in source], width, height)
     r.det = det
+    r.launch_rng_reuse = launch_rng_reuse
     return r
 
 

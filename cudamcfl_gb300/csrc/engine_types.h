@@ -60,6 +60,8 @@ typedef struct MCFL_ALIGN(16) McflJob {
   const uint64_t *src_q;   /* MCFL_SRC_VOXELS: fixed-point exit weights per voxel (2^-40 units) */
   uint32_t per_voxel;      /* MCFL_SRC_VOXELS: photons per voxel */
   uint32_t fhd_on;
+  uint32_t launch_rng_reuse; /* 1: photons 0..32767 of a run (of each voxel) restart their stream after launch */
+  uint32_t pad0;
   /* detector (R at z = 0, T at z = esp) */
   float det_x0, det_y0, det_dx, det_dy, size_x, size_y;
   uint32_t det_nx, xy_size;

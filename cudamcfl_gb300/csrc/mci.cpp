@@ -520,6 +520,7 @@ extern "C" int mcfl_run_desc_from_simulation(const mcfl_simulation *sim, unsigne
   run->det.dy = sim->det.dy;
   run->det.nx = sim->det.nx;
   run->det.ny = sim->det.ny;
+  run->launch_rng_reuse = 1; /* the reference's statistics, quirk included */
   return MCFL_OK;
 }
 

@@ -256,6 +256,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   je.stats = c->stats.as<unsigned long long>();
   je.key = mcfl_stream_key(run->seed_exc, 0);
   je.photons = run->photons;
+  je.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
   if (emission) {
     McflJob &jf = jobs[1];
     fill_medium(jf, m, true);
@@ -269,6 +270,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     jf.stats = c->stats.as<unsigned long long>() + MCFL_ST_COUNT;
     jf.key = mcfl_stream_key(run->seed_fl, 1);
     jf.photons = 0; /* written by the list build */
+    jf.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
   }
 
   unsigned long long *cnt = c->counters.as<unsigned long long>();
@@ -431,6 +433,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     j.T = c->bT.as<unsigned long long>() + i * xy;
     j.stats = c->bstats.as<unsigned long long>() + i * (size_t)MCFL_ST_COUNT;
     j.key = mcfl_stream_key(runs[i].seed_exc, 0);
+    j.launch_rng_reuse = runs[i].launch_rng_reuse ? 1u : 0u;
     j.ticket_begin = schedule == MCFL_SCHEDULE_BATCHED ? tickets : 0;
     j.photons = runs[i].photons;
     tickets += runs[i].photons;
@@ -584,6 +587,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   t.stats = c->stats.as<unsigned long long>() + MCFL_ST_COUNT;
   t.key = mcfl_stream_key(run->seed_fl, 1);
   t.photons = run->photons_per_voxel;
+  t.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
   for (size_t i = 0; i < NL; ++i) {
     McflJob &j = c->h_jobs[i];
     j = t;
@@ -661,6 +665,7 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   j.stats = c->stats.as<unsigned long long>();
   j.key = mcfl_stream_key(run->seed_fl, 1);
   j.photons = run->photons;
+  j.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
   MCFL_CUDA_TRY(cudaMemcpyAsync(c->jobs.p, &j, sizeof(j), cudaMemcpyHostToDevice, s));
   McflLaunch L = base_launch(c);
   L.jobs = c->jobs.as<McflJob>();

@@ -153,6 +153,7 @@ int mcfl_server::upload(Request &r) {
   j.fhd = r.run.fluence ? r.fhd.as<unsigned long long>() : nullptr;
   j.stats = r.stats.as<unsigned long long>();
   j.key = mcfl_stream_key(r.run.seed_exc, 0);
+  j.launch_rng_reuse = r.run.launch_rng_reuse ? 1u : 0u;
   j.rng_offset = 0;
   j.ticket_begin = r.ticket_begin;
   j.photons = r.run.photons;

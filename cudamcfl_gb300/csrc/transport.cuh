@@ -156,10 +156,13 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
                                               Photon &p, Rng &r, uint32_t &src_idx) {
   mcfl_photon_stream(__ldg((const unsigned long long *)&J->key),
                      __ldg((const unsigned long long *)&J->rng_offset) + k, mult, &r.x, &r.a);
+  const uint64_t x_at_launch = r.x;
   const uint32_t kind = __ldg(&J->src_kind);
+  uint64_t k_in_run = k;
   if (kind == MCFL_SRC_VOXELS) {
     const uint32_t per = __ldg(&J->per_voxel);
     src_idx = (uint32_t)(k / per);
+    k_in_run = k - (uint64_t)src_idx * per;
     const uint32_t v = __ldg(&J->src_vox[src_idx]);
     const uint32_t ix = v % m.nx, iy = (v / m.nx) % m.ny, iz = v / (m.nx * m.ny);
     const float xi = ((float)ix / m.gx) - m.hx;
@@ -201,6 +204,12 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     p.weight = __ldg(&J->start_weight);
   }
   p.label = start_label(m, p);
+  /* The reference's first photon on each of its 32768 threads draws its first
+   * passes from the stream state its launch started from, because
+   * LaunchPhoton_Global does not store the advanced state
+   * (CUDAMCFLtransport.cu:574-581).  Reproduced on request for photons
+   * 0..32767 of a run (of each emitting voxel's run). */
+  if (__ldg(&J->launch_rng_reuse) && k_in_run < 32768u) r.x = x_at_launch;
 }
 
 __device__ __forceinline__ void spin(Photon &p, float g, Rng &r) {

@@ -227,6 +227,15 @@ typedef struct mcfl_run_desc {
   unsigned int start_weight;      /* 0: (2^32-1)(1 - R_specular) from n of labels 0 and 1 */
   mcfl_source source;
   mcfl_detector det;
+  /* 1: reproduce the reference's first-photon random-number reuse: photons
+   * 0..32767 of the excitation run and of each emitting voxel's run draw their
+   * first passes from the numbers their launch drew, as each reference thread's
+   * first photon does (LaunchPhoton_Global keeps no RNG state,
+   * CUDAMCFLtransport.cu:574-581).  This correlates a first photon's launch
+   * with its first steps (a small bias, visible mostly in the emission images
+   * where 32768 of every voxel's photons are first photons).  0: independent
+   * numbers (default of the engine API; the .mci path sets 1). */
+  int launch_rng_reuse;
 } mcfl_run_desc;
 
 #define MCFL_NSTATS 9

@@ -71,6 +71,8 @@ typedef struct oracle_sim {
   float vox_per_cm[3];
   const float *fluor_map; /* optional emission-strength factor per voxel */
   long max_fl_voxels;     /* refstream only: stop after this many emitting voxels (0: all) */
+  int launch_rng_reuse;   /* photon only: photons 0..32767 of a run (of each voxel) restart their stream
+                             after launch, as each reference thread's first photon does */
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);
@@ -94,7 +96,7 @@ int oracle_run_refstream(const oracle_sim *sim, const char *safeprimes_path, uns
  * one job over all emitting voxels with fixed-point voxel weights.  With
  * math_libm=0 it is bit-identical to the CUDA engine's exact-math kernel. */
 int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipliers, unsigned int n_multipliers,
-                      unsigned long long seed_exc, unsigned long long seed_fl, int math_libm,
+                      unsigned long long seed_exc, unsigned long long seed_fl, int math_libm, int nthreads,
                       oracle_result *res);
 
 /* Writers of the emission images in the reference's text format

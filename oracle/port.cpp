@@ -44,6 +44,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <atomic>
 #include <thread>
 #include <vector>
@@ -111,6 +112,7 @@ struct Phase {
   float xi, yi, zi, dir;
   uint32_t start_weight;
   int guard; /* reproduce the reference's non-atomic overflow guards */
+  int launch_rng_reuse;
 };
 
 inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
@@ -343,9 +345,9 @@ struct Sink {
 inline void add128(unsigned long long *acc, uint32_t w, uint64_t q) {
   unsigned __int128 prod = (unsigned __int128)w * q;
   uint64_t lo = (uint64_t)prod, hi = (uint64_t)(prod >> 64);
-  uint64_t old = acc[0];
-  acc[0] = old + lo;
-  acc[1] += hi + (acc[0] < old ? 1u : 0u);
+  uint64_t old = __atomic_fetch_add(&acc[0], lo, __ATOMIC_RELAXED);
+  uint64_t carry = (old + lo < old) ? 1u : 0u;
+  if (hi + carry) __atomic_fetch_add(&acc[1], hi + carry, __ATOMIC_RELAXED);
 }
 
 /* One pass of the MCd3D loop body up to the survival test.  Returns 1 while
@@ -457,6 +459,7 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
   ph.xi = sim->xi; ph.yi = sim->yi; ph.zi = sim->zi;
   ph.dir = emission ? 0.0f : sim->dir;
   ph.start_weight = sim->start_weight;
+  ph.launch_rng_reuse = sim->launch_rng_reuse;
 }
 
 /* init_RNG (CUDAMCFLrng.cu:31-90) restated.  Returns 0 on success. */
@@ -636,6 +639,8 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
   for (uint64_t k = k0; k < k1; ++k) {
     Rng r;
     mcfl_photon_stream(key, k, table, &r.x, &r.a);
+    const uint64_t x_at_launch = r.x;
+    const uint64_t k_in_run = vox ? k % nv : k;
     Photon p;
     if (vox) {
       uint32_t v = vox[k / nv];
@@ -648,14 +653,40 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
     } else {
       launch_photon<M>(p, r, ph, ph.xi, ph.yi, ph.zi);
     }
+    if (ph.launch_rng_reuse && k_in_run < kThreads) r.x = x_at_launch;
     while (step<M>(p, r, ph, sk)) {
     }
   }
 }
 
+/* Photon ranges dealt to host threads; integer tallies make the result
+ * independent of the thread count. */
+template <class M>
+void run_photon_threads(const Phase &ph, uint64_t key, const uint32_t *table, uint64_t n, Sink &sk,
+                        const uint32_t *vox, const uint64_t *voxq, unsigned nv, int nthreads) {
+  if (nthreads <= 1 || n < 4096) {
+    run_photon_range<M>(ph, key, table, 0, n, sk, vox, voxq, nv);
+    return;
+  }
+  std::vector<Sink> local(nthreads, sk);
+  for (auto &l : local) { l.absorbed = l.exit_top = l.exit_bottom = l.r_loss = l.r_gain = l.w0_loss = l.steps = 0; }
+  std::vector<std::thread> pool;
+  const uint64_t chunk = (n + nthreads - 1) / nthreads;
+  for (int w = 0; w < nthreads; ++w)
+    pool.emplace_back([&, w] {
+      const uint64_t k0 = std::min<uint64_t>(n, (uint64_t)w * chunk), k1 = std::min<uint64_t>(n, k0 + chunk);
+      run_photon_range<M>(ph, key, table, k0, k1, local[w], vox, voxq, nv);
+    });
+  for (auto &t : pool) t.join();
+  for (auto &l : local) {
+    sk.absorbed += l.absorbed; sk.exit_top += l.exit_top; sk.exit_bottom += l.exit_bottom;
+    sk.r_loss += l.r_loss; sk.r_gain += l.r_gain; sk.w0_loss += l.w0_loss; sk.steps += l.steps;
+  }
+}
+
 template <class M>
 int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc, uint64_t seed_fl,
-                oracle_result *res) {
+                oracle_result *res, int nthreads) {
   Phase ph;
   make_phase(sim, ph, 0);
   ph.guard = 0;
@@ -673,7 +704,7 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
   Sink sk;
   sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
   const unsigned long long N = sim->number_of_photons;
-  run_photon_range<M>(ph, mcfl_stream_key(seed_exc, 0), table, 0, N, sk, nullptr, nullptr, 1);
+  run_photon_threads<M>(ph, mcfl_stream_key(seed_exc, 0), table, N, sk, nullptr, nullptr, 1, nthreads);
   res->photons_exc = N;
   res->steps_exc = sk.steps;
   res->balance[0] = sk.absorbed; res->balance[1] = sk.exit_top; res->balance[2] = sk.exit_bottom;
@@ -703,7 +734,7 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
   s2.R128 = res->flR128; s2.T128 = res->flT128;
   const unsigned nv = sim->number_of_photons_per_voxel;
   const uint64_t M_total = (uint64_t)vox.size() * nv;
-  run_photon_range<M>(fl, mcfl_stream_key(seed_fl, 1), table, 0, M_total, s2, vox.data(), q.data(), nv);
+  run_photon_threads<M>(fl, mcfl_stream_key(seed_fl, 1), table, M_total, s2, vox.data(), q.data(), nv, nthreads);
   res->steps_fl = s2.steps;
   res->fl_voxels = (long)vox.size();
   res->photons_fl = M_total;
@@ -735,11 +766,11 @@ extern "C" int oracle_run_refstream(const oracle_sim *sim, const char *safeprime
 
 extern "C" int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipliers, unsigned int n_multipliers,
                                  unsigned long long seed_exc, unsigned long long seed_fl, int math_libm,
-                                 oracle_result *res) {
+                                 int nthreads, oracle_result *res) {
   memset(res, 0, sizeof(*res));
   if (sim->bulk_method != 2 || sim->n_bulks > ORACLE_MAX_BULKS || n_multipliers != 32768) return -1;
-  return math_libm ? photon_impl<LibmMath>(sim, multipliers, seed_exc, seed_fl, res)
-                   : photon_impl<PortableMath>(sim, multipliers, seed_exc, seed_fl, res);
+  return math_libm ? photon_impl<LibmMath>(sim, multipliers, seed_exc, seed_fl, res, nthreads)
+                   : photon_impl<PortableMath>(sim, multipliers, seed_exc, seed_fl, res, nthreads);
 }
 
 /* ---------------------------------------------------------- test helpers */

@@ -87,6 +87,7 @@ class CSim(ctypes.Structure):
         ("vox_per_cm", ctypes.c_float * 3),
         ("fluor_map", ctypes.POINTER(ctypes.c_float)),
         ("max_fl_voxels", ctypes.c_long),
+        ("launch_rng_reuse", ctypes.c_int),
     ]
 
 
@@ -164,7 +165,8 @@ class Oracle:
         L.oracle_run_refstream.argtypes = [ctypes.POINTER(CSim), ctypes.c_char_p, ctypes.c_ulonglong,
                                            ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int, ctypes.POINTER(CResult)]
         L.oracle_run_photon.argtypes = [ctypes.POINTER(CSim), ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint,
-                                        ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_int, ctypes.POINTER(CResult)]
+                                        ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int,
+                                        ctypes.POINTER(CResult)]
         L.oracle_safeprime_multipliers.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]
         L.oracle_write_safeprimes.argtypes = [ctypes.c_char_p, ctypes.c_int]
 
@@ -189,12 +191,14 @@ class Oracle:
         return _to_result(self.lib, r)
 
     def run_photon(self, sim: "CSim", table32768: np.ndarray, seed_exc: int, seed_fl: int,
-                   libm: bool = False) -> Result:
+                   libm: bool = False, nthreads: int = 0) -> Result:
+        """nthreads 0: all host cores; the result does not depend on it."""
+        nthreads = nthreads or (os.cpu_count() or 1)
         t = np.ascontiguousarray(table32768, dtype=np.uint32)
         assert t.size == 32768
         r = CResult()
         rc = self.lib.oracle_run_photon(ctypes.byref(sim), t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)),
-                                        t.size, seed_exc, seed_fl, 1 if libm else 0, ctypes.byref(r))
+                                        t.size, seed_exc, seed_fl, 1 if libm else 0, nthreads, ctypes.byref(r))
         if rc != 0:
             raise RuntimeError(f"oracle_run_photon failed ({rc})")
         return _to_result(self.lib, r)

@@ -152,4 +152,15 @@ def sphere(photons=40000, per_voxel=33000) -> Case:
                 1.0, photons, per_voxel, (0.04, 0.04, 50, 50, 0.0, 0.0))
 
 
+def deep(photons=40000, per_voxel=40000) -> Case:
+    """tiny with the fluorescent block one voxel layer below the beam entry
+    (0.25-0.5 cm deep), away from the voxels whose photon hitting density the
+    reference's first-photon random-number reuse touches."""
+    lab = _labels(0.5, 4)
+    lab[1, 3:5, 3:5] = 2
+    return Case("deep", 0.5, 4, lab,
+                [(1.4, 0.1, 100.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.4, 0.1, 100.0, 1.0, 0.05, 0.02, 0.1, 0.9)],
+                1.0, photons, per_voxel, (0.1, 0.1, 20, 20, 0.0, 0.0))
+
+
 ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere}

@@ -1,0 +1,118 @@
+"""Statistical gates of the CUDA engine (3 sigma of the batch-means standard
+error per pixel; integrated reflectance, transmittance and absorbed fraction
+within 3 sigma and within 0.1 % where the photon budget resolves 0.1 %).
+
+  fast-math kernel vs exact-math kernel: same physics, hardware SFU
+  intrinsics vs the portable series (the exact kernel is bit-identical to the
+  oracle's photon-indexed restatement);
+  CUDA engine vs the reference's own RNG streams and schedule (the oracle's
+  reference-stream restatement, bit-identical to the reference), with the
+  reference's first-photon random-number reuse reproduced.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cudamcfl_gb300 as mc
+from tests import cases, stats
+
+B = 16
+
+
+def _run(ctx, med, case, b, photons=None, per_voxel=None, emission=True, seed0=0, reuse=0):
+    rd = case.run_desc(seed0 + 11 + b, seed0 + 5011 + b, photons=photons)
+    if per_voxel is not None:
+        rd.photons_per_voxel = per_voxel
+    if not emission:
+        rd.photons_per_voxel = 0
+    rd.launch_rng_reuse = reuse
+    return ctx.run(med, rd)
+
+
+def _fractions(results, w0):
+    out = {}
+    for k in ("absorbed", "exit_top", "exit_bottom"):
+        out[k] = [r.stats_exc[k] / (r.stats_exc["done"] * w0) for r in results]
+    return out
+
+
+@pytest.mark.gpu
+def test_fast_math_kernel_agrees_with_exact_kernel(gpu_ctx):
+    case = cases.sphere()
+    fast = mc.Context(math=mc.MATH_FAST)
+    try:
+        me, mf = case.engine_medium(gpu_ctx), case.engine_medium(fast)
+        ex = [_run(gpu_ctx, me, case, b, photons=400_000, per_voxel=300) for b in range(B)]
+        fa = [_run(fast, mf, case, b, photons=400_000, per_voxel=300, seed0=100) for b in range(B)]
+        xy = case.det[2] * case.det[3]
+        for k in ("Rd", "Tt", "fhd"):
+            a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in fa])
+            b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ex])
+            stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+        for k in ("flR", "flT"):
+            stats.gate(np.stack([getattr(r, k)[:xy] for r in fa]), np.stack([getattr(r, k)[:xy] for r in ex]),
+                       frac_max=0.02, min_rel=1e-2)
+        # integrated, 1.6e8 photons per kernel: 0.1 %
+        ex = [_run(gpu_ctx, me, case, b, photons=10_000_000, emission=False, seed0=7) for b in range(B)]
+        fa = [_run(fast, mf, case, b, photons=10_000_000, emission=False, seed0=900) for b in range(B)]
+        w0 = case.start_weight()
+        fx, ff = _fractions(ex, w0), _fractions(fa, w0)
+        for k in fx:
+            stats.scalar_gate(ff[k], fx[k], rel_tol=1e-3)
+    finally:
+        fast.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("math", [mc.MATH_EXACT, mc.MATH_FAST])
+def test_engine_agrees_with_reference_streams(math, oracle, safeprimes_file):
+    """tiny medium, fluorescent voxels at the beam entry; the reference side is
+    the reference-stream restatement on all host cores."""
+    nthreads = os.cpu_count() or 1
+    case = cases.tiny(photons=250_000, per_voxel=33000)
+    sim = case.oracle_sim()
+    ref = [oracle.run_refstream(sim, safeprimes_file, 1000 + b, 2000 + b, libm=True, nthreads=nthreads)
+           for b in range(B)]
+    ctx = mc.Context(math=math)
+    try:
+        med = case.engine_medium(ctx)
+        eng = [_run(ctx, med, case, b, reuse=1, seed0=300) for b in range(B)]
+    finally:
+        pass
+    xy = case.det[2] * case.det[3]
+    for k in ("Rd", "Tt", "fhd"):
+        a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in eng])
+        b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ref])
+        stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+    for k in ("flR", "flT"):
+        stats.gate(np.stack([getattr(r, k)[:xy] for r in eng]), np.stack([getattr(r, k)[:xy] for r in ref]),
+                   frac_max=0.02, min_rel=1e-2)
+    w0 = case.start_weight()
+    fe = _fractions(eng, w0)
+    for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
+        stats.scalar_gate(fe[k], [r.balance[i] / (r.photons_exc * w0) for r in ref])
+    ctx.close()
+
+
+@pytest.mark.gpu
+def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_file):
+    """Integrated R, T and absorbed fraction of the fast kernel within 0.1 % of
+    the reference streams, on a budget whose standard error resolves it."""
+    nthreads = os.cpu_count() or 1
+    case = cases.tiny(photons=1_000_000, per_voxel=0)
+    case.do_fl = 0
+    sim = case.oracle_sim()
+    ref = [oracle.run_refstream(sim, safeprimes_file, 70_000 + b, 1, libm=True, nthreads=nthreads)
+           for b in range(B)]
+    ctx = mc.Context(math=mc.MATH_FAST)
+    med = case.engine_medium(ctx)
+    eng = [_run(ctx, med, case, b, photons=20_000_000, emission=False, reuse=0, seed0=5000) for b in range(B)]
+    ctx.close()
+    w0 = case.start_weight()
+    fe = _fractions(eng, w0)
+    for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
+        r = [x.balance[i] / (x.photons_exc * w0) for x in ref]
+        out = stats.scalar_gate(fe[k], r)
+        assert 3 * out["sigma"] / abs(out["b"]) < 1e-3 or k == "exit_bottom", out  # the budget resolves 0.1 %
+        assert out["rel_diff"] < 1e-3 or (k == "exit_bottom" and out["rel_diff"] < 3 * out["sigma"] / out["b"]), out

@@ -1,0 +1,181 @@
+"""Pins the CPU oracle to the reference.
+
+The restatement in oracle/port.cpp, run with the reference's RNG streams and
+schedule and C-library math, must reproduce the reference's own transport
+(compiled for the host from its sources, oracle/_ref) bit for bit:
+  - against golden fixtures made by that build (tests/golden/, runs anywhere);
+  - live against the build itself where the reference checkout is present.
+The product's parser, writers and init_RNG are checked against the
+reference's own functions the same way.
+"""
+import ctypes
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from tests import cases
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+FIXTURES = {"tiny": dict(photons=40000, per_voxel=33000), "mismatch": dict(photons=36000, per_voxel=33000),
+            "glass": dict(photons=36000, per_voxel=33000)}
+
+
+def _same(a, b):
+    assert a.shape == b.shape
+    return np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", sorted(FIXTURES))
+def test_port_reproduces_reference_golden(name, oracle, safeprimes_file, tmp_path):
+    g = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
+    case = cases.ALL[name](**FIXTURES[name])
+    # the fixture was made from the .mci this case writes
+    mci = case.write_mci(str(tmp_path))
+    assert open(mci).read() == str(g["mci"])
+    s1, s2 = (int(v) for v in g["seeds"])
+    r = oracle.run_refstream(case.oracle_sim(), safeprimes_file, s1, s2, libm=True)
+    assert r.photons_exc == int(g["photons_exc"]) and r.photons_fl == int(g["photons_fl"])
+    assert r.fl_voxels == int(g["fl_voxels"])
+    for k in ("Rd", "Tt", "fhd", "flR", "flT"):
+        assert _same(getattr(r, k), g[k]), k
+
+
+@pytest.mark.parametrize("name", ["tiny", "glass"])
+def test_port_reproduces_reference_build_live(name, oracle, ref_oracle, safeprimes_file, tmp_path):
+    case = cases.ALL[name](photons=34000, per_voxel=32800)
+    mci = case.write_mci(str(tmp_path))
+    sim = ref_oracle.parse_mci(mci)
+    a = ref_oracle.run_mci(mci, safeprimes_file, 4242, 99)
+    b = oracle.run_refstream(sim, safeprimes_file, 4242, 99, libm=True)
+    for k in ("Rd", "Tt", "fhd", "flR", "flT"):
+        assert _same(getattr(a, k), getattr(b, k)), k
+
+
+def _sim_fields(s):
+    out = {k: getattr(s, k) for k, _ in s._fields_ if k not in ("bulks", "bulk_info", "vox_per_cm", "fluor_map")}
+    out["bulks"] = [tuple(np.float32(getattr(s.bulks[i], f)).tobytes() for f, _ in s.bulks[i]._fields_)
+                    for i in range(s.n_bulks + 2)]
+    return out
+
+
+@pytest.mark.parametrize("name", sorted(cases.ALL))
+def test_case_builder_matches_reference_parser(name, ref_oracle, tmp_path):
+    """tests/cases.py builds the oracle input with the same floats the
+    reference's parser derives from the .mci text."""
+    case = cases.ALL[name]()
+    mci = case.write_mci(str(tmp_path))
+    parsed = ref_oracle.parse_mci(mci)
+    built = case.oracle_sim()
+    a, b = _sim_fields(parsed), _sim_fields(built)
+    for k in ("number_of_photons", "number_of_photons_per_voxel", "n_bulks", "start_weight", "grid_size", "esp",
+              "xi", "yi", "zi", "dir", "fhd_activated", "do_fl_sim", "det_dx", "det_dy", "det_nx", "det_ny",
+              "det_x0", "det_y0", "bulks"):
+        assert a[k] == b[k], k
+    n = int(np.prod(case.labels.shape))
+    pa = np.ctypeslib.as_array(parsed.bulk_info, shape=(n,))
+    assert np.array_equal(pa, case.labels.ravel().astype(np.int16))
+
+
+def _product_parse(lib, mci):
+    import cudamcfl_gb300 as mc
+    cwd = os.getcwd()
+    os.chdir(os.path.dirname(mci))
+    try:
+        p, n = mc.read_simulation_data(os.path.basename(mci))
+    finally:
+        os.chdir(cwd)
+    return p, n
+
+
+def _ref_sample(path):
+    ref_dir = "/root/reference"
+    p = os.path.join(ref_dir, path)
+    if not os.path.exists(p):
+        pytest.skip("reference checkout not present")
+    return p
+
+
+@pytest.mark.parametrize("src", ["case:tiny", "case:mismatch", "case:glass", "ref:sample2.mci"])
+def test_product_parser_matches_reference_parser(src, mcfl_lib, ref_oracle, tmp_path):
+    import cudamcfl_gb300 as mc
+    if src.startswith("case:"):
+        mci = cases.ALL[src[5:]]().write_mci(str(tmp_path))
+    else:
+        mci = _ref_sample(src[4:])
+    ref = ref_oracle.parse_mci(mci)
+    p, n = _product_parse(mcfl_lib, mci)
+    try:
+        s = p[0]
+        for k in ("number_of_photons", "number_of_photons_per_voxel", "n_bulks", "start_weight", "grid_size",
+                  "do_fl_sim", "fhd_activated", "bulk_method"):
+            assert getattr(s, k) == getattr(ref, k), k
+        for k in ("esp", "xi", "yi", "zi", "dir"):
+            assert np.float32(getattr(s, k)).tobytes() == np.float32(getattr(ref, k)).tobytes(), k
+        for k, rk in (("dx", "det_dx"), ("dy", "det_dy"), ("x0", "det_x0"), ("y0", "det_y0")):
+            assert np.float32(getattr(s.det, k)).tobytes() == np.float32(getattr(ref, rk)).tobytes(), k
+        assert (s.det.nx, s.det.ny) == (ref.det_nx, ref.det_ny)
+        for i in range(s.n_bulks + 2):
+            for f, _ in mc.Bulk._fields_:
+                assert np.float32(getattr(s.bulks[i], f)).tobytes() == \
+                    np.float32(getattr(ref.bulks[i], f)).tobytes(), (i, f)
+        nv = s.num_x * s.num_y * s.num_z
+        a = np.ctypeslib.as_array(s.bulk_info, shape=(nv,)).astype(np.int16)
+        b = np.ctypeslib.as_array(ref.bulk_info, shape=(nv,))
+        assert np.array_equal(a, b)
+    finally:
+        mc.free_simulations(p, n)
+
+
+def test_product_init_rng_matches_reference(mcfl_lib, ref_oracle, safeprimes_file):
+    import cudamcfl_gb300 as mc
+    n = 32768
+    xa, aa = (ctypes.c_ulonglong * n)(), (ctypes.c_uint * n)()
+    xb, ab = (ctypes.c_ulonglong * n)(), (ctypes.c_uint * n)()
+    ref_oracle.lib.ref_init_rng.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_uint),
+                                            ctypes.c_uint, ctypes.c_char_p, ctypes.c_ulonglong]
+    for seed in (1, 12345, 2**40 + 7):
+        assert mcfl_lib.mcfl_init_RNG(xa, aa, n, safeprimes_file.encode(), seed) == 0
+        assert ref_oracle.lib.ref_init_rng(xb, ab, n, safeprimes_file.encode(), seed) == 0
+        assert list(xa) == list(xb) and list(aa) == list(ab)
+    assert mcfl_lib.mcfl_init_RNG(xa, aa, n, safeprimes_file.encode(), 0) == 1  # invalid seed, as the reference
+
+
+def _strip_param(text):
+    return [ln for ln in text.splitlines() if not ln.startswith("Compilation date") and "User time" not in ln]
+
+
+def test_writers_match_reference(mcfl_lib, ref_oracle, safeprimes_file, tmp_path):
+    """The product's writers format the reference's own tallies exactly as the
+    reference's writers do (all six output files)."""
+    import cudamcfl_gb300 as mc
+    case = cases.tiny(photons=34000, per_voxel=32800)
+    d1, d2 = tmp_path / "ref", tmp_path / "prod"
+    d1.mkdir()
+    d2.mkdir()
+    mci1 = case.write_mci(str(d1))
+    case.write_mci(str(d2))
+    r = ref_oracle.run_mci(mci1, safeprimes_file, 5, 6, write_files=True)
+    p, n = _product_parse(mcfl_lib, str(d2 / "tiny.mci"))
+    cwd = os.getcwd()
+    os.chdir(d2)
+    try:
+        sim = p[0]
+        Rd, Tt = r.Rd.copy(), r.Tt.copy()
+        assert mcfl_lib.mcfl_Write_Simulation_Results(p, mc.u64ptr(Rd), mc.u64ptr(Tt), 0.0) == 0
+        phd = (r.fhd.astype(np.float64) / float(0xFFFFFFFF * r.photons_exc)).copy()
+        assert mcfl_lib.mcfl_write_phd(p, mc.f64ptr(phd)) == 0
+        flR, flT = r.flR.copy(), r.flT.copy()
+        assert mcfl_lib.mcfl_write_fl_images(p, mc.f64ptr(flR), mc.f64ptr(flT)) == 0
+    finally:
+        os.chdir(cwd)
+        mc.free_simulations(p, n)
+    for suffix in ("_Refl.dat", "_Trans.dat", "_PHD-Ascii.dat", "_FlR.dat", "_FlT.dat"):
+        a = open(d1 / f"tiny-out{suffix}").read()
+        b = open(d2 / f"tiny-out{suffix}").read()
+        assert a == b, suffix
+    a = _strip_param(open(d1 / "tiny-out_param.dat").read())
+    b = _strip_param(open(d2 / "tiny-out_param.dat").read())
+    assert a == b

@@ -255,20 +255,24 @@ class RunResult:
 
 
 class Medium:
+    """A device-resident medium.  It is freed by free(), by garbage
+    collection, or by closing its context, whichever comes first."""
+
     def __init__(self, ctx: "Context", handle: int, shape: tuple, keep: list):
         self.ctx = ctx
         self.handle = handle
         self.shape = shape  # (nz, ny, nx)
         self._keep = keep
+        ctx._media.add(self)
 
     @property
     def nbytes(self) -> int:
         return int(load().mcfl_medium_bytes(self.handle))
 
     def free(self) -> None:
-        if self.handle:
+        if self.handle and self.ctx is not None and self.ctx.handle:
             load().mcfl_medium_free(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -281,8 +285,11 @@ class Context:
     """One GPU context of the engine."""
 
     def __init__(self, device: int = -1, math: int = MATH_EXACT, **options):
+        import weakref
         L = load()
         h = ctypes.c_void_p()
+        self.handle = None
+        self._media = weakref.WeakSet()
         check(L.mcfl_create(device, ctypes.byref(h)))
         self.handle = h
         self.set_option("math", math)
@@ -304,6 +311,8 @@ class Context:
 
     def close(self) -> None:
         if self.handle:
+            for m in list(self._media):
+                m.free()  # media go before their context (mcfl_medium_free needs it)
             load().mcfl_destroy(self.handle)
             self.handle = None
 

@@ -273,7 +273,8 @@ long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
  * restores the context's own stream. */
 int mcfl_set_stream(mcfl_ctx *ctx, void *stream);
 
-/* Uploads a medium; it stays resident until mcfl_medium_free. */
+/* Uploads a medium; it stays resident until mcfl_medium_free, which must
+ * come before mcfl_destroy of its context. */
 int mcfl_medium_create(mcfl_ctx *ctx, const mcfl_medium_desc *desc, mcfl_medium **medium);
 void mcfl_medium_free(mcfl_medium *medium);
 size_t mcfl_medium_bytes(const mcfl_medium *medium);

@@ -71,3 +71,132 @@ def test_excitation_only_and_no_fluence(gpu_ctx, oracle, table32768):
     res = gpu_ctx.run(med, case.run_desc(99, 100))
     assert np.array_equal(res.Rd, ref.Rd) and np.array_equal(res.Tt, ref.Tt)
     assert res.fhd is None and res.flR is None
+
+
+def _synthetic_sim(m, photons, per_voxel):
+    from oracle import pyoracle
+    nz, ny, nx = m.labels.shape
+    vc = m.voxel_cm
+    return pyoracle.sim_from_arrays(
+        m.labels, m.bulks, half_x=float(np.float32(nx * vc[0] / 2)), half_y=float(np.float32(ny * vc[1] / 2)),
+        thickness=float(np.float32(nz * vc[2])), vox_per_cm=[float(np.float32(1 / v)) for v in vc],
+        photons=photons, per_voxel=per_voxel,
+        det=(m.det.dx, m.det.dy, m.det.nx, m.det.ny, m.det.x0, m.det.y0), fluor_map=m.fluor_map)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cfg", ["config1", "config2"])
+def test_benchmark_media_bit_identical_to_oracle(cfg, gpu_ctx, oracle, table32768):
+    """General geometry (anisotropic voxels, lateral extent 2 x thickness),
+    8 labels, the fp32 fluorophore map: the workloads the benchmark runs."""
+    from cudamcfl_gb300 import media
+    m = getattr(media, cfg)()
+    photons, per_voxel = (20000, 40) if cfg == "config1" else (6000, 2)
+    ref = oracle.run_photon(_synthetic_sim(m, photons, per_voxel), table32768, 21, 22, libm=False)
+    med = gpu_ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
+    rd = mc.run_desc(photons, det=m.det, photons_per_voxel=per_voxel, fluence=1, seed_exc=21, seed_fl=22)
+    res = gpu_ctx.run(med, rd)
+    med.free()
+    _compare(res, ref)
+
+
+@pytest.mark.gpu
+def test_launch_rng_reuse_bit_identical_to_oracle(gpu_ctx, oracle, table32768):
+    case = cases.tiny(photons=40000, per_voxel=33000)
+    sim = case.oracle_sim()
+    sim.launch_rng_reuse = 1
+    ref = oracle.run_photon(sim, table32768, 8, 9, libm=False)
+    med = case.engine_medium(gpu_ctx)
+    rd = case.run_desc(8, 9)
+    rd.launch_rng_reuse = 1
+    _compare(gpu_ctx.run(med, rd), ref)
+
+
+@pytest.mark.gpu
+def test_weight_is_conserved_exactly(gpu_ctx):
+    """absorbed + left at both faces + roulette losses - roulette gains =
+    photons x start weight, in integers (no photon wraps its weight here)."""
+    from cudamcfl_gb300 import media
+    m = media.config2()
+    med = gpu_ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
+    for kind in (mc.SOURCE_GAUSS_BEAM, mc.SOURCE_WIDEFIELD):
+        rd = mc.run_desc(200_000, det=m.det, seed_exc=3, kind=kind, width=3.0, height=2.0)
+        r = gpu_ctx.run(med, rd)
+        s = r.stats_exc
+        w0 = int(np.float64(0xFFFFFFFF) * (1 - ((1.0 - np.float64(np.float32(1.4))) /
+                                               (1.0 + np.float64(np.float32(1.4)))) ** 2))
+        lhs = s["absorbed"] + s["exit_top"] + s["exit_bottom"] + s["roulette_loss"] + s["zero_drop_loss"] - \
+            s["roulette_gain"]
+        assert lhs % 2**64 == (200_000 * w0) % 2**64
+        assert abs(r.energy_exc[3]) < 1e-12
+        assert s["done"] == 200_000 and s["capped"] == 0
+    med.free()
+
+
+@pytest.mark.gpu
+def test_reference_host_routines_on_the_engine(mcfl_lib, oracle, table32768, tmp_path):
+    """mcfl_DoOneSimulation / mcfl_DoOneSimulationFl / mcfl_run_mci: the
+    drop-ins of DoOneSimulation, DoOneSimulationFl and cuda_fl's main."""
+    import ctypes
+    import os
+    case = cases.tiny(photons=40000, per_voxel=33000)
+    mci = case.write_mci(str(tmp_path))
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        p, n = mc.read_simulation_data("tiny.mci")
+        sim = p[0]
+        xy = sim.det.nx + sim.det.nx * sim.det.ny
+        nv = sim.num_x * sim.num_y * sim.num_z
+        Rd, Tt, fx = np.zeros(xy, np.uint64), np.zeros(xy, np.uint64), np.zeros(nv)
+        got = mcfl_lib.mcfl_DoOneSimulation(p, 77, mc.f64ptr(fx), mc.u64ptr(Rd), mc.u64ptr(Tt))
+        assert got == 40000 and Rd.sum() > 0 and fx.sum() > 0
+        o = case.oracle_sim()
+        o.do_fl_sim = 0
+        # the .mci path turns the reference's launch-number reuse on
+        o.launch_rng_reuse = 1
+        ref = oracle.run_photon(o, table32768, 77, 78, libm=False)
+        assert np.array_equal(Rd, ref.Rd) and np.array_equal(Tt, ref.Tt)
+        # one emission run from the voxel at the source corner, emission absorption as the caller sets it
+        for i in range(sim.n_bulks + 2):
+            sim.bulks[i].mua = sim.bulks[i].muaf
+        sim.xi, sim.yi, sim.zi = -0.25, -0.25, 0.0
+        sim.number_of_photons = 33000
+        R2, T2 = np.zeros(xy, np.uint64), np.zeros(xy, np.uint64)
+        got = mcfl_lib.mcfl_DoOneSimulationFl(p, 5, mc.u64ptr(R2), mc.u64ptr(T2))
+        assert got == 33000 and R2.sum() > 0
+        mc.free_simulations(p, n)
+        assert mcfl_lib.mcfl_run_mci(b"tiny.mci", ctypes.c_ulonglong(12345)) == 0
+        for suffix in ("_param.dat", "_Refl.dat", "_Trans.dat", "_PHD-Ascii.dat", "_FlR.dat", "_FlT.dat"):
+            assert os.path.getsize(f"tiny-out{suffix}") > 0
+        img = np.loadtxt("tiny-out_FlR.dat")
+        assert img.shape == (20, 20) and img.sum() > 0
+    finally:
+        os.chdir(cwd)
+
+
+@pytest.mark.gpu
+def test_bad_inputs_fail_with_status(gpu_ctx):
+    case = cases.tiny()
+    med = case.engine_medium(gpu_ctx)
+    rd = case.run_desc(1, 2)
+    rd.photons = 0
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.run(med, rd)
+    assert e.value.code == mc.E_ARG
+    rd = case.run_desc(1, 2)
+    rd.det.nx = 0
+    with pytest.raises(mc.McflError):
+        gpu_ctx.run(med, rd)
+    lab = case.labels.copy()
+    lab[0, 0, 0] = 9  # beyond n_bulks + 1
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.medium(lab, case.bulks(), vox_per_cm=(4.0, 4.0, 4.0), half_x=1.0, half_y=1.0, thickness=0.5)
+    assert e.value.code == mc.E_ARG
+    gpu_ctx.set_option("step_cap", 50)  # photons live for hundreds of passes: the cap must report
+    try:
+        with pytest.raises(mc.McflError) as e:
+            gpu_ctx.run(med, case.run_desc(1, 2, photons=2000))
+        assert e.value.code == mc.E_CAPPED
+    finally:
+        gpu_ctx.set_option("step_cap", 1 << 24)

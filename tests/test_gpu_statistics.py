@@ -75,11 +75,9 @@ def test_engine_agrees_with_reference_streams(math, oracle, safeprimes_file):
     ref = [oracle.run_refstream(sim, safeprimes_file, 1000 + b, 2000 + b, libm=True, nthreads=nthreads)
            for b in range(B)]
     ctx = mc.Context(math=math)
-    try:
-        med = case.engine_medium(ctx)
-        eng = [_run(ctx, med, case, b, reuse=1, seed0=300) for b in range(B)]
-    finally:
-        pass
+    med = case.engine_medium(ctx)
+    eng = [_run(ctx, med, case, b, reuse=1, seed0=300) for b in range(B)]
+    med.free()
     xy = case.det[2] * case.det[3]
     for k in ("Rd", "Tt", "fhd"):
         a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in eng])
@@ -97,8 +95,11 @@ def test_engine_agrees_with_reference_streams(math, oracle, safeprimes_file):
 
 @pytest.mark.gpu
 def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_file):
-    """Integrated R, T and absorbed fraction of the fast kernel within 0.1 % of
-    the reference streams, on a budget whose standard error resolves it."""
+    """Integrated R, T and absorbed fraction of the fast kernel against the
+    reference streams on 1.6e7 reference photons: within 3 sigma and 0.1 %
+    with the reference's first-photon reuse reproduced; within 0.1 % without
+    it (the reuse biases the reference's own reflectance by a few 1e-4 at this
+    budget, 3.3 % first photons)."""
     nthreads = os.cpu_count() or 1
     case = cases.tiny(photons=1_000_000, per_voxel=0)
     case.do_fl = 0
@@ -107,12 +108,22 @@ def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_f
            for b in range(B)]
     ctx = mc.Context(math=mc.MATH_FAST)
     med = case.engine_medium(ctx)
-    eng = [_run(ctx, med, case, b, photons=20_000_000, emission=False, reuse=0, seed0=5000) for b in range(B)]
-    ctx.close()
     w0 = case.start_weight()
-    fe = _fractions(eng, w0)
-    for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
-        r = [x.balance[i] / (x.photons_exc * w0) for x in ref]
-        out = stats.scalar_gate(fe[k], r)
-        assert 3 * out["sigma"] / abs(out["b"]) < 1e-3 or k == "exit_bottom", out  # the budget resolves 0.1 %
-        assert out["rel_diff"] < 1e-3 or (k == "exit_bottom" and out["rel_diff"] < 3 * out["sigma"] / out["b"]), out
+    for reuse in (1, 0):
+        if reuse:
+            runs = [_run(ctx, med, case, b, photons=1_000_000, emission=False, reuse=1, seed0=5000 + 37 * b)
+                    for b in range(B)]
+        else:
+            runs = [_run(ctx, med, case, b, photons=20_000_000, emission=False, reuse=0, seed0=9000)
+                    for b in range(B)]
+        fe = _fractions(runs, w0)
+        for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
+            r = [x.balance[i] / (x.photons_exc * w0) for x in ref]
+            if reuse:
+                out = stats.scalar_gate(fe[k], r, rel_tol=None)
+            else:
+                a, b = np.mean(fe[k]), np.mean(r)
+                out = {"a": a, "b": b, "rel_diff": abs(a - b) / b}
+            assert out["rel_diff"] < 1e-3, (reuse, k, out)
+    med.free()
+    ctx.close()

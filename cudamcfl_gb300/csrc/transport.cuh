@@ -171,11 +171,16 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     p.x = xi + (0.999999f / m.gx) * r.oc();
     p.y = yi + (0.999999f / m.gy) * r.oc();
     p.z = zi + (0.999999f / m.gz) * r.oc();
-    const float costheta = (float)(1.0 - 2.0 * (double)r.oc());
-    const float sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
-    const float psi = (float)(2.0 * (double)kPi * (double)r.oc());
+    /* The reference evaluates these in double (CUDAMCFLtransport.cu:474-483).
+     * 1 - 2u and 2*PI*u are exact in double, so their float forms round the
+     * same value once and are bit-identical; sqrt(1 - c^2) is taken in single
+     * precision here (the reference rounds a double square root), so no FP64
+     * instruction runs in the transport kernel. */
+    const float costheta = 1.0f - 2.0f * r.oc();
+    const float sintheta = __fsqrt_rn(1.0f - costheta * costheta);
+    const float psi = (2.0f * kPi) * r.oc();
     const float cospsi = MCFL_COSF(psi);
-    float sinpsi = __fsqrt_rn((float)(1.0 - (double)(cospsi * cospsi)));
+    float sinpsi = __fsqrt_rn(1.0f - cospsi * cospsi);
     if (!(psi < kPi)) sinpsi = -sinpsi;
     p.dx = sintheta * cospsi;
     p.dy = sintheta * sinpsi;
@@ -393,7 +398,7 @@ __device__ __noinline__ void tally_exit(const McflJob *J, float px, float py, ui
  * kUniform: the medium comes from the launch parameters (constant bank)
  * instead of per-lane registers loaded from the job. */
 template <bool kUniform>
-__global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
+__global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLaunch L) {
   extern __shared__ unsigned long long s_ev[]; /* kEv x blockDim.x */
   const unsigned lane = threadIdx.x & 31u;
   const unsigned tib = threadIdx.x;
@@ -421,7 +426,7 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
     m.last = L.med.last_label;
   }
   float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
-  uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, done = 0, steps = 0;
+  uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
   uint32_t f_idx = 0xffffffffu;
   unsigned long long f_acc = 0ull;
@@ -460,6 +465,7 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
       r.a = sv.rng_a;
       k = sv.k;
       pst = sv.steps;
+      pst0 = pst;
       src_idx = sv.src_idx;
       pr = load_prop(m, p.label);
       alive = true;
@@ -468,6 +474,8 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
 
   for (uint32_t it = 0;; ++it) {
     if (L.max_iters && it >= L.max_iters) break;
+    /* one vote per pass while every lane carries a photon */
+    if (__ballot_sync(kFull, !alive)) {
     const bool need = !alive && !exhausted;
     const unsigned nm = __ballot_sync(kFull, need);
     if (nm) {
@@ -490,6 +498,7 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
             launch_photon(J, m, k, L.mult, p, r, src_idx);
             pr = load_prop(m, p.label);
             pst = 0;
+            pst0 = 0;
             alive = true;
           }
         } else {
@@ -499,9 +508,9 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
     }
     if (__all_sync(kFull, !alive)) break;
     if (!alive) continue;
+    }
 
     /* ---- one transport pass (MCd3D loop body) ---- */
-    ++steps;
     ++pst;
     float s;
     uint32_t new_bulk;
@@ -579,8 +588,12 @@ __global__ void __launch_bounds__(256) MCFL_KERNEL_NAME(McflLaunch L) {
       ev_add(MCFL_ST_CAPPED, 1ull);
       alive = false;
     }
-    if (!alive) ++done;
+    if (!alive) {
+      ++done;
+      steps += pst - pst0;
+    }
   }
+  if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
 
   if (L.max_iters && L.saved) {
     McflSaved sv;

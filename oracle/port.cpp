@@ -135,21 +135,32 @@ inline uint32_t start_label(const Phase &ph, const Photon &p) {
   return ph.last_bulk;
 }
 
-template <class M>
+/* kSingle: the engine's all-single-precision isotropic launch (1 - 2u and
+ * 2 PI u are bit-identical either way; the square root of 1 - cos^2 theta is
+ * a single-precision square root instead of a rounded double one). */
+template <class M, bool kSingle = false>
 void launch_photon(Photon &p, Rng &r, const Phase &ph, float xi, float yi, float zi) {
   if (ph.dir == 0.0f) {
     p.x = xi + (0.999999f / ph.gx) * r.oc();
     p.y = yi + (0.999999f / ph.gy) * r.oc();
     p.z = zi + (0.999999f / ph.gz) * r.oc();
-    float costheta = (float)(1.0 - 2.0 * (double)r.oc());
-    float sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
-    float psi = (float)(2.0 * (double)kPi * (double)r.oc());
+    float costheta, sintheta, psi;
+    if (kSingle) {
+      costheta = 1.0f - 2.0f * r.oc();
+      sintheta = sqrtf(1.0f - costheta * costheta);
+      psi = (2.0f * kPi) * r.oc();
+    } else {
+      costheta = (float)(1.0 - 2.0 * (double)r.oc());
+      sintheta = (float)sqrt(1.0 - (double)(costheta * costheta));
+      psi = (float)(2.0 * (double)kPi * (double)r.oc());
+    }
     float cospsi = M::cos(psi);
     float sinpsi;
+    const float sin2 = kSingle ? 1.0f - cospsi * cospsi : (float)(1.0 - (double)(cospsi * cospsi));
     if (psi < kPi)
-      sinpsi = sqrtf((float)(1.0 - (double)(cospsi * cospsi)));
+      sinpsi = sqrtf(sin2);
     else
-      sinpsi = -sqrtf((float)(1.0 - (double)(cospsi * cospsi)));
+      sinpsi = -sqrtf(sin2);
     p.dx = sintheta * cospsi;
     p.dy = sintheta * sinpsi;
     p.dz = costheta;
@@ -649,9 +660,9 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
       float yi = ((float)iy / ph.gy) - ph.hy;
       float zi = ((float)iz / ph.gz);
       sk.voxel_q = voxq[k / nv];
-      launch_photon<M>(p, r, ph, xi, yi, zi);
+      launch_photon<M, true>(p, r, ph, xi, yi, zi);
     } else {
-      launch_photon<M>(p, r, ph, ph.xi, ph.yi, ph.zi);
+      launch_photon<M, true>(p, r, ph, ph.xi, ph.yi, ph.zi);
     }
     if (ph.launch_rng_reuse && k_in_run < kThreads) r.x = x_at_launch;
     while (step<M>(p, r, ph, sk)) {

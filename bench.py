@@ -193,6 +193,7 @@ def main():
                     help="small case for ncu: the benchmark medium, --photons excitation photons and 20 emission "
                          "photons per voxel, --warmup runs then one run (2 transport launches per run)")
     ap.add_argument("--photons", type=int, default=2_000_000)
+    ap.add_argument("--variant", type=int, default=0, help="--profile: kernel variant (0..2)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -228,6 +229,9 @@ def main():
 
     def one_step():
         return lib.mcfl_run(ctx.handle, med.handle, mc.ctypes.byref(rd), mc.ctypes.byref(stats_out))
+
+    # launch shape: time every kernel variant on a 4e6-photon sample, keep the fastest
+    variant, tune_rate = ctx.autotune(med, rd, sample_photons=4_000_000)
 
     for _ in range(args.warmup):
         mc.check(one_step())
@@ -273,7 +277,10 @@ def main():
         "config": {"workload": WORKLOAD, "photons_per_step": photons_step[0], "excitation_photons": EXC_PHOTONS,
                    "emitting_voxels": stats_out.fl_voxels, "emission_photons": stats_out.photons_fl,
                    "math": args.math, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas only",
-                   "schedule": "batched: one persistent launch per phase, CUDA-graph replay"},
+                   "schedule": "batched: one persistent launch per phase, CUDA-graph replay",
+                   "variant": variant, "block": ctx.get_option("launch_block"), "grid": ctx.get_option("grid"),
+                   "regs": ctx.get_option("regs"), "l2_window": ctx.get_option("l2_window"),
+                   "autotune_sample_photons_per_s": tune_rate},
         "phases": {"excitation_ms": statistics.mean(exc_ms), "emission_ms": statistics.mean(fl_ms),
                    "excitation_photons_per_s": EXC_PHOTONS / (statistics.mean(exc_ms) / 1e3),
                    "emission_photons_per_s": stats_out.photons_fl / (statistics.mean(fl_ms) / 1e3),
@@ -289,10 +296,17 @@ def main():
         return 0
 
     # --- roofline of the dominant kernel (the transport kernel) ---
-    # Algorithmic work unit: one transport step of the reference (SURVEY
-    # per-step op table: ~60 FP32 + 10 SFU + 8 conversion + 3 integer).
-    ops_per_step = 81
-    steps_s = result["phases"]["transport_steps_per_s"]
+    # Algorithmic work per transport pass, counted from the reference's
+    # source (CUDAMCFLtransport.cu:286-447,585-625): 10 MUFU (log, sin, cos,
+    # 2 sqrt, rsqrt, 4 reciprocals) + 8 conversions on the XU pipe (16 lanes
+    # per SM per clock), ~60 FP32 operations on the FMA pipes (128 lanes).
+    # achieved = ops per launch / mean launch time (CUDA events around each
+    # transport launch inside the replayed graph); the larger fraction is the
+    # bound.
+    xu_ops, fp32_ops = 18, 60
+    passes = se["steps"] + sf["steps"]
+    launch_s = (statistics.mean(exc_ms) + statistics.mean(fl_ms)) / 1e3
+    pass_rate = passes / launch_s
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -300,21 +314,33 @@ def main():
         pass
     sm_mhz = peaks.get("sm_max_mhz", 2070.0)
     n_sm = ctx.get_option("sm_count")
-    fp32_peak = n_sm * 128 * sm_mhz * 1e6  # FP32 lane operations per second
+    xu_peak = n_sm * 16 * sm_mhz * 1e6
+    fp32_peak = n_sm * 128 * sm_mhz * 1e6
+    # DRAM bytes per transport launch from the ncu launch list summarised in
+    # profiles/transport_fast_config2.md (medium and tallies stay in L2, so a
+    # launch's DRAM traffic is its footprint, independent of its passes)
     traffic = None
     try:
-        prof = json.load(open(os.path.join(ROOT, "profiles", "transport_roofline.json")))
-        traffic = prof.get("dram_bytes_per_step", None)
-        if traffic is not None:
-            traffic = traffic * (se["steps"] + sf["steps"]) / 2
+        vals = {}
+        for line in open(os.path.join(ROOT, "profiles", "transport_fast_config2.md")):
+            if line.startswith("dram_bytes_per_launch_"):
+                k, v = line.split(":", 1)
+                vals[k.strip()] = float(v)
+        if vals:
+            traffic = sum(vals.values()) / len(vals)
     except (OSError, ValueError):
         pass
     result["roofline"] = {
-        "bound": "issue", "achieved": ops_per_step * steps_s / 1e12, "peak": fp32_peak / 1e12, "unit": "Top/s",
-        "frac": ops_per_step * steps_s / fp32_peak, "traffic": traffic,
-        "note": (f"algorithmic FP32/SFU/convert ops of one transport step ({ops_per_step}) x steps/s over "
-                 f"{n_sm} SMs x 128 FP32 lanes x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); neither HBM "
-                 "nor tensor cores bound this kernel"),
+        "bound": "xu", "achieved": xu_ops * pass_rate / 1e12, "peak": xu_peak / 1e12, "unit": "Top/s",
+        "frac": xu_ops * pass_rate / xu_peak, "traffic": traffic,
+        "fp32": {"achieved": fp32_ops * pass_rate / 1e12, "peak": fp32_peak / 1e12,
+                 "frac": fp32_ops * pass_rate / fp32_peak},
+        "passes_per_s": pass_rate,
+        "note": (f"neither HBM nor tensor cores bound this kernel (no contraction; medium and tallies L2-resident): "
+                 f"algorithmic XU ops ({xu_ops}: 10 MUFU + 8 conversions) per transport pass x passes/s over "
+                 f"{n_sm} SMs x 16 XU lanes x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); FP32 analogue "
+                 f"({fp32_ops} ops/pass over 128 lanes) beside it; traffic = mean DRAM bytes per transport launch "
+                 "(ncu, cold cache)"),
     }
 
     # --- e2e through the C ABI with host buffers ---
@@ -399,6 +425,7 @@ def profile_case(args):
     from cudamcfl_gb300 import build, media
     build.build()
     ctx = mc.Context(device=0, math=mc.MATH_FAST if args.math == "fast" else mc.MATH_EXACT)
+    ctx.set_option("variant", args.variant)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
     rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=20, fluence=1, seed_exc=1, seed_fl=2)
@@ -407,7 +434,8 @@ def profile_case(args):
     print(json.dumps({"profile_case": "config2", "math": args.math, "photons": args.photons,
                       "emission_photons": r.photons_fl, "steps_exc": r.stats_exc["steps"],
                       "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
-                      "regs": ctx.get_option("regs"), "grid": ctx.get_option("grid")}), flush=True)
+                      "variant": args.variant, "regs": ctx.get_option("regs"), "grid": ctx.get_option("grid"),
+                      "block": ctx.get_option("launch_block")}), flush=True)
     med.free()
     ctx.close()
     return 0

@@ -24,6 +24,7 @@ LIB_PATH = _build.LIB
 
 MATH_EXACT = 0
 MATH_FAST = 1
+MATH_F64 = 2  # the same kernel in double precision (precision study)
 SOURCE_GAUSS_BEAM = 1
 SOURCE_WIDEFIELD = 3
 NSTATS = 9
@@ -164,6 +165,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mcfl_medium_bytes": (ctypes.c_size_t, [vp]),
         "mcfl_medium_from_simulation": (ctypes.c_int, [vp, P(Simulation), P(vp)]),
         "mcfl_run": (ctypes.c_int, [vp, vp, P(RunDesc), P(RunOut)]),
+        "mcfl_autotune": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_ulonglong, P(ctypes.c_int),
+                                         P(ctypes.c_double)]),
         "mcfl_run_desc_from_simulation": (ctypes.c_int, [P(Simulation), ctypes.c_ulonglong, P(RunDesc)]),
         "mcfl_launch_count": (ctypes.c_ulonglong, [vp]),
         "mcfl_read_simulation_data": (ctypes.c_int, [ctypes.c_char_p, P(P(Simulation)), ctypes.c_int]),
@@ -304,6 +307,15 @@ class Context:
 
     def set_stream(self, stream_handle: int | None) -> None:
         check(load().mcfl_set_stream(self.handle, stream_handle))
+
+    def autotune(self, medium: "Medium", rd: RunDesc, sample_photons: int = 2_000_000) -> tuple[int, float]:
+        """Times every kernel variant (with and without the L2 window) on a
+        sample of `rd` and keeps the fastest; returns (variant, photons/s)."""
+        v = ctypes.c_int(0)
+        rate = ctypes.c_double(0.0)
+        check(load().mcfl_autotune(self.handle, medium.handle, ctypes.byref(rd), int(sample_photons),
+                                   ctypes.byref(v), ctypes.byref(rate)))
+        return v.value, rate.value
 
     @property
     def launches(self) -> int:

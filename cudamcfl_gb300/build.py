@@ -32,10 +32,11 @@ FAST = ["--use_fast_math"]
 CUDA_UNITS = {
     "transport_exact.cu": EXACT,
     "transport_fast.cu": FAST,
+    "transport_f64.cu": [],
     "engine_kernels.cu": EXACT,
     "noalloc.cu": EXACT,
 }
-HOST_UNITS = ["engine.cpp", "run.cpp", "mci.cpp", "safeprimes.cpp", "server.cpp"]
+HOST_UNITS = ["engine.cpp", "run.cpp", "mci.cpp", "safeprimes.cpp", "server.cpp", "tune.cpp"]
 HEADERS = ["engine_types.h", "portable_math.h", "mcfl_internal.h", "transport.cuh"]
 
 

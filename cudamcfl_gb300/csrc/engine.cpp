@@ -64,25 +64,26 @@ void DevBuf::release() {
 using namespace mcfl;
 
 
-int mcfl_ctx::grid_for(int block_size, int *bps_out, bool uniform) {
-  int bps = 0, regs = 0;
-  cudaError_t e;
-  if (uniform)
-    e = math == MCFL_MATH_FAST ? mcfl_attr_transport_fast_uniform(block_size, &bps, &regs)
-                               : mcfl_attr_transport_exact_uniform(block_size, &bps, &regs);
-  else
-    e = math == MCFL_MATH_FAST ? mcfl_attr_transport_fast(block_size, &bps, &regs)
-                               : mcfl_attr_transport_exact(block_size, &bps, &regs);
-  if (e != cudaSuccess || bps <= 0) bps = 1;
+int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs) {
+  *blk = block;
+  *bps = 0;
+  *regs = 0;
+  const int v = uniform ? variant : -1;
+  return (int)attr_fn(math)(v, blk, bps, regs);
+}
+
+int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out) {
+  int blk = 0, bps = 0, regs = 0;
+  if (attr(uniform, &blk, &bps, &regs) != 0 || bps <= 0) bps = 1;
   if (blocks_per_sm > 0 && blocks_per_sm < bps) bps = blocks_per_sm;
   if (bps_out) *bps_out = bps;
+  if (block_out) *block_out = blk;
   return bps * sm_count;
 }
 
 cudaError_t mcfl_ctx::launch_transport(const McflLaunch &L, int grid, int block_size) {
   ++launches;
-  return math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block_size, stream)
-                                : mcfl_launch_transport_exact(&L, grid, block_size, stream);
+  return launch_fn(math)(&L, grid, block_size, stream);
 }
 
 extern "C" const char *mcfl_last_error(void) { return g_last_error.c_str(); }
@@ -133,6 +134,10 @@ extern "C" void mcfl_destroy(mcfl_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+  if (c->l2_persist_bytes) { /* give the set-aside back to the process's other users */
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    cudaCtxResetPersistingL2Cache();
+  }
   for (auto &ev : c->ev)
     if (ev) cudaEventDestroy(ev);
   if (c->graph_run) cudaGraphExecDestroy(c->graph_run);
@@ -147,11 +152,15 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
   if (!c || !key) return fail(MCFL_E_ARG, "mcfl_set_option: null argument");
   const std::string k(key);
   if (k == "math") {
-    if (v != MCFL_MATH_EXACT && v != MCFL_MATH_FAST) return fail(MCFL_E_ARG, "math: 0 (exact) or 1 (fast)");
+    if (v != MCFL_MATH_EXACT && v != MCFL_MATH_FAST && v != MCFL_MATH_F64)
+      return fail(MCFL_E_ARG, "math: 0 (exact), 1 (fast) or 2 (f64)");
     c->math = (int)v;
   } else if (k == "block") {
     if (v < 32 || v > 256 || (v % 32)) return fail(MCFL_E_ARG, "block: a multiple of 32 in [32, 256]");
     c->block = (int)v;
+  } else if (k == "variant") {
+    if (v < 0 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant: 0..2");
+    c->variant = (int)v;
   } else if (k == "blocks_per_sm") {
     if (v < 0 || v > 64) return fail(MCFL_E_ARG, "blocks_per_sm: 0..64");
     c->blocks_per_sm = (int)v;
@@ -159,6 +168,16 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
     if (v < 1 || v > 0x7fffffffLL) return fail(MCFL_E_ARG, "step_cap: 1..2^31-1");
     c->step_cap = (uint32_t)v;
   } else if (k == "l2_window") {
+    MCFL_CUDA_TRY(cudaSetDevice(c->device));
+    if (v) {
+      int persist = 0, window = 0;
+      MCFL_CUDA_TRY(cudaDeviceGetAttribute(&persist, cudaDevAttrMaxPersistingL2CacheSize, c->device));
+      MCFL_CUDA_TRY(cudaDeviceGetAttribute(&window, cudaDevAttrMaxAccessPolicyWindowSize, c->device));
+      if (persist <= 0 || window <= 0) return fail(MCFL_E_STATE, "l2_window: the device has no persisting L2");
+      if (!c->l2_persist_bytes) MCFL_CUDA_TRY(cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)persist));
+      c->l2_persist_bytes = (size_t)persist;
+      c->l2_max_window = (size_t)window;
+    }
     c->l2_window = v ? 1 : 0;
   } else if (k == "graphs") {
     c->use_graphs = v ? 1 : 0;
@@ -174,18 +193,22 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "math") return c->math;
   if (k == "block") return c->block;
   if (k == "blocks_per_sm") return c->blocks_per_sm;
+  if (k == "variant") return c->variant;
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;
   if (k == "graphs") return c->use_graphs;
   if (k == "graph_failed") return c->graph_error.empty() ? 0 : 1;
   if (k == "sm_count") return c->sm_count;
-  if (k == "grid") return c->grid_for(c->block, nullptr, true);
-  if (k == "grid_general") return c->grid_for(c->block, nullptr, false);
+  if (k == "grid") return c->grid_for(true, nullptr);
+  if (k == "grid_general") return c->grid_for(false, nullptr);
+  if (k == "launch_block") {
+    int blk = 0;
+    c->grid_for(true, &blk);
+    return blk;
+  }
   if (k == "regs" || k == "regs_general") {
-    int bps = 0, regs = 0;
-    const bool u = k == "regs";
-    if (c->math == MCFL_MATH_FAST) (u ? mcfl_attr_transport_fast_uniform : mcfl_attr_transport_fast)(c->block, &bps, &regs);
-    else (u ? mcfl_attr_transport_exact_uniform : mcfl_attr_transport_exact)(c->block, &bps, &regs);
+    int blk = 0, bps = 0, regs = 0;
+    c->attr(k == "regs", &blk, &bps, &regs);
     return regs;
   }
   return -1;
@@ -228,11 +251,14 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
   m->bulks.assign(d->bulks, d->bulks + d->n_bulks + 2);
   const int nl = d->n_bulks + 2;
   std::vector<float> pe(4 * (size_t)nl), pm(4 * (size_t)nl), fl(2 * (size_t)nl);
+  std::vector<float> le(MCFL_LAB_FLOATS * (size_t)nl), lm(MCFL_LAB_FLOATS * (size_t)nl);
   for (int i = 0; i < nl; ++i) {
     const mcfl_bulk &b = d->bulks[i];
     pe[4 * i + 0] = b.mutr; pe[4 * i + 1] = b.mua; pe[4 * i + 2] = b.g; pe[4 * i + 3] = b.n;
     pm[4 * i + 0] = b.mutr; pm[4 * i + 1] = b.muaf; pm[4 * i + 2] = b.g; pm[4 * i + 3] = b.n;
     fl[2 * i + 0] = b.eY; fl[2 * i + 1] = b.albedof;
+    mcfl_label_record(b.mutr, b.mua, b.g, b.n, &le[MCFL_LAB_FLOATS * (size_t)i]);
+    mcfl_label_record(b.mutr, b.muaf, b.g, b.n, &lm[MCFL_LAB_FLOATS * (size_t)i]);
   }
   cudaError_t e = m->labels.reserve(total);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->labels.p, d->labels, total, cudaMemcpyHostToDevice, c->stream);
@@ -240,6 +266,10 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->prop_exc.p, pe.data(), pe.size() * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = m->prop_emi.reserve(pm.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->prop_emi.p, pm.data(), pm.size() * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = m->lab_exc.reserve(le.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->lab_exc.p, le.data(), le.size() * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = m->lab_emi.reserve(lm.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->lab_emi.p, lm.data(), lm.size() * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = m->fl.reserve(fl.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->fl.p, fl.data(), fl.size() * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && d->fluor_map) {
@@ -252,7 +282,8 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
     delete m;
     return cuda_fail(e, "mcfl_medium_create");
   }
-  m->bytes = m->labels.bytes + m->prop_exc.bytes + m->prop_emi.bytes + m->fl.bytes + m->fmap.bytes;
+  m->bytes = m->labels.bytes + m->prop_exc.bytes + m->prop_emi.bytes + m->lab_exc.bytes + m->lab_emi.bytes +
+             m->fl.bytes + m->fmap.bytes;
   *out = m;
   return MCFL_OK;
 }

@@ -47,6 +47,7 @@ typedef struct MCFL_ALIGN(16) McflJob {
   /* medium (bulk-descriptor voxel grid, x fastest) */
   const uint8_t *labels;
   const float *prop; /* 4 floats per label: 1/(mu_a+mu_s) (FLT_MAX = no scattering), mu_a, g, n */
+  const float *lab;  /* MCFL_LAB_FLOATS per label, see mcfl_label_record */
   float hx, hy, esp; /* |x| < hx, |y| < hy, 0 <= z < esp */
   float gx, gy, gz;  /* voxels per cm */
   uint32_t nx, ny, nz, total;
@@ -90,10 +91,21 @@ typedef struct MCFL_ALIGN(16) McflSaved {
   uint32_t pad;
 } McflSaved;
 
+/* Per-label constants of the transport, derived once from
+ * (mutr = 1/(mu_a+mu_s), mu_a, g, n) with the operations the reference
+ * performs on every pass, so precomputing them changes no bit:
+ *   [0] mutr   [1] mu_a*mutr   [2] 1-g*g   [3] 1-g
+ *   [4] 2*g    [5] 1+g*g       [6] 1/(2*g) (fast-math kernel only)   [7] n  */
+#define MCFL_LAB_FLOATS 8
+#define MCFL_MAX_LABELS 256
+
 /* Medium of a launch whose jobs all share it (kernel parameters). */
 typedef struct McflMedium {
   const uint8_t *labels;
   const float *prop;
+  const float *lab;     /* label records (MCFL_LAB_FLOATS each), staged in shared memory */
+  uint32_t n_labels;    /* records in lab (<= MCFL_MAX_LABELS) */
+  uint32_t pad0;
   unsigned long long *fhd; /* NULL when no job tallies the photon hitting density */
   float hx, hy, esp, gx, gy, gz;
   uint32_t nx, ny, total, last_label;
@@ -111,7 +123,28 @@ typedef struct McflLaunch {
   McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
   uint32_t uniform_medium; /* 1: every job uses med (and fhd_on agrees with med.fhd) */
+  uint32_t variant;        /* occupancy variant of the single-medium kernel */
+  float l2_hit_ratio;      /* host side: persisting-L2 window over [l2_base, +l2_bytes) when l2_bytes > 0 */
+  const void *l2_base;
+  unsigned long long l2_bytes;
   McflMedium med;
 } McflLaunch;
+
+
+/* Builds one label record (host or device; IEEE single precision, no
+ * contraction in the translation units that call it). */
+#if defined(__CUDACC__)
+__host__ __device__
+#endif
+static inline void mcfl_label_record(float mutr, float mua, float g, float n, float *out) {
+  out[0] = mutr;
+  out[1] = mua * mutr;
+  out[2] = 1.0f - g * g;
+  out[3] = 1.0f - g;
+  out[4] = 2.0f * g;
+  out[5] = 1.0f + g * g;
+  out[6] = 1.0f / (2.0f * g);
+  out[7] = n;
+}
 
 #endif

@@ -62,10 +62,26 @@ extern "C" cudaError_t mcfl_launch_normalize_128(const unsigned long long *raw, 
 /* transport kernels */
 extern "C" cudaError_t mcfl_launch_transport_exact(const McflLaunch *L, int grid, int block, cudaStream_t s);
 extern "C" cudaError_t mcfl_launch_transport_fast(const McflLaunch *L, int grid, int block, cudaStream_t s);
-extern "C" cudaError_t mcfl_attr_transport_exact(int block, int *blocks_per_sm, int *regs);
-extern "C" cudaError_t mcfl_attr_transport_fast(int block, int *blocks_per_sm, int *regs);
-extern "C" cudaError_t mcfl_attr_transport_exact_uniform(int block, int *blocks_per_sm, int *regs);
-extern "C" cudaError_t mcfl_attr_transport_fast_uniform(int block, int *blocks_per_sm, int *regs);
+/* Occupancy of a kernel variant (variant < 0: mixed media; 0..MCFL_N_VARIANTS-1:
+ * single medium) at *block threads (clamped to the variant's bound). */
+extern "C" cudaError_t mcfl_attr_transport_exact(int variant, int *block, int *blocks_per_sm, int *regs);
+extern "C" cudaError_t mcfl_attr_transport_fast(int variant, int *block, int *blocks_per_sm, int *regs);
+extern "C" cudaError_t mcfl_launch_transport_f64(const McflLaunch *L, int grid, int block, cudaStream_t s);
+extern "C" cudaError_t mcfl_attr_transport_f64(int variant, int *block, int *blocks_per_sm, int *regs);
+typedef cudaError_t (*LaunchFn)(const McflLaunch *, int, int, cudaStream_t);
+typedef cudaError_t (*AttrFn)(int, int *, int *, int *);
+/* The transport kernel build of a math mode (MCFL_MATH_*). */
+inline LaunchFn launch_fn(int math) {
+  return math == MCFL_MATH_FAST  ? mcfl_launch_transport_fast
+         : math == MCFL_MATH_F64 ? mcfl_launch_transport_f64
+                                 : mcfl_launch_transport_exact;
+}
+inline AttrFn attr_fn(int math) {
+  return math == MCFL_MATH_FAST  ? mcfl_attr_transport_fast
+         : math == MCFL_MATH_F64 ? mcfl_attr_transport_f64
+                                 : mcfl_attr_transport_exact;
+}
+constexpr int MCFL_N_VARIANTS = 3;
 
 /* engine.cpp: one emission run from one voxel with the medium's excitation
  * table (DoOneSimulationFl), raw 64-bit images */
@@ -79,7 +95,7 @@ void simulation_geometry(const mcfl_simulation *sim, float *half_x, float *half_
 
 struct mcfl_medium {
   mcfl_ctx *ctx = nullptr;
-  mcfl::DevBuf labels, prop_exc, prop_emi, fl, fmap;
+  mcfl::DevBuf labels, prop_exc, prop_emi, lab_exc, lab_emi, fl, fmap;
   int nx = 0, ny = 0, nz = 0;
   uint32_t total = 0;
   float hx = 0, hy = 0, esp = 0, gx = 0, gy = 0, gz = 0;
@@ -113,14 +129,20 @@ struct mcfl_ctx {
   std::string graph_error; /* why graphs were switched off, if they were */
   mcfl::DevBuf bR, bT, bstats, bcnt, seg_scale; /* batch workspace */
   int math = MCFL_MATH_EXACT;
-  int block = 256;
+  int block = 256;   /* threads per block, clamped to the variant's bound */
+  int variant = 0;   /* occupancy variant of the single-medium kernel */
   int blocks_per_sm = 0;
   uint32_t step_cap = 1u << 24;
-  int l2_window = 0;
+  int l2_window = 0;            /* 1: persisting-L2 window over the medium's labels */
+  size_t l2_persist_bytes = 0;  /* persisting set-aside this context asked for */
+  size_t l2_max_window = 0;     /* cudaDevAttrMaxAccessPolicyWindowSize */
   unsigned long long launches = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
-  int grid_for(int block_size, int *bps_out = nullptr, bool uniform = false);
+  /* Grid (SMs x resident blocks) and threads per block of the single-medium
+   * (uniform) or mixed-media kernel under the current options. */
+  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr);
+  int attr(bool uniform, int *block, int *bps, int *regs);
   cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
 };
 

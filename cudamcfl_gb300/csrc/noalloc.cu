@@ -6,8 +6,8 @@
  * synchronisation of cudaMalloc/cudaFree, or that is only handed device
  * buffers it may read and write.  This entry point serves them: the caller
  * passes the medium and the output images on the device, and the scratch the
- * persistent kernel needs (its ticket counter, its job table and the MWC
- * multiplier table) lives in one file-scope __device__ array of fixed size,
+ * persistent kernel needs (its ticket counter, its job table, the label
+ * records and the MWC multiplier table) lives in one file-scope __device__ array of fixed size,
  * which every GPU that loads the library holds until the process exits.
  *
  * Limits and rules:
@@ -41,8 +41,18 @@ struct NoallocScratch {
   unsigned long long counter;
   unsigned long long pad[31]; /* jobs start 256 bytes in */
   McflJob jobs[MCFL_NOALLOC_MAX_JOBS];
+  float lab[MCFL_MAX_LABELS * MCFL_LAB_FLOATS]; /* label records derived from the caller's table */
   uint32_t mult[32768];
 };
+
+/* Label records from the caller's (mutr, mu_a, g, n) table. */
+__global__ void noalloc_label_records(const float4 *prop, uint32_t n, float *lab) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const float4 q = prop[i];
+    mcfl_label_record(q.x, q.y, q.z, q.w, lab + (size_t)i * MCFL_LAB_FLOATS);
+  }
+}
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocScratch)];
 
@@ -111,6 +121,7 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
     McflJob &j = jobs[i];
     j.labels = d_labels;
     j.prop = d_prop;
+    j.lab = sc->lab;
     j.hx = half_x; j.hy = half_y; j.esp = thickness;
     j.gx = vox_per_cm[0]; j.gy = vox_per_cm[1]; j.gz = vox_per_cm[2];
     j.nx = (uint32_t)nx; j.ny = (uint32_t)ny; j.nz = (uint32_t)nz;
@@ -139,6 +150,9 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
   MCFL_CUDA_TRY(cudaMemsetAsync(d_R, 0, (size_t)n * xy * 8, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(d_T, 0, (size_t)n * xy * 8, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(d_stats, 0, (size_t)n * MCFL_ST_COUNT * 8, s));
+  const uint32_t n_labels = (uint32_t)n_bulks + 2u;
+  noalloc_label_records<<<(n_labels + 127) / 128, 128, 0, s>>>((const float4 *)d_prop, n_labels, sc->lab);
+  MCFL_CUDA_TRY(cudaGetLastError());
   McflLaunch L;
   std::memset(&L, 0, sizeof(L));
   L.jobs = sc->jobs;
@@ -150,17 +164,19 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
   L.uniform_medium = 1;
   L.med.labels = d_labels;
   L.med.prop = d_prop;
+  L.med.lab = sc->lab;
+  L.med.n_labels = n_labels;
   L.med.fhd = nullptr;
   L.med.hx = half_x; L.med.hy = half_y; L.med.esp = thickness;
   L.med.gx = vox_per_cm[0]; L.med.gy = vox_per_cm[1]; L.med.gz = vox_per_cm[2];
   L.med.nx = (uint32_t)nx; L.med.ny = (uint32_t)ny; L.med.total = jobs[0].total;
   L.med.last_label = (uint32_t)n_bulks + 1u;
-  const int block = 256;
+  int block = 0; /* variant 0's own: 256 threads */
   int dev = 0, sms = 0, bps = 0, regs = 0;
   MCFL_CUDA_TRY(cudaGetDevice(&dev));
   MCFL_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  MCFL_CUDA_TRY(math == MCFL_MATH_FAST ? mcfl_attr_transport_fast_uniform(block, &bps, &regs)
-                                       : mcfl_attr_transport_exact_uniform(block, &bps, &regs));
+  MCFL_CUDA_TRY(math == MCFL_MATH_FAST ? mcfl_attr_transport_fast(0, &block, &bps, &regs)
+                                       : mcfl_attr_transport_exact(0, &block, &bps, &regs));
   if (bps < 1) bps = 1;
   MCFL_CUDA_TRY(math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, bps * sms, block, s)
                                        : mcfl_launch_transport_exact(&L, bps * sms, block, s));

@@ -15,6 +15,7 @@
  */
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <functional>
 #include <string>
@@ -38,6 +39,7 @@ unsigned int default_start_weight(const mcfl_medium *m) {
 void fill_medium(McflJob &j, const mcfl_medium *m, bool emission) {
   j.labels = m->labels.as<uint8_t>();
   j.prop = emission ? m->prop_emi.as<float>() : m->prop_exc.as<float>();
+  j.lab = emission ? m->lab_emi.as<float>() : m->lab_exc.as<float>();
   j.hx = m->hx;
   j.hy = m->hy;
   j.esp = m->esp;
@@ -188,16 +190,25 @@ McflLaunch base_launch(mcfl_ctx *c) {
   std::memset(&L, 0, sizeof(L));
   L.mult = c->mult.as<uint32_t>();
   L.step_cap = c->step_cap;
+  L.variant = (uint32_t)c->variant;
   return L;
 }
 
 /* Every job of the launch uses medium m with one photon-hitting-density
  * tally (or none): the medium travels in the kernel parameters. */
-void set_uniform(McflLaunch &L, const mcfl_medium *m, bool emission, unsigned long long *fhd) {
+void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool emission, unsigned long long *fhd) {
   L.uniform_medium = 1;
+  if (c->l2_window && c->l2_max_window) {
+    const size_t bytes = std::min<size_t>(m->labels.bytes, c->l2_max_window);
+    L.l2_base = m->labels.p;
+    L.l2_bytes = bytes;
+    L.l2_hit_ratio = (float)std::min(1.0, (double)c->l2_persist_bytes / (double)bytes);
+  }
   McflMedium &u = L.med;
   u.labels = m->labels.as<uint8_t>();
   u.prop = emission ? m->prop_emi.as<float>() : m->prop_exc.as<float>();
+  u.lab = emission ? m->lab_emi.as<float>() : m->lab_exc.as<float>();
+  u.n_labels = (uint32_t)m->n_bulks + 2u;
   u.fhd = fhd;
   u.hx = m->hx;
   u.hy = m->hy;
@@ -274,8 +285,8 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
 
   unsigned long long *cnt = c->counters.as<unsigned long long>();
-  const int grid = c->grid_for(c->block, nullptr, true);
-  const int block = c->block;
+  int block = 0;
+  const int grid = c->grid_for(true, &block);
   const unsigned long long photons = run->photons;
   const unsigned per_voxel = run->photons_per_voxel;
   auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -298,10 +309,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.n_jobs = 1;
     L.ticket_counter = cnt + 0;
     L.ticket_end = photons;
-    set_uniform(L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
+    set_uniform(c, L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
     REC(record_event(c->ev[0], st));
-    REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
-                                  : mcfl_launch_transport_exact(&L, grid, block, st));
+    REC(launch_fn(c->math)(&L, grid, block, st));
     ++*k;
     REC(record_event(c->ev[1], st));
     if (emission) {
@@ -314,10 +324,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       Lf.jobs = c->jobs.as<McflJob>() + 1;
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
-      set_uniform(Lf, m, true, nullptr);
+      set_uniform(c, Lf, m, true, nullptr);
       REC(record_event(c->ev[2], st));
-      REC(c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&Lf, grid, block, st)
-                                    : mcfl_launch_transport_exact(&Lf, grid, block, st));
+      REC(launch_fn(c->math)(&Lf, grid, block, st));
       ++*k;
       REC(record_event(c->ev[3], st));
     }
@@ -330,7 +339,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                    c->h_jobs, c->h_out, c->stats.p, c->block_counts.p, (const void *)s},
                                   {xy, nv, (unsigned long long)emission, (unsigned long long)fluence, photons,
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
-                                   (unsigned long long)block, c->step_cap});
+                                   (unsigned long long)block, c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
   if (rc != MCFL_OK) return rc;
 
@@ -438,8 +447,8 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     j.photons = runs[i].photons;
     tickets += runs[i].photons;
   }
-  const int grid = c->grid_for(c->block, nullptr, true);
-  const int block = c->block;
+  int block = 0;
+  const int grid = c->grid_for(true, &block);
   float ms = 0.f;
   if (schedule == MCFL_SCHEDULE_BATCHED) {
     auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -454,10 +463,9 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = (uint32_t)n;
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
-      set_uniform(L, m, false, nullptr);
+      set_uniform(c, L, m, false, nullptr);
       if ((e = record_event(c->ev[0], st))) return e;
-      if ((e = c->math == MCFL_MATH_FAST ? mcfl_launch_transport_fast(&L, grid, block, st)
-                                         : mcfl_launch_transport_exact(&L, grid, block, st)))
+      if ((e = launch_fn(c->math)(&L, grid, block, st)))
         return e;
       ++*k;
       if ((e = record_event(c->ev[1], st))) return e;
@@ -466,7 +474,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     const std::string key =
         ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
-                 c->step_cap});
+                 c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
@@ -484,7 +492,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = 1;
       L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
       L.ticket_end = runs[i].photons;
-      set_uniform(L, m, false, nullptr);
+      set_uniform(c, L, m, false, nullptr);
       MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
     }
@@ -597,7 +605,8 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   }
   MCFL_CUDA_TRY(cudaMemcpyAsync(c->jobs.p, c->h_jobs, NL * sizeof(McflJob), cudaMemcpyHostToDevice, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(c->bcnt.p, 0, NL * 8 + 8, s));
-  const int grid = c->grid_for(c->block, nullptr, true);
+  int block = 0;
+  const int grid = c->grid_for(true, &block);
   MCFL_CUDA_TRY(cudaEventRecord(c->ev[2], s));
   for (size_t i = 0; i < NL; ++i) {
     McflLaunch L = base_launch(c);
@@ -605,8 +614,8 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     L.n_jobs = 1;
     L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
     L.ticket_end = run->photons_per_voxel;
-    set_uniform(L, m, true, nullptr);
-    MCFL_CUDA_TRY(c->launch_transport(L, grid, c->block));
+    set_uniform(c, L, m, true, nullptr);
+    MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
     MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulationFl */
   }
   MCFL_CUDA_TRY(cudaEventRecord(c->ev[3], s));
@@ -672,8 +681,10 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   L.n_jobs = 1;
   L.ticket_counter = c->counters.as<unsigned long long>();
   L.ticket_end = run->photons;
-  set_uniform(L, m, false, nullptr);
-  MCFL_CUDA_TRY(c->launch_transport(L, c->grid_for(c->block, nullptr, true), c->block));
+  set_uniform(c, L, m, false, nullptr);
+  int block = 0;
+  const int grid = c->grid_for(true, &block);
+  MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
   std::vector<unsigned long long> r(2 * xy), t(2 * xy);
   MCFL_CUDA_TRY(cudaMemcpyAsync(r.data(), c->R128.p, xy * 16, cudaMemcpyDeviceToHost, s));
   MCFL_CUDA_TRY(cudaMemcpyAsync(t.data(), c->T128.p, xy * 16, cudaMemcpyDeviceToHost, s));

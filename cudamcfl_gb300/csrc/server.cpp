@@ -91,6 +91,7 @@ struct mcfl_server {
   unsigned long long *h_read = nullptr;
   uint64_t tickets_end = 0;
   int grid = 0;
+  int block = 256;
   /* metrics */
   std::vector<double> latencies_ms;
   unsigned long long photons_done = 0, slices = 0, max_inflight = 0, inflight_sum = 0;
@@ -126,6 +127,7 @@ int mcfl_server::upload(Request &r) {
   std::memset(&j, 0, sizeof(j));
   j.labels = m->labels.as<uint8_t>();
   j.prop = m->prop_exc.as<float>();
+  j.lab = m->lab_exc.as<float>();
   j.hx = m->hx; j.hy = m->hy; j.esp = m->esp;
   j.gx = m->gx; j.gy = m->gy; j.gz = m->gz;
   j.nx = (uint32_t)m->nx; j.ny = (uint32_t)m->ny; j.nz = (uint32_t)m->nz; j.total = m->total;
@@ -248,7 +250,7 @@ void mcfl_server::loop() {
     L.mult = ctx->mult.as<uint32_t>();
     L.saved = parked.as<McflSaved>();
     L.step_cap = ctx->step_cap;
-    cudaError_t e = ctx->launch_transport(L, grid, ctx->block);
+    cudaError_t e = ctx->launch_transport(L, grid, block);
     cudaMemcpyAsync(h_read, counter.p, 8, cudaMemcpyDeviceToHost, s);
     for (unsigned i = 0; i < n; ++i) {
       Request &r = *active[h_order[i]];
@@ -315,6 +317,8 @@ void mcfl_server::loop() {
 extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, mcfl_server **out) {
   if (!ctx || !out) return fail(MCFL_E_ARG, "mcfl_server_create: null argument");
   *out = nullptr;
+  if (ctx->math == MCFL_MATH_F64)
+    return fail(MCFL_E_ARG, "mcfl_server_create: the f64 build runs whole launches only (no parked photons)");
   auto *sv = new mcfl_server();
   sv->ctx = ctx;
   size_t free_b = 0, total_b = 0;
@@ -328,8 +332,8 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
     return fail(MCFL_E_RANGE, "max_jobs above 4096");
   }
   sv->active.assign(sv->slots, nullptr);
-  sv->grid = ctx->grid_for(ctx->block);
-  const size_t threads = (size_t)sv->grid * ctx->block;
+  sv->grid = ctx->grid_for(false, &sv->block);
+  const size_t threads = (size_t)sv->grid * sv->block;
   cudaError_t e = sv->slot_jobs.reserve(sv->slots * sizeof(McflJob));
   if (!e) e = sv->order.reserve(sv->slots * 4);
   if (!e) e = sv->counter.reserve(8);

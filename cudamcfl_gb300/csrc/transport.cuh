@@ -35,20 +35,66 @@
  *     step budget per launch lets a server slot new jobs in between slices
  *     while photons in flight are parked in HBM;
  *   - labels are uint8 in HBM (L2-resident: 4 MB for 200x200x100 voxels);
- *     the optical properties of the photon's current label live in registers
- *     and are reloaded (one 16-byte L1 load) only when the label changes;
+ *     each label's transport constants (a 32-byte record: 1/mu_t,
+ *     mu_a/mu_t, 1-g^2, 1-g, 2g, 1+g^2, 1/(2g), n) sit in shared memory when
+ *     the launch has one medium, or in registers for the photon's current
+ *     label (reloaded on a label change) when it mixes media;
  *   - the photon-hitting-density tally is run-length aggregated per thread:
  *     successive passes in the same voxel add up in a register and reach HBM
  *     as one 64-bit atomic;
  *   - per-job weight accounting (absorbed, left at each face, roulette) for
  *     an exact integer energy balance.
  */
+#include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "engine_types.h"
 #include "portable_math.h"
 
+#ifndef MCFL_F64
+#define MCFL_F64 0
+#endif
+
+#if MCFL_F64
+/* Every transport quantity in double, IEEE double functions. */
+typedef double real;
+struct __align__(16) real4 {
+  double x, y, z, w;
+};
+#define MCFL_C(c) (c)
+#define MCFL_LOGF(x) log(x)
+#define MCFL_SINCOSF(x, s, c) sincos((x), (s), (c))
+#define MCFL_COSF(x) cos(x)
+#define MCFL_RSQRTF(x) rsqrt(x)
+#define MCFL_SQRT(x) sqrt(x)
+#define MCFL_SQRT_RN(x) sqrt(x)
+#define MCFL_FABS(x) fabs(x)
+#define MCFL_COPYSIGN(a, b) copysign((a), (b))
+#define MCFL_U2R_RZ(u) ((double)(u))
+#define MCFL_U2R_RN(u) ((double)(u))
+#define MCFL_I2R_RN(i) ((double)(i))
+#define MCFL_R2U_RZ(x) __double2uint_rz(x)
+#define MCFL_R2U_RU(x) __double2uint_ru(x)
+#define MCFL_R2U_RN(x) __double2uint_rn(x)
+#define MCFL_KERNEL_NAME mcfl_transport_f64
+#define MCFL_LAUNCHER mcfl_launch_transport_f64
+#define MCFL_ATTR_FN mcfl_attr_transport_f64
+#else
+typedef float real;
+typedef float4 real4;
+#define MCFL_C(c) (c##f)
+#define MCFL_SQRT(x) sqrtf(x)
+#define MCFL_SQRT_RN(x) __fsqrt_rn(x)
+#define MCFL_FABS(x) fabsf(x)
+#define MCFL_COPYSIGN(a, b) copysignf((a), (b))
+#define MCFL_U2R_RZ(u) __uint2float_rz(u)
+#define MCFL_U2R_RN(u) __uint2float_rn(u)
+#define MCFL_I2R_RN(i) __int2float_rn(i)
+#define MCFL_R2U_RZ(x) __float2uint_rz(x)
+#define MCFL_R2U_RU(x) __float2uint_ru(x)
+#define MCFL_R2U_RN(x) __float2uint_rn(x)
 #if MCFL_EXACT_MATH
 #define MCFL_LOGF(x) mcfl_plogf(x)
 #define MCFL_SINCOSF(x, s, c) mcfl_psincosf((x), (s), (c))
@@ -57,7 +103,6 @@
 #define MCFL_KERNEL_NAME mcfl_transport_exact
 #define MCFL_LAUNCHER mcfl_launch_transport_exact
 #define MCFL_ATTR_FN mcfl_attr_transport_exact
-#define MCFL_ATTR_FN_U mcfl_attr_transport_exact_uniform
 #else
 #define MCFL_LOGF(x) __logf(x)
 #define MCFL_SINCOSF(x, s, c) __sincosf((x), (s), (c))
@@ -66,44 +111,52 @@
 #define MCFL_KERNEL_NAME mcfl_transport_fast
 #define MCFL_LAUNCHER mcfl_launch_transport_fast
 #define MCFL_ATTR_FN mcfl_attr_transport_fast
-#define MCFL_ATTR_FN_U mcfl_attr_transport_fast_uniform
+#endif
 #endif
 
 namespace {
 
-constexpr float kPi = 3.141592654f;        /* CUDAMCFL.h:22 */
+constexpr real kPi = MCFL_C(3.141592654);        /* CUDAMCFL.h:22 */
 constexpr uint32_t kWeightRoulette = 429497u; /* CUDAMCFL.h:33 */
-constexpr float kChance = 0.1f;            /* CUDAMCFL.h:34 */
+constexpr real kChance = MCFL_C(0.1);            /* CUDAMCFL.h:34 */
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kEv = 6; /* event counters kept in shared memory: EXIT_TOP .. CAPPED */
 
 struct Rng {
   uint64_t x;
   uint32_t a;
-  __device__ __forceinline__ float co() {
+  __device__ __forceinline__ real co() {
     x = (uint64_t)(uint32_t)x * a + (x >> 32);
-    return __uint2float_rz((uint32_t)x) * 0x1p-32f;
+    return MCFL_U2R_RZ((uint32_t)x) * MCFL_C(0x1p-32);
   }
-  __device__ __forceinline__ float oc() { return 1.0f - co(); }
+  __device__ __forceinline__ real oc() { return MCFL_C(1.0) - co(); }
 };
 
 struct Photon {
-  float x, y, z, dx, dy, dz;
+  real x, y, z, dx, dy, dz;
   uint32_t weight, label;
 };
 
 /* The current job's medium, held in registers. */
 struct Med {
   const uint8_t *labels;
-  const float4 *prop;
+#if MCFL_F64
+  const float4 *prop; /* (mutr, mu_a, g, n) per label; records are built from it in double */
+#else
+  const float4 *lab; /* label records, two float4 each */
+#endif
   unsigned long long *fhd;
-  float hx, hy, esp, gx, gy, gz;
+  real hx, hy, esp, gx, gy, gz;
   uint32_t nx, ny, total, last;
 };
 
 __device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
   m.labels = (const uint8_t *)__ldg((const unsigned long long *)&J->labels);
+#if MCFL_F64
   m.prop = (const float4 *)__ldg((const unsigned long long *)&J->prop);
+#else
+  m.lab = (const float4 *)__ldg((const unsigned long long *)&J->lab);
+#endif
   m.fhd = __ldg(&J->fhd_on) ? (unsigned long long *)__ldg((const unsigned long long *)&J->fhd) : nullptr;
   m.hx = __ldg(&J->hx);
   m.hy = __ldg(&J->hy);
@@ -117,17 +170,40 @@ __device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
   m.last = __ldg(&J->last_label);
 }
 
-__device__ __forceinline__ float4 load_prop(const Med &m, uint32_t label) { return __ldg(&m.prop[label]); }
+/* The label record: a = (mutr, mu_a*mutr, 1-g^2, 1-g), b = (2g, 1+g^2, 1/(2g), n). */
+struct Rec {
+  real4 a, b;
+};
 
-__device__ __forceinline__ uint32_t voxel_index(const Med &m, float x, float y, float z) {
-  uint32_t i = __float2uint_rz((x + m.hx) * m.gx) +
-               m.nx * (__float2uint_rz((y + m.hy) * m.gy) + m.ny * __float2uint_rz(z * m.gz));
+#if MCFL_F64
+/* The record in double from a (mutr, mu_a, g, n) entry. */
+__device__ __forceinline__ Rec make_rec(float4 q) {
+  const double mutr = q.x, mua = q.y, g = q.z, n = q.w;
+  Rec r;
+  r.a = real4{mutr, mua * mutr, 1.0 - g * g, 1.0 - g};
+  r.b = real4{2.0 * g, 1.0 + g * g, 1.0 / (2.0 * g), n};
+  return r;
+}
+
+__device__ __forceinline__ Rec load_rec(const Med &m, uint32_t label) { return make_rec(__ldg(&m.prop[label])); }
+#else
+__device__ __forceinline__ Rec load_rec(const Med &m, uint32_t label) {
+  Rec r;
+  r.a = __ldg(&m.lab[2 * label]);
+  r.b = __ldg(&m.lab[2 * label + 1]);
+  return r;
+}
+#endif
+
+__device__ __forceinline__ uint32_t voxel_index(const Med &m, real x, real y, real z) {
+  uint32_t i = MCFL_R2U_RZ((x + m.hx) * m.gx) +
+               m.nx * (MCFL_R2U_RZ((y + m.hy) * m.gy) + m.ny * MCFL_R2U_RZ(z * m.gz));
   return i < m.total ? i : m.total - 1u;
 }
 
 __device__ __forceinline__ uint32_t start_label(const Med &m, const Photon &p) {
   if (p.z < m.esp) {
-    if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy) return (uint32_t)m.labels[voxel_index(m, p.x, p.y, p.z)];
+    if (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy) return (uint32_t)m.labels[voxel_index(m, p.x, p.y, p.z)];
     return 1u;
   }
   return m.last;
@@ -165,47 +241,47 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     k_in_run = k - (uint64_t)src_idx * per;
     const uint32_t v = __ldg(&J->src_vox[src_idx]);
     const uint32_t ix = v % m.nx, iy = (v / m.nx) % m.ny, iz = v / (m.nx * m.ny);
-    const float xi = ((float)ix / m.gx) - m.hx;
-    const float yi = ((float)iy / m.gy) - m.hy;
-    const float zi = ((float)iz / m.gz);
-    p.x = xi + (0.999999f / m.gx) * r.oc();
-    p.y = yi + (0.999999f / m.gy) * r.oc();
-    p.z = zi + (0.999999f / m.gz) * r.oc();
+    const real xi = ((real)ix / m.gx) - m.hx;
+    const real yi = ((real)iy / m.gy) - m.hy;
+    const real zi = ((real)iz / m.gz);
+    p.x = xi + (MCFL_C(0.999999) / m.gx) * r.oc();
+    p.y = yi + (MCFL_C(0.999999) / m.gy) * r.oc();
+    p.z = zi + (MCFL_C(0.999999) / m.gz) * r.oc();
     /* The reference evaluates these in double (CUDAMCFLtransport.cu:474-483).
-     * 1 - 2u and 2*PI*u are exact in double, so their float forms round the
-     * same value once and are bit-identical; sqrt(1 - c^2) is taken in single
-     * precision here (the reference rounds a double square root), so no FP64
-     * instruction runs in the transport kernel. */
-    const float costheta = 1.0f - 2.0f * r.oc();
-    const float sintheta = __fsqrt_rn(1.0f - costheta * costheta);
-    const float psi = (2.0f * kPi) * r.oc();
-    const float cospsi = MCFL_COSF(psi);
-    float sinpsi = __fsqrt_rn(1.0f - cospsi * cospsi);
+     * 1 - 2u and 2*PI*u are exact in double, so their single-precision forms
+     * round the same value once and are bit-identical; sqrt(1 - c^2) is taken
+     * in single precision here (the reference rounds a double square root), so
+     * no FP64 instruction runs in the single-precision kernels. */
+    const real costheta = MCFL_C(1.0) - MCFL_C(2.0) * r.oc();
+    const real sintheta = MCFL_SQRT_RN(MCFL_C(1.0) - costheta * costheta);
+    const real psi = (MCFL_C(2.0) * kPi) * r.oc();
+    const real cospsi = MCFL_COSF(psi);
+    real sinpsi = MCFL_SQRT_RN(MCFL_C(1.0) - cospsi * cospsi);
     if (!(psi < kPi)) sinpsi = -sinpsi;
     p.dx = sintheta * cospsi;
     p.dy = sintheta * sinpsi;
     p.dz = costheta;
     p.weight = 0xFFFFFFFFu;
   } else if (kind == MCFL_SRC_WIDEFIELD) {
-    p.x = __ldg(&J->sx) + (r.co() - 0.5f) * __ldg(&J->src_w);
-    p.y = __ldg(&J->sy) + (r.co() - 0.5f) * __ldg(&J->src_h);
+    p.x = __ldg(&J->sx) + (r.co() - MCFL_C(0.5)) * __ldg(&J->src_w);
+    p.y = __ldg(&J->sy) + (r.co() - MCFL_C(0.5)) * __ldg(&J->src_h);
     p.z = __ldg(&J->sz);
-    p.dx = 0.0f;
-    p.dy = 0.0f;
-    p.dz = 1.0f;
+    p.dx = MCFL_C(0.0);
+    p.dy = MCFL_C(0.0);
+    p.dz = MCFL_C(1.0);
     p.weight = __ldg(&J->start_weight);
   } else {
-    const float input_fibre_diameter = 0.03f;
-    const float sample_rad = input_fibre_diameter * __fsqrt_rn(-MCFL_LOGF(r.oc()));
-    const float sample_phi = 2 * kPi * r.oc();
-    float sin_phi, cos_phi;
+    const real input_fibre_diameter = MCFL_C(0.03);
+    const real sample_rad = input_fibre_diameter * MCFL_SQRT_RN(-MCFL_LOGF(r.oc()));
+    const real sample_phi = 2 * kPi * r.oc();
+    real sin_phi, cos_phi;
     MCFL_SINCOSF(sample_phi, &sin_phi, &cos_phi);
     p.x = __ldg(&J->sx) + sample_rad * cos_phi;
     p.y = __ldg(&J->sy) + sample_rad * sin_phi;
     p.z = __ldg(&J->sz);
-    p.dx = 0.0f;
-    p.dy = 0.0f;
-    p.dz = 1.0f;
+    p.dx = MCFL_C(0.0);
+    p.dy = MCFL_C(0.0);
+    p.dz = MCFL_C(1.0);
     p.weight = __ldg(&J->start_weight);
   }
   p.label = start_label(m, p);
@@ -217,20 +293,29 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
   if (__ldg(&J->launch_rng_reuse) && k_in_run < 32768u) r.x = x_at_launch;
 }
 
-__device__ __forceinline__ void spin(Photon &p, float g, Rng &r) {
-  float cost, sint, cosp, sinp, temp;
-  const float tempdir = p.dx;
-  temp = (1.0f - g * g) / (1.0f - g + 2.0f * g * r.co());
-  cost = (1.0f + g * g - temp * temp) / (2.0f * g);
-  if (g == 0.0f) cost = 2.0f * r.co() - 1.0f;
-  sint = sqrtf(1.0f - cost * cost);
+/* Henyey-Greenstein deflection and rotation of the direction
+ * (CUDAMCFLtransport.cu:585-625).  The exact kernel keeps the reference's
+ * expressions, with its per-label subexpressions (1-g^2, 1-g, 2g, 1+g^2)
+ * taken from the label record: the same roundings.  The fast kernel uses
+ * reciprocals and one reciprocal square root for the rotation instead of
+ * divisions: the same physics at fast-math accuracy. */
+__device__ __forceinline__ void spin(Photon &p, const Rec &c, Rng &r) {
+  real cost, sint, cosp, sinp;
+  const real two_g = c.b.x;
+#if MCFL_EXACT_MATH
+  real temp;
+  const real tempdir = p.dx;
+  temp = c.a.z / (c.a.w + two_g * r.co());
+  cost = (c.b.y - temp * temp) / two_g;
+  if (two_g == MCFL_C(0.0)) cost = MCFL_C(2.0) * r.co() - MCFL_C(1.0);
+  sint = MCFL_SQRT(MCFL_C(1.0) - cost * cost);
   /* sin goes to cosp and cos to sinp, as in CUDAMCFLtransport.cu:603 */
-  MCFL_SINCOSF(2.0f * kPi * r.co(), &cosp, &sinp);
-  temp = sqrtf(1.0f - p.dz * p.dz);
-  if (temp == 0.0f) {
+  MCFL_SINCOSF(MCFL_C(2.0) * kPi * r.co(), &cosp, &sinp);
+  temp = MCFL_SQRT(MCFL_C(1.0) - p.dz * p.dz);
+  if (temp == MCFL_C(0.0)) {
     p.dx = sint * cosp;
     p.dy = sint * sinp;
-    p.dz = copysignf(cost, p.dz * cost);
+    p.dz = MCFL_COPYSIGN(cost, p.dz * cost);
   } else {
     p.dx = (sint * (p.dx * p.dz * cosp - p.dy * sinp)) / temp + p.dx * cost;
     p.dy = (sint * (p.dy * p.dz * cosp + tempdir * sinp)) / temp + p.dy * cost;
@@ -240,58 +325,73 @@ __device__ __forceinline__ void spin(Photon &p, float g, Rng &r) {
   p.dx = p.dx * temp;
   p.dy = p.dy * temp;
   p.dz = p.dz * temp;
+#else
+  const real temp = c.a.z / (c.a.w + two_g * r.co());
+  cost = (c.b.y - temp * temp) * c.b.z;
+  if (two_g == MCFL_C(0.0)) cost = MCFL_C(2.0) * r.co() - MCFL_C(1.0);
+  sint = MCFL_SQRT(MCFL_C(1.0) - cost * cost);
+  __sincosf(MCFL_C(2.0) * kPi * r.co(), &cosp, &sinp);
+  const real q = MCFL_C(1.0) - p.dz * p.dz;
+  real dx, dy, dz;
+  if (q > MCFL_C(0.0)) {
+    const real rq = rsqrtf(q); /* 1/sin(theta_old) */
+    const real st = sint * rq;
+    dx = st * (p.dx * p.dz * cosp - p.dy * sinp) + p.dx * cost;
+    dy = st * (p.dy * p.dz * cosp + p.dx * sinp) + p.dy * cost;
+    dz = -sint * cosp * (q * rq) + p.dz * cost;
+  } else {
+    dx = sint * cosp;
+    dy = sint * sinp;
+    dz = MCFL_COPYSIGN(cost, p.dz * cost);
+  }
+  const real nrm = rsqrtf(dx * dx + dy * dy + dz * dz);
+  p.dx = dx * nrm;
+  p.dy = dy * nrm;
+  p.dz = dz * nrm;
+#endif
 }
 
-/* Fresnel reflection / refraction with z as the interface normal.  On
- * transmission the label and the cached properties change. */
-__device__ __forceinline__ void reflect(Photon &p, uint32_t newlb, Rng &r, const Med &m, float4 &pr) {
-  const float n1 = pr.w;
-  const float4 pn = load_prop(m, newlb);
-  const float n2 = pn.w;
-  float rr;
-  const float cos_angle_i = fabsf(p.dz);
-  if (n1 == n2) {
-    p.label = newlb;
-    pr = pn;
-    return;
-  }
+/* Fresnel reflection / refraction with z as the interface normal
+ * (CUDAMCFLtransport.cu:628-700).  Returns true when the photon crosses into
+ * the new label (the caller then changes its label). */
+__device__ __forceinline__ bool reflect(Photon &p, real n1, real n2, Rng &r) {
+  real rr;
+  const real cos_angle_i = MCFL_FABS(p.dz);
+  if (n1 == n2) return true;
   if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
-    p.dz *= -1.0f;
-    return;
+    p.dz *= -MCFL_C(1.0);
+    return false;
   }
-  if (cos_angle_i == 1.0f) {
+  if (cos_angle_i == MCFL_C(1.0)) {
     rr = (n1 - n2) / (n1 + n2);
     if (r.co() <= rr * rr) {
-      p.dz *= -1.0f;
-    } else {
-      p.label = newlb;
-      pr = pn;
+      p.dz *= -MCFL_C(1.0);
+      return false;
     }
-    return;
+    return true;
   }
-  float e = (n1 * n1) / (n2 * n2) * (1.0f - cos_angle_i * cos_angle_i);
-  rr = 2 * sqrtf((1.0f - cos_angle_i * cos_angle_i) * (1.0f - e) * e * cos_angle_i * cos_angle_i);
-  e = e + (cos_angle_i * cos_angle_i) * (1.0f - 2.0f * e);
-  rr = e * ((1.0f - e - rr) / ((1.0f - e + rr) * (e + rr)));
+  real e = (n1 * n1) / (n2 * n2) * (MCFL_C(1.0) - cos_angle_i * cos_angle_i);
+  rr = 2 * MCFL_SQRT((MCFL_C(1.0) - cos_angle_i * cos_angle_i) * (MCFL_C(1.0) - e) * e * cos_angle_i * cos_angle_i);
+  e = e + (cos_angle_i * cos_angle_i) * (MCFL_C(1.0) - MCFL_C(2.0) * e);
+  rr = e * ((MCFL_C(1.0) - e - rr) / ((MCFL_C(1.0) - e + rr) * (e + rr)));
   if (r.co() <= rr) {
-    p.dz *= -1.0f;
-    return;
+    p.dz *= -MCFL_C(1.0);
+    return false;
   }
   rr = n1 / n2;
-  e = rr * rr * (1.0f - cos_angle_i * cos_angle_i);
+  e = rr * rr * (MCFL_C(1.0) - cos_angle_i * cos_angle_i);
   p.dx *= rr;
   p.dy *= rr;
-  p.dz = copysignf(sqrtf(1 - e), p.dz);
-  p.label = newlb;
-  pr = pn;
+  p.dz = MCFL_COPYSIGN(MCFL_SQRT(1 - e), p.dz);
+  return true;
 }
 
 /* Scattering-free voxels: march in half-voxel steps to the next label, then
  * back-project onto the sphere of radius 0.707 voxel around the centre of the
  * voxel reached.  The march is bounded by max_s. */
-__device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, float max_s) {
-  float search_step = 1 / (2 * m.gx);
-  float total_move = 0;
+__device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, real max_s) {
+  real search_step = 1 / (2 * m.gx);
+  real total_move = 0;
   int index = 1;
   const uint32_t old_bulk = p.label;
   uint32_t present_bulk = old_bulk;
@@ -299,7 +399,7 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
     p.x += p.dx * search_step;
     p.y += p.dy * search_step;
     p.z += p.dz * search_step;
-    if (p.z + p.dz * search_step < 0.0f) {
+    if (p.z + p.dz * search_step < MCFL_C(0.0)) {
       present_bulk = 0;
       index = -1;
       search_step = (-p.z) / p.dz;
@@ -307,7 +407,7 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
       present_bulk = m.last;
       index = -1;
       search_step = (m.esp - p.z) / p.dz;
-    } else if (fabsf(p.x + p.dx * search_step) >= m.hx || fabsf(p.y + p.dy * search_step) >= m.hy) {
+    } else if (MCFL_FABS(p.x + p.dx * search_step) >= m.hx || MCFL_FABS(p.y + p.dy * search_step) >= m.hy) {
       present_bulk = 1;
       index = -1;
     } else {
@@ -323,15 +423,15 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
     const uint32_t y_grid = uidx / m.nx;
     const uint32_t x_grid = uidx % m.nx;
     const double half = 1. / (2. * (double)m.gx);
-    const float y_voxel = (float)((double)(__int2float_rn((int)y_grid) / m.gy - m.hy) + half);
-    const float x_voxel = (float)((double)(__int2float_rn((int)x_grid) / m.gx - m.hx) + half);
-    const float z_voxel = (float)((double)(__int2float_rn((int)z_grid) / m.gz) + half);
+    const real y_voxel = (real)((double)(MCFL_I2R_RN((int)y_grid) / m.gy - m.hy) + half);
+    const real x_voxel = (real)((double)(MCFL_I2R_RN((int)x_grid) / m.gx - m.hx) + half);
+    const real z_voxel = (real)((double)(MCFL_I2R_RN((int)z_grid) / m.gz) + half);
     const double rv = 0.707107 * (double)(1 / m.gx);
-    const float r_voxel2 = (float)(rv * rv);
-    const float pow_dx = p.dx * p.dx, pow_dy = p.dy * p.dy, pow_dz = p.dz * p.dz;
-    const float pow_px = p.x * p.x, pow_py = p.y * p.y, pow_pz = p.z * p.z;
-    const float pow_cx = x_voxel * x_voxel, pow_cy = y_voxel * y_voxel, pow_cz = z_voxel * z_voxel;
-    const float disc =
+    const real r_voxel2 = (real)(rv * rv);
+    const real pow_dx = p.dx * p.dx, pow_dy = p.dy * p.dy, pow_dz = p.dz * p.dz;
+    const real pow_px = p.x * p.x, pow_py = p.y * p.y, pow_pz = p.z * p.z;
+    const real pow_cx = x_voxel * x_voxel, pow_cy = y_voxel * y_voxel, pow_cz = z_voxel * z_voxel;
+    const real disc =
         2 * x_voxel * y_voxel * p.dx * p.dy - (pow_cy + pow_cz) * pow_dx - (pow_cx + pow_cz) * pow_dy -
         (pow_cx + pow_cy) * pow_dz - (pow_dy + pow_dz) * pow_px - (pow_dx + pow_dz) * pow_py -
         (pow_dx + pow_dy) * pow_pz + (pow_dx + pow_dy + pow_dz) * r_voxel2 +
@@ -341,13 +441,13 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
             p.y +
         2 * (z_voxel * pow_dx + z_voxel * pow_dy + p.dx * p.dz * p.x + p.dy * p.dz * p.y -
              (x_voxel * p.dx + y_voxel * p.dy) * p.dz) * p.z;
-    const float root = sqrtf(disc);
-    const float lin = x_voxel * p.dx + y_voxel * p.dy + z_voxel * p.dz - p.dx * p.x - p.dy * p.y - p.dz * p.z;
-    const float den = pow_dx + pow_dy + pow_dz;
-    const float back_step1 = -(lin + root) / den;
-    const float back_step2 = -(lin - root) / den;
-    const float npx1 = p.x - p.dx * back_step1, npy1 = p.y - p.dy * back_step1, npz1 = p.z - p.dz * back_step1;
-    const float npx2 = p.x - p.dx * back_step2, npy2 = p.y - p.dy * back_step2, npz2 = p.z - p.dz * back_step2;
+    const real root = MCFL_SQRT(disc);
+    const real lin = x_voxel * p.dx + y_voxel * p.dy + z_voxel * p.dz - p.dx * p.x - p.dy * p.y - p.dz * p.z;
+    const real den = pow_dx + pow_dy + pow_dz;
+    const real back_step1 = -(lin + root) / den;
+    const real back_step2 = -(lin - root) / den;
+    const real npx1 = p.x - p.dx * back_step1, npy1 = p.y - p.dy * back_step1, npz1 = p.z - p.dz * back_step1;
+    const real npx2 = p.x - p.dx * back_step2, npy2 = p.y - p.dy * back_step2, npz2 = p.z - p.dz * back_step2;
     if (((npx1 - x_voxel) * (npx1 - x_voxel) + (npy1 - y_voxel) * (npy1 - y_voxel) +
          (npz1 - z_voxel) * (npz1 - z_voxel)) <
         ((npx2 - x_voxel) * (npx2 - x_voxel) + (npy2 - y_voxel) * (npy2 - y_voxel) +
@@ -373,13 +473,13 @@ __device__ __forceinline__ void add128(unsigned long long *acc, uint32_t w, uint
 
 /* Exit through a face: image tally when the exit point is inside the
  * detector.  top: R (z = 0), else T (z = esp). */
-__device__ __noinline__ void tally_exit(const McflJob *J, float px, float py, uint32_t weight, bool top,
+__device__ __noinline__ void tally_exit(const McflJob *J, real px, real py, uint32_t weight, bool top,
                                         uint32_t src_idx) {
-  const float x0 = __ldg(&J->det_x0), y0 = __ldg(&J->det_y0);
-  const float size_x = __ldg(&J->size_x), size_y = __ldg(&J->size_y);
-  if (!(fabsf(px - x0) < size_x && fabsf(py - y0) < size_y)) return;
-  uint32_t idx = __float2uint_rz((py - y0 + size_y) / __ldg(&J->det_dy)) * __ldg(&J->det_nx) +
-                 __float2uint_rz((px - x0 + size_x) / __ldg(&J->det_dx));
+  const real x0 = __ldg(&J->det_x0), y0 = __ldg(&J->det_y0);
+  const real size_x = __ldg(&J->size_x), size_y = __ldg(&J->size_y);
+  if (!(MCFL_FABS(px - x0) < size_x && MCFL_FABS(py - y0) < size_y)) return;
+  uint32_t idx = MCFL_R2U_RZ((py - y0 + size_y) / __ldg(&J->det_dy)) * __ldg(&J->det_nx) +
+                 MCFL_R2U_RZ((px - x0 + size_x) / __ldg(&J->det_dx));
   const uint32_t xy = __ldg(&J->xy_size);
   if (idx >= xy) idx = xy - 1u;
   if (__ldg(&J->src_kind) == MCFL_SRC_VOXELS) {
@@ -397,13 +497,28 @@ __device__ __noinline__ void tally_exit(const McflJob *J, float px, float py, ui
 /* One warp-synchronous persistent loop per thread; see the file comment.
  * kUniform: the medium comes from the launch parameters (constant bank)
  * instead of per-lane registers loaded from the job. */
-template <bool kUniform>
-__global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLaunch L) {
-  extern __shared__ unsigned long long s_ev[]; /* kEv x blockDim.x */
+template <bool kUniform, int kThreads, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
+  /* shared memory: kEv x blockDim.x event counters, then (uniform medium)
+   * the label records of the medium */
+  extern __shared__ unsigned long long s_ev[];
+  real4 *s_lab = reinterpret_cast<real4 *>(s_ev + kEv * blockDim.x);
   const unsigned lane = threadIdx.x & 31u;
   const unsigned tib = threadIdx.x;
   const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (int e = 0; e < kEv; ++e) s_ev[e * blockDim.x + tib] = 0ull;
+  if (kUniform) {
+#if MCFL_F64
+    for (uint32_t i = tib; i < L.med.n_labels; i += blockDim.x) {
+      const Rec q = make_rec(__ldg((const float4 *)L.med.prop + i));
+      s_lab[2 * i] = q.a;
+      s_lab[2 * i + 1] = q.b;
+    }
+#else
+    for (uint32_t i = tib; i < 2 * L.med.n_labels; i += blockDim.x) s_lab[i] = __ldg((const float4 *)L.med.lab + i);
+#endif
+    __syncthreads();
+  }
 
   const uint64_t ticket_end = L.ticket_end_dev ? *L.ticket_end_dev : L.ticket_end;
   bool alive = false, exhausted = false;
@@ -412,7 +527,11 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
   Med m = {};
   if (kUniform) {
     m.labels = L.med.labels;
+#if MCFL_F64
     m.prop = (const float4 *)L.med.prop;
+#else
+    m.lab = (const float4 *)L.med.lab;
+#endif
     m.fhd = L.med.fhd;
     m.hx = L.med.hx;
     m.hy = L.med.hy;
@@ -425,7 +544,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
     m.total = L.med.total;
     m.last = L.med.last_label;
   }
-  float4 pr = make_float4(0.f, 0.f, 0.f, 0.f);
+  Rec rc = {}; /* general kernel: the record of the photon's label, in registers */
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
   uint32_t f_idx = 0xffffffffu;
@@ -467,7 +586,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
       pst = sv.steps;
       pst0 = pst;
       src_idx = sv.src_idx;
-      pr = load_prop(m, p.label);
+      if (!kUniform) rc = load_rec(m, p.label);
       alive = true;
     }
   }
@@ -496,7 +615,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
             }
             k = t - __ldg((const unsigned long long *)&J->ticket_begin);
             launch_photon(J, m, k, L.mult, p, r, src_idx);
-            pr = load_prop(m, p.label);
+            if (!kUniform) rc = load_rec(m, p.label);
             pst = 0;
             pst0 = 0;
             alive = true;
@@ -512,13 +631,14 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
 
     /* ---- one transport pass (MCd3D loop body) ---- */
     ++pst;
-    float s;
+    real s;
     uint32_t new_bulk;
     uint32_t vi = 0xffffffffu; /* voxel of the end point, when looked up */
-    if (pr.x != FLT_MAX) {
-      s = -MCFL_LOGF(r.oc()) * pr.x;
+    const Rec c = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
+    if (c.a.x != FLT_MAX) {
+      s = -MCFL_LOGF(r.oc()) * c.a.x;
       new_bulk = p.label;
-      if (p.z + s * p.dz < 0.0f) {
+      if (p.z + s * p.dz < MCFL_C(0.0)) {
         new_bulk = 0;
         s = (-p.z) / p.dz;
       }
@@ -530,7 +650,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
       p.y += p.dy * s;
       p.z += p.dz * s;
       if (new_bulk != 0u && new_bulk != m.last) {
-        if (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp) {
+        if (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp) {
           vi = voxel_index(m, p.x, p.y, p.z);
           new_bulk = (uint32_t)m.labels[vi];
         } else {
@@ -538,13 +658,19 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
         }
       }
     } else {
-      s = 100.0f;
+      s = MCFL_C(100.0);
       new_bulk = move_to_first_boundary(p, m, s);
     }
-    if (new_bulk != p.label) reflect(p, new_bulk, r, m, pr);
+    if (new_bulk != p.label) {
+      const Rec cn = kUniform ? Rec{s_lab[2 * new_bulk], s_lab[2 * new_bulk + 1]} : load_rec(m, new_bulk);
+      if (reflect(p, c.b.w, cn.b.w, r)) {
+        p.label = new_bulk;
+        if (!kUniform) rc = cn;
+      }
+    }
     /* the hitting density is tallied at the end point, where the label was
      * looked up unless the pass was clipped to a face */
-    if (m.fhd && (vi != 0xffffffffu || (fabsf(p.x) < m.hx && fabsf(p.y) < m.hy && p.z < m.esp))) {
+    if (m.fhd && (vi != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp))) {
       const uint32_t fi = vi != 0xffffffffu ? vi : voxel_index(m, p.x, p.y, p.z);
       if (fi != f_idx) {
         if (f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
@@ -558,10 +684,11 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
       tally_exit(J, p.x, p.y, p.weight, top, src_idx);
       ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
       p.weight = 0u;
-      s = 0.0f;
+      s = MCFL_C(0.0);
     }
-    if (s > 0.0f) {
-      const uint32_t w = __float2uint_ru(pr.y * pr.x * __uint2float_rn(p.weight));
+    if (s > MCFL_C(0.0)) {
+      const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
+      const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
       if (w > 0u) {
         p.weight -= w;
         absorbed += w;
@@ -569,7 +696,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
         ev_add(MCFL_ST_W0_LOSS, p.weight);
         p.weight = 0u;
       }
-      spin(p, pr.z, r);
+      spin(p, c2, r);
     }
     /* PhotonSurvive */
     if (p.weight <= kWeightRoulette) {
@@ -577,7 +704,7 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
         alive = false;
       } else if (r.co() < kChance) {
         const uint32_t w0 = p.weight;
-        p.weight = __float2uint_rn(__uint2float_rn(p.weight) / kChance);
+        p.weight = MCFL_R2U_RN(MCFL_U2R_RN(p.weight) / kChance);
         ev_add(MCFL_ST_R_GAIN, (unsigned long long)(p.weight - w0));
       } else {
         ev_add(MCFL_ST_R_LOSS, p.weight);
@@ -599,7 +726,8 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
     McflSaved sv;
     sv.alive = alive ? 1u : 0u;
     if (alive) {
-      sv.x = p.x; sv.y = p.y; sv.z = p.z; sv.dx = p.dx; sv.dy = p.dy; sv.dz = p.dz;
+      sv.x = (float)p.x; sv.y = (float)p.y; sv.z = (float)p.z;
+      sv.dx = (float)p.dx; sv.dy = (float)p.dy; sv.dz = (float)p.dz;
       sv.weight = p.weight;
       sv.label = p.label;
       sv.rng_x = r.x;
@@ -615,31 +743,83 @@ __global__ void __launch_bounds__(256, kUniform ? 4 : 3) MCFL_KERNEL_NAME(McflLa
   if (kUniform && m.fhd && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 }
 
+/* dynamic shared memory of a launch */
+static size_t smem_bytes(int block, bool uniform) {
+  return (size_t)kEv * block * sizeof(unsigned long long) +
+         (uniform ? (size_t)MCFL_MAX_LABELS * MCFL_LAB_FLOATS * sizeof(real) : 0);
+}
+
+/* Occupancy variants of the single-medium kernel (threads per block, blocks
+ * per SM the register budget is cut for): 0 = 256 x 4 (64 registers),
+ * 1 = 256 x 5 (48), 2 = 128 x 9 (56).  The autotuner picks one per
+ * workload; the mixed-media kernel has one variant, 256 x 3. */
+#define MCFL_VARIANTS(X) X(0, 256, 4) X(1, 256, 5) X(2, 128, 9)
+
+/* Launches variant L->variant (or the mixed-media kernel); with
+ * L->l2_bytes > 0 the launch carries a persisting-L2 access window (a launch
+ * attribute, so it is recorded with the kernel node when captured). */
 extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, cudaStream_t stream) {
-  const size_t smem = (size_t)kEv * block * sizeof(unsigned long long);
-  if (L->uniform_medium)
-    MCFL_KERNEL_NAME<true><<<grid, block, smem, stream>>>(*L);
-  else
-    MCFL_KERNEL_NAME<false><<<grid, block, smem, stream>>>(*L);
-  return cudaGetLastError();
+  if (L->uniform_medium && L->med.n_labels > MCFL_MAX_LABELS) return cudaErrorInvalidValue;
+#if MCFL_F64
+  if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
+#endif
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof(cfg));
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)block);
+  cfg.dynamicSmemBytes = smem_bytes(block, L->uniform_medium != 0);
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  if (L->l2_bytes) {
+    memset(attr, 0, sizeof(attr));
+    attr[0].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[0].val.accessPolicyWindow.base_ptr = const_cast<void *>(L->l2_base);
+    attr[0].val.accessPolicyWindow.num_bytes = (size_t)L->l2_bytes;
+    attr[0].val.accessPolicyWindow.hitRatio = L->l2_hit_ratio;
+    attr[0].val.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+    attr[0].val.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+  }
+  if (!L->uniform_medium) {
+    if (block > 256) return cudaErrorInvalidValue;
+    return cudaLaunchKernelEx(&cfg, MCFL_KERNEL_NAME<false, 256, 3>, *L);
+  }
+  switch (L->variant) {
+#define MCFL_CASE(v, t, b)                                   \
+  case v:                                                    \
+    if (block > t) return cudaErrorInvalidValue;             \
+    return cudaLaunchKernelEx(&cfg, MCFL_KERNEL_NAME<true, t, b>, *L);
+    MCFL_VARIANTS(MCFL_CASE)
+#undef MCFL_CASE
+  default:
+    return cudaErrorInvalidValue;
+  }
 }
 
-/* Occupancy of the general (per-lane medium) instantiation, the larger of
- * the two, so one grid size serves both. */
-extern "C" cudaError_t MCFL_ATTR_FN(int block, int *blocks_per_sm, int *regs) {
+/* Resident blocks per SM and registers of a variant (variant < 0: the
+ * mixed-media kernel) at *block threads per block; *block <= 0 or above the
+ * variant's bound is replaced by the bound. */
+extern "C" cudaError_t MCFL_ATTR_FN(int variant, int *block, int *blocks_per_sm, int *regs) {
   cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME<false>);
+  cudaError_t e = cudaErrorInvalidValue;
+  int t = 0;
+  const void *fn = nullptr;
+  if (variant < 0) {
+    t = 256;
+    fn = (const void *)MCFL_KERNEL_NAME<false, 256, 3>;
+  }
+#define MCFL_ATTR_CASE(v, tt, b)                        \
+  if (variant == v) {                                   \
+    t = tt;                                             \
+    fn = (const void *)MCFL_KERNEL_NAME<true, tt, b>;   \
+  }
+  MCFL_VARIANTS(MCFL_ATTR_CASE)
+#undef MCFL_ATTR_CASE
+  if (!fn) return e;
+  e = cudaFuncGetAttributes(&a, fn);
   if (e != cudaSuccess) return e;
   if (regs) *regs = a.numRegs;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME<false>, block,
-                                                       (size_t)kEv * block * sizeof(unsigned long long));
-}
-
-extern "C" cudaError_t MCFL_ATTR_FN_U(int block, int *blocks_per_sm, int *regs) {
-  cudaFuncAttributes a;
-  cudaError_t e = cudaFuncGetAttributes(&a, MCFL_KERNEL_NAME<true>);
-  if (e != cudaSuccess) return e;
-  if (regs) *regs = a.numRegs;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, MCFL_KERNEL_NAME<true>, block,
-                                                       (size_t)kEv * block * sizeof(unsigned long long));
+  if (*block <= 0 || *block > t) *block = t;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, *block, smem_bytes(*block, variant >= 0));
 }

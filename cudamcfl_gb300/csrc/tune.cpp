@@ -1,0 +1,66 @@
+/*
+ * Launch-shape autotuner (mcfl_autotune).
+ *
+ * The reference fixes its launch shape at compile time (128 blocks of 256
+ * threads, CUDAMCFL.h:18-20).  The persistent kernel here is compiled in
+ * several occupancy variants of the single-medium kernel (threads per block x
+ * the blocks per SM the register budget is cut for) and can put a persisting
+ * L2 access window on the labels and tallies.  Which combination is fastest
+ * depends on the medium (how often photons change label, how deep they go)
+ * and on the emission/excitation mix, so the tuner times every combination on
+ * a sample of the caller's own run and keeps the fastest in the context.
+ */
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "mcfl_internal.h"
+
+using namespace mcfl;
+
+extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run,
+                             unsigned long long sample_photons, int *variant_out, double *rate_out) {
+  if (!c || !m || !run) return fail(MCFL_E_ARG, "mcfl_autotune: null argument");
+  if (sample_photons == 0) return fail(MCFL_E_ARG, "mcfl_autotune: sample_photons must be positive");
+  mcfl_run_desc r = *run;
+  r.photons = std::min<unsigned long long>(sample_photons, run->photons ? run->photons : sample_photons);
+  if (run->photons_per_voxel) {
+    /* keep the run's emission/excitation proportion */
+    const double f = (double)r.photons / (double)(run->photons ? run->photons : r.photons);
+    r.photons_per_voxel = (unsigned)std::max(1.0, (double)run->photons_per_voxel * f);
+  }
+  const int old_variant = c->variant, old_l2 = c->l2_window;
+  int best_v = old_variant, best_l2 = old_l2;
+  double best = -1.0;
+  for (int v = 0; v < MCFL_N_VARIANTS; ++v) {
+    for (int l2 = 0; l2 < 2; ++l2) {
+      c->variant = v;
+      c->l2_window = l2;
+      double rate = 0.0;
+      for (int rep = 0; rep < 3; ++rep) { /* the first run records the graph */
+        mcfl_run_out o;
+        std::memset(&o, 0, sizeof(o));
+        const int rc = mcfl_run(c, m, &r, &o);
+        if (rc != MCFL_OK) {
+          c->variant = old_variant;
+          c->l2_window = old_l2;
+          return rc;
+        }
+        const double ms = (double)o.ms_exc + (double)o.ms_fl;
+        const double photons = (double)o.stats_exc[0] + (double)o.stats_fl[0];
+        if (rep > 0 && ms > 0) rate = std::max(rate, photons / (ms * 1e-3));
+      }
+      if (rate > best) {
+        best = rate;
+        best_v = v;
+        best_l2 = l2;
+      }
+    }
+  }
+  c->variant = best_v;
+  c->l2_window = best_l2;
+  if (variant_out) *variant_out = best_v;
+  if (rate_out) *rate_out = best;
+  return MCFL_OK;
+}

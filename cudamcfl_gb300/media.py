@@ -17,6 +17,8 @@ Workloads (all cm):
             mus U(50, 150), g U(0.8, 0.95), n=1.4; 5-20 spheres
             (r 0.1-0.5) and cylinders (r 0.05-0.3, random axis) carrying a
             U(0, 1) fluorophore map; quantum yield U(0.05, 0.2).
+  config5   the large precision-study medium: 512 x 512 x 256 voxels of
+            0.01 cm, mu_s' = 20/cm, fp32 fluorophore map, wide-field source.
   raster    the 16 x 16 grid of beam positions over the top face used for the
             batched sweep, with log-uniform budgets.
 Emission scattering equals excitation scattering: the reference's emission
@@ -59,26 +61,48 @@ def _grid_centres(shape, voxel_cm):
     return z[:, None, None], y[None, :, None], x[None, None, :]
 
 
+def _box(shape, voxel_cm, lo, hi):
+    """Index slices of the voxels whose centres may lie in [lo, hi] (cm,
+    x/y/z), widened by one voxel; the mask is then evaluated on that box only,
+    with the same centre coordinates as on the whole grid."""
+    nz, ny, nx = shape
+    sl = []
+    for n, d, a, b, off in ((nz, voxel_cm[2], lo[2], hi[2], 0.0), (ny, voxel_cm[1], lo[1], hi[1], ny * voxel_cm[1] / 2),
+                            (nx, voxel_cm[0], lo[0], hi[0], nx * voxel_cm[0] / 2)):
+        i0 = int(np.floor((a + off) / d)) - 1
+        i1 = int(np.ceil((b + off) / d)) + 1
+        sl.append(slice(min(max(i0, 0), n), min(max(i1, 0), n)))
+    return tuple(sl)
+
+
+def _centres_in(shape, voxel_cm, box):
+    z, y, x = _grid_centres(shape, voxel_cm)
+    return z[box[0], :, :], y[:, box[1], :], x[:, :, box[2]]
+
+
 def add_sphere(labels, voxel_cm, centre, r, label, fmap=None, fval=None):
-    z, y, x = _grid_centres(labels.shape, voxel_cm)
+    box = _box(labels.shape, voxel_cm, [c - r for c in centre], [c + r for c in centre])
+    z, y, x = _centres_in(labels.shape, voxel_cm, box)
     m = (x - centre[0]) ** 2 + (y - centre[1]) ** 2 + (z - centre[2]) ** 2 <= r * r
-    labels[m] = label
+    labels[box][m] = label
     if fmap is not None:
-        fmap[m] = fval if np.isscalar(fval) else fval[m]
+        fmap[box][m] = fval if np.isscalar(fval) else fval[box][m]
     return int(m.sum())
 
 
 def add_cylinder(labels, voxel_cm, point, axis, r, half_len, label, fmap=None, fval=None):
-    z, y, x = _grid_centres(labels.shape, voxel_cm)
     a = np.asarray(axis, dtype=np.float64)
     a = a / np.linalg.norm(a)
+    ext = [abs(a[i]) * half_len + r for i in range(3)]
+    box = _box(labels.shape, voxel_cm, [point[i] - ext[i] for i in range(3)], [point[i] + ext[i] for i in range(3)])
+    z, y, x = _centres_in(labels.shape, voxel_cm, box)
     px, py, pz = x - point[0], y - point[1], z - point[2]
     t = px * a[0] + py * a[1] + pz * a[2]
     d2 = px * px + py * py + pz * pz - t * t
     m = (d2 <= r * r) & (np.abs(t) <= half_len)
-    labels[m] = label
+    labels[box][m] = label
     if fmap is not None:
-        fmap[m] = fval if np.isscalar(fval) else fval[m]
+        fmap[box][m] = fval if np.isscalar(fval) else fval[box][m]
     return int(m.sum())
 
 
@@ -131,6 +155,53 @@ def config2(seed: int = 2, n_labels: int = 8) -> SyntheticMedium:
             shapes.append(("cylinder", label, r, nvx))
     det = Detector(0.0, 0.0, 0.04, 0.04, 100, 100)
     return SyntheticMedium(lab, bulks, vox, fmap, det, (0.0, 0.0, 0.0), {"inclusions": shapes})
+
+
+def config5(seed: int = 5, shape=(256, 512, 512), voxel: float = 0.01, n_labels: int = 8,
+            musp: float = 20.0) -> SyntheticMedium:
+    """The large precision-study medium: (nz, ny, nx) = 256 x 512 x 512
+    voxels of 0.01 cm (5.12 x 5.12 x 2.56 cm) with a fp32 U(0, 1) fluorophore
+    map (268 MB), reduced scattering mu_s' = mu_s (1 - g) = 20/cm in every
+    label, mua U(0.02, 0.5), g U(0.8, 0.95), n = 1.4, 5-20 spheres and
+    cylinders as in config2; a uniform wide-field source covers the top face
+    and the R/T images are 256 x 256 pixels over the same area.
+    config5(shape=(64, 128, 128), voxel=0.04) is the same medium at a quarter
+    of the resolution (the size a CPU oracle finishes)."""
+    rng = np.random.default_rng(seed)
+    nz, ny, nx = shape
+    vox = (voxel, voxel, voxel)
+    lab = np.ones((nz, ny, nx), dtype=np.uint8)
+    fmap = np.zeros((nz, ny, nx), dtype=np.float32)
+    mua = rng.uniform(0.02, 0.5, n_labels)
+    g = rng.uniform(0.8, 0.95, n_labels)
+    mus = musp / (1.0 - g)
+    qy = rng.uniform(0.05, 0.2, n_labels)
+    fl_abs = rng.uniform(0.01, 0.1, n_labels)
+    fl_emi = rng.uniform(0.005, 0.05, n_labels)
+    bulks = [outer_bulk(1.0)]
+    for i in range(n_labels):
+        fluorescent = i > 0
+        bulks.append(bulk_from_mci_columns(1.4, mua[i], mus[i], 1.0 if fluorescent else 0.0,
+                                           fl_abs[i] if fluorescent else 0.0, fl_emi[i] if fluorescent else 0.0,
+                                           qy[i] if fluorescent else 0.0, g[i]))
+    bulks.append(outer_bulk(1.0))
+    hx, hy, depth = nx * voxel / 2, ny * voxel / 2, nz * voxel
+    fval = rng.random(size=lab.shape, dtype=np.float32)
+    shapes = []
+    for _ in range(int(rng.integers(5, 21))):
+        label = int(rng.integers(2, n_labels + 1))
+        c = (rng.uniform(-hx + 0.5, hx - 0.5), rng.uniform(-hy + 0.5, hy - 0.5), rng.uniform(0.3, depth - 0.3))
+        if rng.uniform() < 0.5:
+            r = rng.uniform(0.1, 0.5)
+            shapes.append(("sphere", label, r, add_sphere(lab, vox, c, r, label, fmap, fval)))
+        else:
+            r = rng.uniform(0.05, 0.3)
+            ax = rng.normal(size=3)
+            shapes.append(("cylinder", label, r,
+                           add_cylinder(lab, vox, c, ax, r, rng.uniform(0.3, 1.5), label, fmap, fval)))
+    det = Detector(0.0, 0.0, 2 * hx / 256, 2 * hy / 256, 256, 256)
+    return SyntheticMedium(lab, bulks, vox, fmap, det, (0.0, 0.0, 0.0),
+                           {"inclusions": shapes, "widefield": (2 * hx, 2 * hy), "musp": musp})
 
 
 def raster_sources(n: int = 16, extent: float = 4.0, seed: int = 3, lo: float = 1e6, hi: float = 5e7,

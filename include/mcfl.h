@@ -183,7 +183,8 @@ typedef struct mcfl_medium mcfl_medium;
 /* Kernel numerics. */
 enum {
   MCFL_MATH_EXACT = 0, /* IEEE single precision, bit-identical to the CPU oracle */
-  MCFL_MATH_FAST = 1   /* hardware SFU intrinsics (the reference's GPU numerics) */
+  MCFL_MATH_FAST = 1,  /* hardware SFU intrinsics (the reference's GPU numerics) */
+  MCFL_MATH_F64 = 2    /* the same kernel in double precision: states the single-precision error */
 };
 
 /* Source kinds. */
@@ -263,9 +264,12 @@ int mcfl_create(int device, mcfl_ctx **ctx);
 void mcfl_destroy(mcfl_ctx *ctx);
 const char *mcfl_last_error(void);
 
-/* Options: "math" (MCFL_MATH_*), "block" (threads per block), "blocks_per_sm"
- * (0 = occupancy maximum), "step_cap" (passes per photon), "l2_window"
- * (1: persisting L2 access window on the labels and tallies). */
+/* Options: "math" (MCFL_MATH_*), "block" (threads per block, at most the
+ * variant's bound), "variant" (occupancy variant of the single-medium kernel:
+ * 0 = 256 threads x 4 blocks per SM, 1 = 256 x 5, 2 = 128 x 9),
+ * "blocks_per_sm" (0 = occupancy maximum), "step_cap" (passes per photon),
+ * "l2_window" (1: persisting L2 access window on the labels and tallies).
+ * The launch shape of the reference is fixed (CUDAMCFL.h:18-20). */
 int mcfl_set_option(mcfl_ctx *ctx, const char *key, long long value);
 long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
 
@@ -281,6 +285,13 @@ size_t mcfl_medium_bytes(const mcfl_medium *medium);
 
 /* Builds the medium of a parsed .mci simulation (bulk method 2). */
 int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_medium **medium);
+
+/* Times every kernel variant with and without the L2 window on a sample of
+ * `run` (sample_photons excitation photons, photons_per_voxel scaled by the
+ * same fraction) and keeps the fastest in ctx's options; returns the chosen
+ * variant and its photons/s.  No counterpart in the reference. */
+int mcfl_autotune(mcfl_ctx *ctx, const mcfl_medium *medium, const struct mcfl_run_desc *run,
+                  unsigned long long sample_photons, int *variant, double *photons_per_s);
 
 /* Runs one two-phase simulation and copies the requested results. */
 int mcfl_run(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *run, mcfl_run_out *out);
@@ -374,7 +385,8 @@ void mcfl_server_destroy(mcfl_server *server);
  * for labels 0..n_bulks+1) and the outputs on the device (d_R, d_T: n images
  * of det.nx + det.nx*det.ny 64-bit sums; d_stats: n x MCFL_NSTATS), which
  * the call clears.  Every run must give start_weight.  The kernel's scratch
- * (ticket counter, job table, multiplier table, about 145 KB) is one static
+ * (ticket counter, job table, label records, multiplier table, about
+ * 153 KB) is one static
  * device array that every GPU loading the library holds until exit; the
  * first call on a device sets it up (make it before any stream capture);
  * calls share it, so calls that overlap on the GPU race.  Asynchronous on

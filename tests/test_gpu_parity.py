@@ -57,9 +57,37 @@ def test_exact_kernel_launch_shape_does_not_change_tallies(gpu_ctx, oracle, tabl
             gpu_ctx.set_option("block", block)
             gpu_ctx.set_option("blocks_per_sm", bps)
             _compare(gpu_ctx.run(med, case.run_desc(5, 6)), ref)
+        gpu_ctx.set_option("block", 256)
+        gpu_ctx.set_option("blocks_per_sm", 0)
+        # every occupancy variant, with and without the persisting-L2 window
+        for variant, bound in ((0, 256), (1, 256), (2, 128)):
+            for l2 in (0, 1):
+                gpu_ctx.set_option("variant", variant)
+                gpu_ctx.set_option("l2_window", l2)
+                assert gpu_ctx.get_option("launch_block") == bound
+                _compare(gpu_ctx.run(med, case.run_desc(5, 6)), ref)
     finally:
         gpu_ctx.set_option("block", 256)
         gpu_ctx.set_option("blocks_per_sm", 0)
+        gpu_ctx.set_option("variant", 0)
+        gpu_ctx.set_option("l2_window", 0)
+
+
+@pytest.mark.gpu
+def test_autotune_keeps_a_variant_and_tallies(gpu_ctx, oracle, table32768):
+    """The autotuner leaves one of the variants in the context; the run after
+    it still equals the oracle bit for bit."""
+    case = cases.sphere(photons=20000, per_voxel=200)
+    ref = oracle.run_photon(case.oracle_sim(), table32768, 8, 9, libm=False)
+    med = case.engine_medium(gpu_ctx)
+    try:
+        variant, rate = gpu_ctx.autotune(med, case.run_desc(8, 9), sample_photons=20000)
+        assert variant in (0, 1, 2) and rate > 0
+        assert gpu_ctx.get_option("variant") == variant
+        _compare(gpu_ctx.run(med, case.run_desc(8, 9)), ref)
+    finally:
+        gpu_ctx.set_option("variant", 0)
+        gpu_ctx.set_option("l2_window", 0)
 
 
 @pytest.mark.gpu

@@ -103,10 +103,17 @@ class Detector(ctypes.Structure):
                 ("nx", ctypes.c_int), ("ny", ctypes.c_int)]
 
 
+class TimeDetectors(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("x0", ctypes.c_float), ("y0", ctypes.c_float),
+                ("sep_x", ctypes.c_float), ("sep_y", ctypes.c_float), ("radius", ctypes.c_float),
+                ("face", ctypes.c_int), ("bins", ctypes.c_int), ("max_fs", ctypes.c_ulonglong)]
+
+
 class RunDesc(ctypes.Structure):
     _fields_ = [("photons", ctypes.c_ulonglong), ("photons_per_voxel", ctypes.c_uint), ("fluence", ctypes.c_int),
                 ("seed_exc", ctypes.c_ulonglong), ("seed_fl", ctypes.c_ulonglong), ("start_weight", ctypes.c_uint),
-                ("source", Source), ("det", Detector), ("launch_rng_reuse", ctypes.c_int)]
+                ("source", Source), ("det", Detector), ("launch_rng_reuse", ctypes.c_int),
+                ("tdet", TimeDetectors)]
 
 
 _u64p = ctypes.POINTER(ctypes.c_ulonglong)
@@ -118,7 +125,8 @@ class RunOut(ctypes.Structure):
                 ("flR", _f64p), ("flT", _f64p), ("flR128", _u64p), ("flT128", _u64p),
                 ("stats_exc", ctypes.c_ulonglong * NSTATS), ("stats_fl", ctypes.c_ulonglong * NSTATS),
                 ("photons_fl", ctypes.c_ulonglong), ("fl_voxels", ctypes.c_longlong),
-                ("energy_exc", ctypes.c_double * 4), ("ms_exc", ctypes.c_float), ("ms_fl", ctypes.c_float)]
+                ("energy_exc", ctypes.c_double * 4), ("ms_exc", ctypes.c_float), ("ms_fl", ctypes.c_float),
+                ("time_xyt", _u64p)]
 
 
 SCHEDULE_BATCHED = 0
@@ -180,6 +188,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mcfl_DoOneSimulationFl": (ctypes.c_ulonglong, [P(Simulation), ctypes.c_ulonglong, _u64p, _u64p]),
         "mcfl_Write_Simulation_Results": (ctypes.c_int, [P(Simulation), _u64p, _u64p, ctypes.c_double]),
         "mcfl_write_phd": (ctypes.c_int, [P(Simulation), _f64p]),
+        "mcfl_write_time": (ctypes.c_int, [P(Simulation), _u64p]),
         "mcfl_write_fl_images": (ctypes.c_int, [P(Simulation), _f64p, _f64p]),
         "mcfl_run_mci": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_ulonglong]),
         "mcfl_batch_run": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_int, ctypes.c_int, P(RunOut),
@@ -255,6 +264,7 @@ class RunResult:
     energy_exc: tuple
     ms_exc: float
     ms_fl: float
+    time_xyt: np.ndarray | None = None  # uint64 (bins, ny, nx) raw time-resolved tallies
 
 
 class Medium:
@@ -402,6 +412,9 @@ class Context:
             if emission128:
                 alloc("flR128", 2 * xy, np.uint64, u64ptr)
                 alloc("flT128", 2 * xy, np.uint64, u64ptr)
+        td = rd.tdet
+        if td.nx > 0:
+            alloc("time_xyt", td.nx * td.ny * td.bins, np.uint64, u64ptr)
         rc = load().mcfl_run(self.handle, medium.handle, ctypes.byref(rd), ctypes.byref(out))
         check(rc)
         g = keep.get
@@ -411,7 +424,8 @@ class Context:
             flT128=None if g("flT128") is None else g("flT128").reshape(xy, 2),
             stats_exc=dict(zip(STAT_NAMES, list(out.stats_exc))), stats_fl=dict(zip(STAT_NAMES, list(out.stats_fl))),
             photons_fl=int(out.photons_fl), fl_voxels=int(out.fl_voxels), energy_exc=tuple(out.energy_exc),
-            ms_exc=float(out.ms_exc), ms_fl=float(out.ms_fl))
+            ms_exc=float(out.ms_exc), ms_fl=float(out.ms_fl),
+            time_xyt=None if g("time_xyt") is None else g("time_xyt").reshape(td.bins, td.ny, td.nx))
 
 
 def _medium_desc(labels, bulks, voxel_cm, fluor_map=None):
@@ -548,7 +562,9 @@ class Server:
 
 def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per_voxel: int = 0, fluence: int = 0,
              seed_exc: int = 1, seed_fl: int = 2, start_weight: int = 0, kind: int = SOURCE_GAUSS_BEAM,
-             width: float = 0.0, height: float = 0.0, launch_rng_reuse: int = 0) -> RunDesc:
+             width: float = 0.0, height: float = 0.0, launch_rng_reuse: int = 0, tdet: tuple | None = None) -> RunDesc:
+    """tdet: time-resolved detectors (x0, y0, nx, ny, sep_x, sep_y, radius,
+    face, bins, max_fs), or None."""
     r = RunDesc()
     r.photons = photons
     r.photons_per_voxel = photons_per_voxel
@@ -559,6 +575,9 @@ def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per
     r.source = Source(kind, *[float(v) for v in source], width, height)
     r.det = det
     r.launch_rng_reuse = launch_rng_reuse
+    if tdet:
+        x0, y0, tnx, tny, sx, sy, rad, face, bins, tmax = tdet
+        r.tdet = TimeDetectors(tnx, tny, x0, y0, sx, sy, rad, face, bins, tmax)
     return r
 
 

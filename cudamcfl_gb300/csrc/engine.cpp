@@ -64,17 +64,17 @@ void DevBuf::release() {
 using namespace mcfl;
 
 
-int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs) {
+int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time) {
   *blk = block;
   *bps = 0;
   *regs = 0;
-  const int v = uniform ? variant : -1;
+  const int v = uniform ? (time ? 3 : variant) : (time ? -2 : -1);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
-int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out) {
+int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out, bool time) {
   int blk = 0, bps = 0, regs = 0;
-  if (attr(uniform, &blk, &bps, &regs) != 0 || bps <= 0) bps = 1;
+  if (attr(uniform, &blk, &bps, &regs, time) != 0 || bps <= 0) bps = 1;
   if (blocks_per_sm > 0 && blocks_per_sm < bps) bps = blocks_per_sm;
   if (bps_out) *bps_out = bps;
   if (block_out) *block_out = blk;

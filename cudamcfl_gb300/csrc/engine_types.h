@@ -62,7 +62,7 @@ typedef struct MCFL_ALIGN(16) McflJob {
   uint32_t per_voxel;      /* MCFL_SRC_VOXELS: photons per voxel */
   uint32_t fhd_on;
   uint32_t launch_rng_reuse; /* 1: photons 0..32767 of a run (of each voxel) restart their stream after launch */
-  uint32_t pad0;
+  uint32_t time_on;          /* 1: time-resolved detectors (the launch must run a time-of-flight kernel) */
   /* detector (R at z = 0, T at z = esp) */
   float det_x0, det_y0, det_dx, det_dy, size_x, size_y;
   uint32_t det_nx, xy_size;
@@ -71,6 +71,14 @@ typedef struct MCFL_ALIGN(16) McflJob {
   unsigned long long *R128, *T128; /* (lo, hi) sums of weight x src_q, MCFL_SRC_VOXELS */
   unsigned long long *fhd;         /* photon hitting density, when fhd_on */
   unsigned long long *stats;       /* MCFL_ST_COUNT counters */
+  /* time-resolved detectors: tnx x tny discs of radius tdet_r at (tpos_x[i],
+   * tpos_y[j]) on face tdet_face (0: z = 0, 1: z = esp); tbins bins over
+   * [0, tmax) fs; time_xyt[i + tnx*(j + tny*bin)] */
+  const float *tpos_x, *tpos_y;
+  unsigned long long *time_xyt;
+  uint64_t tmax;
+  float tdet_r;
+  uint32_t tnx, tny, tbins, tdet_face, pad1;
   /* photons */
   uint64_t key;          /* stream family key */
   uint64_t rng_offset;   /* stream index of the job's photon 0 */
@@ -124,6 +132,8 @@ typedef struct McflLaunch {
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
   uint32_t uniform_medium; /* 1: every job uses med (and fhd_on agrees with med.fhd) */
   uint32_t variant;        /* occupancy variant of the single-medium kernel */
+  uint32_t time_on;        /* 1: carry the time of flight (some job has time-resolved detectors) */
+  uint32_t pad2;
   float l2_hit_ratio;      /* host side: persisting-L2 window over [l2_base, +l2_bytes) when l2_bytes > 0 */
   const void *l2_base;
   unsigned long long l2_bytes;

@@ -90,6 +90,9 @@ int run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
 
 /* mci.cpp */
 void simulation_geometry(const mcfl_simulation *sim, float *half_x, float *half_y, float *esp, float *g);
+/* Detector-array positions of time-resolved detectors, as the reference
+ * computes them (CUDAMCFLmain.cu:94-100, single precision). */
+void time_positions(const mcfl_time_detectors &td, float *px, float *py);
 
 } // namespace mcfl
 
@@ -116,6 +119,7 @@ struct mcfl_ctx {
   mcfl::DevBuf saved;      /* parked photons of budgeted launches */
   /* run workspace */
   mcfl::DevBuf R, T, fhd, R128, T128, stats, vox, q, block_counts, outd;
+  mcfl::DevBuf tpos, tarr; /* time-resolved detector positions and tallies */
   /* pinned staging for job tables and results read back after a launch */
   McflJob *h_jobs = nullptr;
   size_t h_jobs_cap = 0;
@@ -141,8 +145,8 @@ struct mcfl_ctx {
 
   /* Grid (SMs x resident blocks) and threads per block of the single-medium
    * (uniform) or mixed-media kernel under the current options. */
-  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr);
-  int attr(bool uniform, int *block, int *bps, int *regs);
+  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr, bool time = false);
+  int attr(bool uniform, int *block, int *bps, int *regs, bool time = false);
   cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
 };
 

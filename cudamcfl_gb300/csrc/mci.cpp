@@ -459,6 +459,58 @@ extern "C" int mcfl_Write_Simulation_Results(const mcfl_simulation *sim, const u
   return write_image(out_path(sim, "_Refl.dat"), sim->det.nx, sim->det.ny, nullptr, Rd_xy, scale2);
 }
 
+namespace mcfl {
+
+void time_positions(const mcfl_time_detectors &td, float *px, float *py) {
+  for (int xi = 0; xi < td.nx; xi++) px[xi] = xi * td.sep_x - ((td.nx - 1) * td.sep_x) / 2 + td.x0;
+  for (int yi = 0; yi < td.ny; yi++) py[yi] = yi * td.sep_y - ((td.ny - 1) * td.sep_y) / 2 + td.y0;
+}
+
+} // namespace mcfl
+
+namespace {
+
+mcfl_time_detectors time_detectors_of(const mcfl_simulation *sim) {
+  mcfl_time_detectors td;
+  std::memset(&td, 0, sizeof(td));
+  if (sim->do_temp_sim != 1) return td;
+  td.nx = (int)sim->det.x_temp_numdets;
+  td.ny = (int)sim->det.y_temp_numdets;
+  td.x0 = sim->det.x0_temp_det;
+  td.y0 = sim->det.y0_temp_det;
+  td.sep_x = sim->det.x_temp_sepdets;
+  td.sep_y = sim->det.y_temp_sepdets;
+  td.radius = sim->det.temp_det_r;
+  td.face = (int)sim->det.temp_rort;
+  td.bins = (int)sim->det.temp_bins;
+  td.max_fs = (unsigned long long)sim->det.max_temp;
+  return td;
+}
+
+} // namespace
+
+extern "C" int mcfl_write_time(const mcfl_simulation *sim, const unsigned long long *time_xyt) {
+  if (!sim || !time_xyt) return fail(MCFL_E_ARG, "mcfl_write_time: null argument");
+  const mcfl_time_detectors td = time_detectors_of(sim);
+  if (td.nx <= 0 || td.ny <= 0 || td.bins <= 0) return fail(MCFL_E_ARG, "mcfl_write_time: no time-resolved detectors");
+  std::vector<float> px((size_t)td.nx), py((size_t)td.ny);
+  mcfl::time_positions(td, px.data(), py.data());
+  const double scale1 = (double)0xFFFFFFFF * (double)sim->number_of_photons;
+  const std::string p = out_path(sim, "_time.dat");
+  FILE *f = fopen(p.c_str(), "w");
+  if (!f) return fail(MCFL_E_IO, "cannot write " + p);
+  fprintf(f, "#x y timebins[numbins]\n");
+  for (int ix = 0; ix < td.nx; ix++)
+    for (int iy = 0; iy < td.ny; iy++) {
+      fprintf(f, "%f %f ", px[ix], py[iy]);
+      for (int it = 0; it < td.bins; it++)
+        fprintf(f, " %E ", (double)time_xyt[ix + (size_t)td.nx * (iy + (size_t)it * td.ny)] / scale1);
+      fprintf(f, " \n ");
+    }
+  fclose(f);
+  return MCFL_OK;
+}
+
 extern "C" int mcfl_write_phd(const mcfl_simulation *sim, const double *fhd) {
   if (!sim || !fhd) return fail(MCFL_E_ARG, "mcfl_write_phd: null argument");
   const std::string p = out_path(sim, "_PHD-Ascii.dat");
@@ -521,6 +573,7 @@ extern "C" int mcfl_run_desc_from_simulation(const mcfl_simulation *sim, unsigne
   run->det.nx = sim->det.nx;
   run->det.ny = sim->det.ny;
   run->launch_rng_reuse = 1; /* the reference's statistics, quirk included */
+  run->tdet = time_detectors_of(sim);
   return MCFL_OK;
 }
 
@@ -601,6 +654,7 @@ extern "C" int mcfl_run_mci(const char *mci_path, unsigned long long seed) {
   const size_t nv = (size_t)sim->num_x * sim->num_y * sim->num_z;
   std::vector<unsigned long long> Rd(xy), Tt(xy);
   std::vector<double> phd(nv), flR(xy), flT(xy);
+  std::vector<unsigned long long> tim;
   mcfl_run_desc run;
   mcfl_run_out out;
   std::memset(&out, 0, sizeof(out));
@@ -611,10 +665,15 @@ extern "C" int mcfl_run_mci(const char *mci_path, unsigned long long seed) {
     out.phd = sim->fhd_activated ? phd.data() : nullptr;
     out.flR = flR.data();
     out.flT = flT.data();
+    if (run.tdet.nx > 0) {
+      tim.assign((size_t)run.tdet.nx * run.tdet.ny * run.tdet.bins, 0ull);
+      out.time_xyt = tim.data();
+    }
     const auto t0 = std::chrono::steady_clock::now();
     rc = mcfl_run(c, m, &run, &out);
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (rc == MCFL_OK) rc = mcfl_Write_Simulation_Results(sim, Rd.data(), Tt.data(), secs);
+    if (rc == MCFL_OK && !tim.empty()) rc = mcfl_write_time(sim, tim.data());
   }
   if (rc == MCFL_OK && sim->fhd_activated == 1) rc = mcfl_write_phd(sim, phd.data());
   if (rc == MCFL_OK && sim->do_fl_sim != 0) rc = mcfl_write_fl_images(sim, flR.data(), flT.data());

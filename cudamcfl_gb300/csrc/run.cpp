@@ -84,6 +84,14 @@ int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run)
   if (run->photons == 0) return fail(MCFL_E_ARG, "zero photons");
   if (run->source.kind != MCFL_SOURCE_GAUSS_BEAM && run->source.kind != MCFL_SOURCE_WIDEFIELD)
     return fail(MCFL_E_ARG, "unknown source kind");
+  const mcfl_time_detectors &td = run->tdet;
+  if (td.nx != 0) {
+    if (td.nx < 0 || td.ny <= 0 || td.bins <= 0 || td.max_fs == 0 || (td.face != 0 && td.face != 1) ||
+        !(td.radius > 0))
+      return fail(MCFL_E_ARG, "bad time-resolved detectors");
+    if ((unsigned long long)td.nx * (unsigned long long)td.ny * (unsigned long long)td.bins >= (1ull << 31))
+      return fail(MCFL_E_RANGE, "time-resolved tally too large");
+  }
   return MCFL_OK;
 }
 
@@ -253,6 +261,16 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
   const size_t nout = 2 * MCFL_ST_COUNT + 4;
   MCFL_CUDA_TRY(ensure_pinned(c, 2, nout));
+  const mcfl_time_detectors &td = run->tdet;
+  const bool timed = td.nx > 0;
+  const size_t tsize = timed ? (size_t)td.nx * td.ny * td.bins : 0;
+  if (timed) {
+    MCFL_CUDA_TRY(c->tpos.reserve((size_t)(td.nx + td.ny) * 4));
+    MCFL_CUDA_TRY(c->tarr.reserve(tsize * 8));
+    std::vector<float> pos((size_t)(td.nx + td.ny));
+    time_positions(td, pos.data(), pos.data() + td.nx);
+    MCFL_CUDA_TRY(cudaMemcpyAsync(c->tpos.p, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice, s));
+  }
 
   McflJob *jobs = c->h_jobs;
   std::memset(jobs, 0, 2 * sizeof(McflJob));
@@ -268,6 +286,18 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   je.key = mcfl_stream_key(run->seed_exc, 0);
   je.photons = run->photons;
   je.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
+  if (timed) {
+    je.time_on = 1;
+    je.tpos_x = c->tpos.as<float>();
+    je.tpos_y = c->tpos.as<float>() + td.nx;
+    je.time_xyt = c->tarr.as<unsigned long long>();
+    je.tmax = td.max_fs;
+    je.tdet_r = td.radius;
+    je.tnx = (uint32_t)td.nx;
+    je.tny = (uint32_t)td.ny;
+    je.tbins = (uint32_t)td.bins;
+    je.tdet_face = (uint32_t)td.face;
+  }
   if (emission) {
     McflJob &jf = jobs[1];
     fill_medium(jf, m, true);
@@ -285,8 +315,10 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
 
   unsigned long long *cnt = c->counters.as<unsigned long long>();
-  int block = 0;
+  int block = 0, block_exc = 0;
   const int grid = c->grid_for(true, &block);
+  const int grid_exc = timed ? c->grid_for(true, &block_exc, nullptr, true) : grid;
+  if (!timed) block_exc = block;
   const unsigned long long photons = run->photons;
   const unsigned per_voxel = run->photons_per_voxel;
   auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -299,6 +331,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     REC(cudaMemsetAsync(c->stats.p, 0, 2 * MCFL_ST_COUNT * 8, st));
     REC(cudaMemsetAsync(c->counters.p, 0, 16 * 8, st));
     if (fluence) REC(cudaMemsetAsync(c->fhd.p, 0, nv * 8, st));
+    if (timed) REC(cudaMemsetAsync(c->tarr.p, 0, tsize * 8, st));
     if (emission) {
       REC(cudaMemsetAsync(c->R128.p, 0, xy * 16, st));
       REC(cudaMemsetAsync(c->T128.p, 0, xy * 16, st));
@@ -310,8 +343,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.ticket_counter = cnt + 0;
     L.ticket_end = photons;
     set_uniform(c, L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
+    L.time_on = timed ? 1u : 0u;
     REC(record_event(c->ev[0], st));
-    REC(launch_fn(c->math)(&L, grid, block, st));
+    REC(launch_fn(c->math)(&L, grid_exc, block_exc, st));
     ++*k;
     REC(record_event(c->ev[1], st));
     if (emission) {
@@ -321,6 +355,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                     cnt + 2, c->jobs.as<McflJob>() + 1, cnt + 3, st));
       *k += 3;
       McflLaunch Lf = L;
+      Lf.time_on = 0;
       Lf.jobs = c->jobs.as<McflJob>() + 1;
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
@@ -336,10 +371,13 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     return cudaSuccess;
   };
   const std::string key = ptr_key({m, c->R.p, c->T.p, c->fhd.p, c->R128.p, c->T128.p, c->vox.p, c->q.p, c->jobs.p,
-                                   c->h_jobs, c->h_out, c->stats.p, c->block_counts.p, (const void *)s},
+                                   c->h_jobs, c->h_out, c->stats.p, c->block_counts.p, (const void *)s,
+                                   timed ? c->tarr.p : nullptr},
                                   {xy, nv, (unsigned long long)emission, (unsigned long long)fluence, photons,
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
-                                   (unsigned long long)block, c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window});
+                                   (unsigned long long)block, c->step_cap, (unsigned long long)c->variant,
+                                   (unsigned long long)c->l2_window, tsize, (unsigned long long)grid_exc,
+                                   (unsigned long long)block_exc});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
   if (rc != MCFL_OK) return rc;
 
@@ -377,6 +415,8 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       MCFL_CUDA_TRY(cudaMemcpyAsync(out->flR128, c->R128.p, xy * 16, cudaMemcpyDeviceToHost, s));
     if (emission && out->flT128)
       MCFL_CUDA_TRY(cudaMemcpyAsync(out->flT128, c->T128.p, xy * 16, cudaMemcpyDeviceToHost, s));
+    if (timed && out->time_xyt)
+      MCFL_CUDA_TRY(cudaMemcpyAsync(out->time_xyt, c->tarr.p, tsize * 8, cudaMemcpyDeviceToHost, s));
   }
   MCFL_CUDA_TRY(cudaStreamSynchronize(s));
   const unsigned long long *st = c->h_out;
@@ -414,8 +454,8 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   for (int i = 0; i < n; ++i) {
     int rc = check_run(c, m, &runs[i]);
     if (rc) return rc;
-    if (runs[i].photons_per_voxel || runs[i].fluence)
-      return fail(MCFL_E_ARG, "mcfl_batch_run: excitation images only (no fluence, no emission)");
+    if (runs[i].photons_per_voxel || runs[i].fluence || runs[i].tdet.nx)
+      return fail(MCFL_E_ARG, "mcfl_batch_run: excitation images only (no fluence, emission or time detectors)");
     const mcfl_detector &d = runs[i].det;
     if (d.nx != det.nx || d.ny != det.ny) return fail(MCFL_E_ARG, "mcfl_batch_run: detectors must share a size");
   }

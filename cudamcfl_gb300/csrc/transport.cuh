@@ -135,7 +135,19 @@ struct Rng {
 struct Photon {
   real x, y, z, dx, dy, dz;
   uint32_t weight, label;
+  uint64_t tof; /* time of flight [fs], time-of-flight kernels only */
 };
+
+/* Time-of-flight increment (unsigned long)(v / c) of a path of optical
+ * length v [cm] (CUDAMCFLtransport.cu:316,725,832,840; c = 2.99792e-5 cm/fs,
+ * CUDAMCFL.h:29), converted with saturation (a negative value adds 0). */
+#if MCFL_F64
+__device__ __forceinline__ uint64_t tof_fs(double v) { return __double2ull_rz(v / 2.99792E-5); }
+#elif MCFL_EXACT_MATH
+__device__ __forceinline__ uint64_t tof_fs(float v) { return __double2ull_rz((double)v / 2.99792E-5); }
+#else
+__device__ __forceinline__ uint64_t tof_fs(float v) { return __float2ull_rz(v * 33356.4609375f); }
+#endif
 
 /* The current job's medium, held in registers. */
 struct Med {
@@ -285,6 +297,7 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     p.weight = __ldg(&J->start_weight);
   }
   p.label = start_label(m, p);
+  p.tof = 0;
   /* The reference's first photon on each of its 32768 threads draws its first
    * passes from the stream state its launch started from, because
    * LaunchPhoton_Global does not store the advanced state
@@ -389,6 +402,7 @@ __device__ __forceinline__ bool reflect(Photon &p, real n1, real n2, Rng &r) {
 /* Scattering-free voxels: march in half-voxel steps to the next label, then
  * back-project onto the sphere of radius 0.707 voxel around the centre of the
  * voxel reached.  The march is bounded by max_s. */
+template <bool kTime>
 __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med &m, real max_s) {
   real search_step = 1 / (2 * m.gx);
   real total_move = 0;
@@ -399,6 +413,7 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
     p.x += p.dx * search_step;
     p.y += p.dy * search_step;
     p.z += p.dz * search_step;
+    if (kTime) p.tof += tof_fs(search_step);
     if (p.z + p.dz * search_step < MCFL_C(0.0)) {
       present_bulk = 0;
       index = -1;
@@ -453,8 +468,10 @@ __device__ __forceinline__ uint32_t move_to_first_boundary(Photon &p, const Med 
         ((npx2 - x_voxel) * (npx2 - x_voxel) + (npy2 - y_voxel) * (npy2 - y_voxel) +
          (npz2 - z_voxel) * (npz2 - z_voxel))) {
       p.x = npx1; p.y = npy1; p.z = npz1;
+      if (kTime) p.tof -= tof_fs(back_step1);
     } else {
       p.x = npx2; p.y = npy2; p.z = npz2;
+      if (kTime) p.tof -= tof_fs(back_step2);
     }
   }
   return present_bulk;
@@ -492,12 +509,43 @@ __device__ __noinline__ void tally_exit(const McflJob *J, real px, real py, uint
   }
 }
 
+/* Time-resolved detectors at an exit (CUDAMCFLtransport.cu:379-390,406-417):
+ * when the exit face is the array's and the time of flight is below the
+ * range, every disc that contains the exit point gets the weight in the
+ * photon's time bin (a bin that rounds onto the end of the range is the last
+ * one). */
+__device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint32_t weight, uint64_t tof, bool top) {
+  if (!__ldg(&J->time_on) || __ldg(&J->tdet_face) != (top ? 0u : 1u)) return;
+  const uint64_t tmax = __ldg((const unsigned long long *)&J->tmax);
+  if (!(tof < tmax)) return;
+  const uint32_t nx = __ldg(&J->tnx), ny = __ldg(&J->tny), bins = __ldg(&J->tbins);
+  const float *tx = (const float *)__ldg((const unsigned long long *)&J->tpos_x);
+  const float *ty = (const float *)__ldg((const unsigned long long *)&J->tpos_y);
+  unsigned long long *hist = (unsigned long long *)__ldg((const unsigned long long *)&J->time_xyt);
+  const real r = __ldg(&J->tdet_r);
+#if MCFL_F64
+  uint32_t bin = __double2uint_rz(((double)tof / (double)tmax) * (double)bins);
+#elif MCFL_EXACT_MATH
+  uint32_t bin = __float2uint_rz((__ull2float_rn(tof) / __ull2float_rn(tmax)) * __uint2float_rn(bins));
+#else
+  uint32_t bin = __float2uint_rz(__fdividef(__ull2float_rn(tof), __ull2float_rn(tmax)) * __uint2float_rn(bins));
+#endif
+  if (bin >= bins) bin = bins - 1u;
+  for (uint32_t i = 0; i < nx; ++i) {
+    const real dx = px - (real)__ldg(&tx[i]);
+    for (uint32_t j = 0; j < ny; ++j) {
+      const real dy = py - (real)__ldg(&ty[j]);
+      if (dx * dx + dy * dy < r * r) atomicAdd(&hist[i + (size_t)nx * (j + (size_t)ny * bin)], (unsigned long long)weight);
+    }
+  }
+}
+
 } // namespace
 
 /* One warp-synchronous persistent loop per thread; see the file comment.
  * kUniform: the medium comes from the launch parameters (constant bank)
  * instead of per-lane registers loaded from the job. */
-template <bool kUniform, int kThreads, int kMinBlocks>
+template <bool kUniform, bool kTime, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   /* shared memory: kEv x blockDim.x event counters, then (uniform medium)
    * the label records of the medium */
@@ -649,6 +697,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       p.x += p.dx * s;
       p.y += p.dy * s;
       p.z += p.dz * s;
+      if (kTime) p.tof += tof_fs(s * c.b.w);
       if (new_bulk != 0u && new_bulk != m.last) {
         if (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp) {
           vi = voxel_index(m, p.x, p.y, p.z);
@@ -659,7 +708,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       }
     } else {
       s = MCFL_C(100.0);
-      new_bulk = move_to_first_boundary(p, m, s);
+      new_bulk = move_to_first_boundary<kTime>(p, m, s);
     }
     if (new_bulk != p.label) {
       const Rec cn = kUniform ? Rec{s_lab[2 * new_bulk], s_lab[2 * new_bulk + 1]} : load_rec(m, new_bulk);
@@ -682,6 +731,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (p.label == 0u || p.label == m.last) {
       const bool top = p.label == 0u;
       tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+      if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
       ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
       p.weight = 0u;
       s = MCFL_C(0.0);
@@ -749,13 +799,27 @@ static size_t smem_bytes(int block, bool uniform) {
          (uniform ? (size_t)MCFL_MAX_LABELS * MCFL_LAB_FLOATS * sizeof(real) : 0);
 }
 
-/* Occupancy variants of the single-medium kernel (threads per block, blocks
- * per SM the register budget is cut for): 0 = 256 x 4 (64 registers),
- * 1 = 256 x 5 (48), 2 = 128 x 9 (56).  The autotuner picks one per
- * workload; the mixed-media kernel has one variant, 256 x 3. */
-#define MCFL_VARIANTS(X) X(0, 256, 4) X(1, 256, 5) X(2, 128, 9)
+/* Kernel variants.  Single medium (occupancy variants: threads per block x
+ * the blocks per SM the register budget is cut for): 0 = 256 x 4,
+ * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner; 3 = 256 x 3 carrying
+ * the time of flight.  Mixed media: -1 = 256 x 3, -2 = 256 x 2 with the time
+ * of flight. */
+typedef void (*TransportKernel)(McflLaunch);
 
-/* Launches variant L->variant (or the mixed-media kernel); with
+static TransportKernel kernel_of(int variant, int *threads) {
+  switch (variant) {
+  case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, 256, 2>;
+  case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, 256, 3>;
+  case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, 256, 4>;
+  case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, 256, 5>;
+  case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, 128, 9>;
+  case 3: *threads = 256; return MCFL_KERNEL_NAME<true, true, 256, 3>;
+  default: *threads = 0; return nullptr;
+  }
+}
+
+/* Launches the kernel the launch asks for (single medium: L->variant, or
+ * variant 3 when it carries the time of flight; mixed media: -1 or -2); with
  * L->l2_bytes > 0 the launch carries a persisting-L2 access window (a launch
  * attribute, so it is recorded with the kernel node when captured). */
 extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, cudaStream_t stream) {
@@ -763,6 +827,11 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
 #if MCFL_F64
   if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
 #endif
+  if (L->max_iters && L->time_on) return cudaErrorNotSupported; /* parked photons carry no time of flight */
+  const int v = L->uniform_medium ? (L->time_on ? 3 : (int)L->variant) : (L->time_on ? -2 : -1);
+  int t = 0;
+  const TransportKernel fn = kernel_of(v, &t);
+  if (!fn || block > t) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3((unsigned)grid);
@@ -781,45 +850,21 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
     cfg.attrs = attr;
     cfg.numAttrs = 1;
   }
-  if (!L->uniform_medium) {
-    if (block > 256) return cudaErrorInvalidValue;
-    return cudaLaunchKernelEx(&cfg, MCFL_KERNEL_NAME<false, 256, 3>, *L);
-  }
-  switch (L->variant) {
-#define MCFL_CASE(v, t, b)                                   \
-  case v:                                                    \
-    if (block > t) return cudaErrorInvalidValue;             \
-    return cudaLaunchKernelEx(&cfg, MCFL_KERNEL_NAME<true, t, b>, *L);
-    MCFL_VARIANTS(MCFL_CASE)
-#undef MCFL_CASE
-  default:
-    return cudaErrorInvalidValue;
-  }
+  return cudaLaunchKernelEx(&cfg, fn, *L);
 }
 
-/* Resident blocks per SM and registers of a variant (variant < 0: the
- * mixed-media kernel) at *block threads per block; *block <= 0 or above the
- * variant's bound is replaced by the bound. */
+/* Resident blocks per SM and registers of a kernel variant (see kernel_of)
+ * at *block threads per block; *block <= 0 or above the variant's bound is
+ * replaced by the bound. */
 extern "C" cudaError_t MCFL_ATTR_FN(int variant, int *block, int *blocks_per_sm, int *regs) {
-  cudaFuncAttributes a;
-  cudaError_t e = cudaErrorInvalidValue;
   int t = 0;
-  const void *fn = nullptr;
-  if (variant < 0) {
-    t = 256;
-    fn = (const void *)MCFL_KERNEL_NAME<false, 256, 3>;
-  }
-#define MCFL_ATTR_CASE(v, tt, b)                        \
-  if (variant == v) {                                   \
-    t = tt;                                             \
-    fn = (const void *)MCFL_KERNEL_NAME<true, tt, b>;   \
-  }
-  MCFL_VARIANTS(MCFL_ATTR_CASE)
-#undef MCFL_ATTR_CASE
-  if (!fn) return e;
-  e = cudaFuncGetAttributes(&a, fn);
+  const TransportKernel fn = kernel_of(variant, &t);
+  if (!fn) return cudaErrorInvalidValue;
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, (const void *)fn);
   if (e != cudaSuccess) return e;
   if (regs) *regs = a.numRegs;
   if (*block <= 0 || *block > t) *block = t;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, *block, smem_bytes(*block, variant >= 0));
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void *)fn, *block,
+                                                       smem_bytes(*block, variant >= 0));
 }

@@ -160,6 +160,11 @@ unsigned long long mcfl_DoOneSimulationFl(const mcfl_simulation *simulation, uns
 int mcfl_Write_Simulation_Results(const mcfl_simulation *sim, const unsigned long long *Rd_xy,
                                   const unsigned long long *Tt_xy, double simulation_time_s);
 
+/* The time-resolved file of Write_Simulation_Results, CUDAMCFLio.cu:168-187
+ * (<out>_time.dat): per detector its position and its bins divided by
+ * (2^32-1) number_of_photons.  time_xyt: raw tallies as mcfl_run_out. */
+int mcfl_write_time(const mcfl_simulation *sim, const unsigned long long *time_xyt);
+
 /* The PHD dump of CUDAMCFLmain.cu:368-392 (<out>_PHD-Ascii.dat). */
 int mcfl_write_phd(const mcfl_simulation *sim, const double *fhd);
 
@@ -216,6 +221,25 @@ typedef struct mcfl_detector {
   int nx, ny;
 } mcfl_detector;
 
+/* Time-resolved detectors (the reference's temporal simulation, det.*temp*
+ * of CUDAMCFL.h, .mci lines of CUDAMCFLio.cu:374-422, tallies of
+ * CUDAMCFLtransport.cu:379-390,406-417): an nx x ny array of discs of radius
+ * `radius`, centred on (x0, y0) with separations sep_x, sep_y (detector i at
+ * x = i sep_x - (nx - 1) sep_x / 2 + x0), on the entry face (face 0, z = 0) or
+ * the exit face (face 1).  A photon leaving through that face inside a disc
+ * adds its weight to the disc's bin of its time of flight, `bins` bins over
+ * [0, max_fs) femtoseconds; every disc that contains the exit point counts
+ * it.  Excitation phase only.  nx = 0: off. */
+typedef struct mcfl_time_detectors {
+  int nx, ny;
+  float x0, y0;
+  float sep_x, sep_y;
+  float radius;
+  int face;
+  int bins;
+  unsigned long long max_fs;
+} mcfl_time_detectors;
+
 /* One two-phase run: excitation from a source, optionally the photon
  * hitting density, optionally the emission phase (photons_per_voxel photons
  * from every voxel whose label has albedof < 1 and whose weight
@@ -237,6 +261,7 @@ typedef struct mcfl_run_desc {
    * where 32768 of every voxel's photons are first photons).  0: independent
    * numbers (default of the engine API; the .mci path sets 1). */
   int launch_rng_reuse;
+  mcfl_time_detectors tdet; /* mcfl_run only; zero: none */
 } mcfl_run_desc;
 
 #define MCFL_NSTATS 9
@@ -257,6 +282,8 @@ typedef struct mcfl_run_out {
   long long fl_voxels;               /* emitting voxels */
   double energy_exc[4];              /* R_all, T_all, absorbed, residual as fractions of the launched weight */
   float ms_exc, ms_fl;               /* GPU time of the two transport launches */
+  unsigned long long *time_xyt;      /* raw time-resolved tallies (tdet.nx*tdet.ny*tdet.bins), index
+                                        ix + nx*(iy + ny*bin), weights of 2^-32 photon */
 } mcfl_run_out;
 
 /* Context on one GPU (device < 0: current device). */
@@ -386,7 +413,7 @@ void mcfl_server_destroy(mcfl_server *server);
  * of det.nx + det.nx*det.ny 64-bit sums; d_stats: n x MCFL_NSTATS), which
  * the call clears.  Every run must give start_weight.  The kernel's scratch
  * (ticket counter, job table, label records, multiplier table, about
- * 153 KB) is one static
+ * 159 KB) is one static
  * device array that every GPU loading the library holds until exit; the
  * first call on a device sets it up (make it before any stream capture);
  * calls share it, so calls that overlap on the GPU race.  Asynchronous on

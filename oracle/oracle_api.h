@@ -36,6 +36,10 @@ typedef struct oracle_result {
    * gained by roulette, killed by a zero weight drop */
   unsigned long long balance[6];
   unsigned long long steps_exc, steps_fl;
+  /* time-resolved detectors of the excitation phase (when enabled): raw
+   * weights per detector and time bin, index ix + nx*(iy + ny*bin) */
+  unsigned long long *time_xyt;
+  long time_size;
 } oracle_result;
 
 /* Parsed method-2 simulation (the fields of SimulationStruct that the
@@ -73,6 +77,19 @@ typedef struct oracle_sim {
   long max_fl_voxels;     /* refstream only: stop after this many emitting voxels (0: all) */
   int launch_rng_reuse;   /* photon only: photons 0..32767 of a run (of each voxel) restart their stream
                              after launch, as each reference thread's first photon does */
+  /* Time-resolved detectors (CUDAMCFL.h det.*temp*; .mci lines of
+   * CUDAMCFLio.cu:374-422): a tdet_nx x tdet_ny array of discs of radius
+   * tdet_r centred on (tdet_x0, tdet_y0) with separations tdet_sep_*, on the
+   * entry (tdet_face 0) or exit face (1); tdet_bins bins over [0, tdet_max)
+   * femtoseconds of time of flight.  Excitation phase only. */
+  int do_temp_sim;
+  float tdet_x0, tdet_y0;
+  int tdet_nx, tdet_ny;
+  float tdet_sep_x, tdet_sep_y;
+  float tdet_r;
+  int tdet_face;
+  long tdet_bins;
+  unsigned long long tdet_max;
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);

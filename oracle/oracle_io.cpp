@@ -45,6 +45,6 @@ extern "C" int oracle_write_fl_images(const char *prefix, const double *flR, con
 
 extern "C" void oracle_free_result(oracle_result *r) {
   free(r->Rd); free(r->Tt); free(r->fhd); free(r->flR); free(r->flT);
-  free(r->flR128); free(r->flT128);
+  free(r->flR128); free(r->flT128); free(r->time_xyt);
   memset(r, 0, sizeof(*r));
 }

@@ -32,9 +32,14 @@
  *
  * Where the reference indexes past an array when a coordinate rounds onto the
  * far edge of the grid or detector, the linear index is clamped to the last
- * element (the engine does the same).  The reference's transport of the time
- * of flight only feeds the time-resolved detectors, which this oracle does not
- * tally.
+ * element (the engine does the same); so is a time bin that rounds onto the
+ * end of the histogram.  The reference converts time-of-flight increments
+ * from double to unsigned long; a glass voxel's back-projection, and the
+ * first step after it when it left the photon outside the slab, can make that
+ * value negative, which C leaves undefined.  The GPU saturates it to 0 (the
+ * engine does the same); the reference's x86-64 host build wraps it modulo
+ * 2^64.  refstream+libm follows the host build (so that it stays bit-identical
+ * to it), every other mode the GPU.
  */
 #include <float.h>
 #include <limits.h>
@@ -61,14 +66,26 @@ const unsigned kStepsPerLaunch = 80000;  /* CUDAMCFL.h:21 */
 const float kPi = 3.141592654f;          /* CUDAMCFL.h:22 */
 const unsigned kWeightRoulette = 429497u; /* CUDAMCFL.h:33 */
 const float kChance = 0.1f;              /* CUDAMCFL.h:34 */
+const double kCcmfs = 2.99792E-5;        /* speed of light [cm/fs], CUDAMCFL.h:29 */
+
+/* (unsigned long)(v) for a double: saturating as the GPU converts, or
+ * wrapping negative values modulo 2^64 as the x86-64 host build does. */
+inline uint64_t tof_u64(double v, int host_wrap) {
+  if (host_wrap && v < 9223372036854775808.0) return (uint64_t)(int64_t)v;
+  if (!(v > 0.0)) return 0;
+  if (v >= 18446744073709551616.0) return 0xFFFFFFFFFFFFFFFFull;
+  return (uint64_t)v;
+}
 
 struct LibmMath {
+  static const int kHost = 1; /* the host build's library and conversions */
   static float log(float x) { return logf(x); }
   static float cos(float x) { return cosf(x); }
   static void sincos(float x, float *s, float *c) { *s = sinf(x); *c = cosf(x); }
 };
 
 struct PortableMath {
+  static const int kHost = 0;
   static float log(float x) { return mcfl_plogf(x); }
   static float cos(float x) { return mcfl_pcosf(x); }
   static void sincos(float x, float *s, float *c) { mcfl_psincosf(x, s, c); }
@@ -92,6 +109,7 @@ struct Photon {
   float x, y, z, dx, dy, dz;
   uint32_t weight;
   uint32_t bulkpos;
+  uint64_t tof; /* time of flight [fs] */
 };
 
 /* Everything one transport phase reads (the reference's __constant__ set). */
@@ -113,6 +131,15 @@ struct Phase {
   uint32_t start_weight;
   int guard; /* reproduce the reference's non-atomic overflow guards */
   int launch_rng_reuse;
+  /* time-resolved detectors (excitation phase) */
+  int tof_wrap; /* host-build conversion of negative time increments (see the file comment) */
+  int time_on;
+  int tdet_face;
+  unsigned tnx, tny;
+  long tbins;
+  uint64_t tmax;
+  float tdet_r;
+  const float *tposx, *tposy;
 };
 
 inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
@@ -180,6 +207,7 @@ void launch_photon(Photon &p, Rng &r, const Phase &ph, float xi, float yi, float
     p.weight = ph.start_weight;
   }
   p.bulkpos = start_label(ph, p);
+  p.tof = 0;
 }
 
 template <class M>
@@ -262,6 +290,7 @@ inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase
     p.x += p.dx * search_step;
     p.y += p.dy * search_step;
     p.z += p.dz * search_step;
+    p.tof += tof_u64(search_step / kCcmfs, ph.tof_wrap);
     if (p.z + p.dz * search_step < 0.0f) {
       present_bulk = 0;
       index = -1;
@@ -315,8 +344,10 @@ inline uint32_t move_to_first_boundary(Photon &p, uint32_t old_bulk, const Phase
         ((new_px2 - x_voxel) * (new_px2 - x_voxel) + (new_py2 - y_voxel) * (new_py2 - y_voxel) +
          (new_pz2 - z_voxel) * (new_pz2 - z_voxel))) {
       p.x = new_px1; p.y = new_py1; p.z = new_pz1;
+      p.tof -= tof_u64(back_step1 / kCcmfs, ph.tof_wrap);
     } else {
       p.x = new_px2; p.y = new_py2; p.z = new_pz2;
+      p.tof -= tof_u64(back_step2 / kCcmfs, ph.tof_wrap);
     }
   }
   return present_bulk;
@@ -347,7 +378,7 @@ inline void add_guarded(unsigned long long *t, uint32_t w, int guard) {
  * (R) or the bottom (T); the emission phase of the photon-indexed variant
  * weights exits with the emitting voxel's fixed-point factor instead. */
 struct Sink {
-  unsigned long long *Rd = nullptr, *Tt = nullptr, *fhd = nullptr;
+  unsigned long long *Rd = nullptr, *Tt = nullptr, *fhd = nullptr, *time_xyt = nullptr;
   unsigned long long *R128 = nullptr, *T128 = nullptr; /* lo,hi pairs */
   uint64_t voxel_q = 0;
   uint64_t absorbed = 0, exit_top = 0, exit_bottom = 0, r_loss = 0, r_gain = 0, w0_loss = 0, steps = 0;
@@ -359,6 +390,23 @@ inline void add128(unsigned long long *acc, uint32_t w, uint64_t q) {
   uint64_t old = __atomic_fetch_add(&acc[0], lo, __ATOMIC_RELAXED);
   uint64_t carry = (old + lo < old) ? 1u : 0u;
   if (hi + carry) __atomic_fetch_add(&acc[1], hi + carry, __ATOMIC_RELAXED);
+}
+
+/* Time-resolved detectors at an exit through the detector array's face
+ * (CUDAMCFLtransport.cu:379-390,406-417): every disc that contains the exit
+ * point gets the weight in the photon's time bin. */
+inline void tally_time(const Phase &ph, const Photon &p, Sink &sk) {
+  if (!(p.tof < ph.tmax)) return;
+  for (unsigned xpos = 0; xpos < ph.tnx; xpos++)
+    for (unsigned ypos = 0; ypos < ph.tny; ypos++) {
+      if (((p.x - ph.tposx[xpos]) * (p.x - ph.tposx[xpos]) + (p.y - ph.tposy[ypos]) * (p.y - ph.tposy[ypos])) <
+          (ph.tdet_r * ph.tdet_r)) {
+        unsigned bin = mcfl_f2u_rz(((float)p.tof / (float)ph.tmax) * (float)ph.tbins);
+        if ((long)bin >= ph.tbins) bin = (unsigned)(ph.tbins - 1);
+        const size_t idx = xpos + (size_t)ph.tnx * (ypos + (size_t)ph.tny * bin);
+        add_guarded(&sk.time_xyt[idx], p.weight, ph.guard);
+      }
+    }
 }
 
 /* One pass of the MCd3D loop body up to the survival test.  Returns 1 while
@@ -383,6 +431,7 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
     p.x += p.dx * s;
     p.y += p.dy * s;
     p.z += p.dz * s;
+    p.tof += tof_u64((double)(s * ph.prop[p.bulkpos].n) / kCcmfs, ph.tof_wrap);
     if (new_bulk != 0 && new_bulk != last_bulk) {
       if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy && p.z < ph.esp)
         new_bulk = (uint32_t)(unsigned short)ph.labels[voxel_index(ph, p.x, p.y, p.z)];
@@ -402,6 +451,7 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
       if (sk.R128) add128(&sk.R128[2 * (size_t)idx], p.weight, sk.voxel_q);
       else add_guarded(&sk.Rd[idx], p.weight, ph.guard);
     }
+    if (ph.time_on && ph.tdet_face == 0) tally_time(ph, p, sk);
     sk.exit_top += p.weight;
     p.weight = 0u;
     s = 0.0f;
@@ -412,6 +462,7 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
       if (sk.T128) add128(&sk.T128[2 * (size_t)idx], p.weight, sk.voxel_q);
       else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
     }
+    if (ph.time_on && ph.tdet_face == 1) tally_time(ph, p, sk);
     sk.exit_bottom += p.weight;
     p.weight = 0u;
     s = 0.0f;
@@ -471,6 +522,38 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
   ph.dir = emission ? 0.0f : sim->dir;
   ph.start_weight = sim->start_weight;
   ph.launch_rng_reuse = sim->launch_rng_reuse;
+  ph.time_on = (!emission && sim->do_temp_sim == 1 && sim->tdet_nx > 0 && sim->tdet_ny > 0 && sim->tdet_bins > 0)
+                   ? 1 : 0;
+  ph.tdet_face = sim->tdet_face;
+  ph.tnx = (unsigned)sim->tdet_nx;
+  ph.tny = (unsigned)sim->tdet_ny;
+  ph.tbins = sim->tdet_bins;
+  ph.tmax = sim->tdet_max;
+  ph.tdet_r = sim->tdet_r;
+}
+
+/* Detector-array positions as DoOneSimulation computes them
+ * (CUDAMCFLmain.cu:94-100), in single precision. */
+void time_positions(const oracle_sim *sim, std::vector<float> &px, std::vector<float> &py) {
+  px.resize(sim->tdet_nx > 0 ? sim->tdet_nx : 1);
+  py.resize(sim->tdet_ny > 0 ? sim->tdet_ny : 1);
+  for (int xi = 0; xi < sim->tdet_nx; xi++)
+    px[xi] = xi * sim->tdet_sep_x - ((sim->tdet_nx - 1) * sim->tdet_sep_x) / 2 + sim->tdet_x0;
+  for (int yi = 0; yi < sim->tdet_ny; yi++)
+    py[yi] = yi * sim->tdet_sep_y - ((sim->tdet_ny - 1) * sim->tdet_sep_y) / 2 + sim->tdet_y0;
+}
+
+/* Allocates the time histogram of the result and points the phase at the
+ * detector positions. */
+void setup_time(const oracle_sim *sim, Phase &ph, std::vector<float> &px, std::vector<float> &py,
+                oracle_result *res, Sink &sk) {
+  if (!ph.time_on) return;
+  time_positions(sim, px, py);
+  ph.tposx = px.data();
+  ph.tposy = py.data();
+  res->time_size = (long)sim->tdet_nx * sim->tdet_ny * sim->tdet_bins;
+  res->time_xyt = (unsigned long long *)calloc((size_t)res->time_size, 8);
+  sk.time_xyt = res->time_xyt;
 }
 
 /* init_RNG (CUDAMCFLrng.cu:31-90) restated.  Returns 0 on success. */
@@ -550,7 +633,9 @@ unsigned long long run_threads(const Phase &ph, unsigned long long nphot, std::v
       for (unsigned t = 0; t < kThreads; ++t) body(t, sk);
     } else {
       std::vector<Sink> local(nthreads);
-      for (auto &l : local) { l.Rd = sk.Rd; l.Tt = sk.Tt; l.fhd = sk.fhd; l.R128 = sk.R128; l.T128 = sk.T128; }
+      for (auto &l : local) {
+        l.Rd = sk.Rd; l.Tt = sk.Tt; l.fhd = sk.fhd; l.R128 = sk.R128; l.T128 = sk.T128; l.time_xyt = sk.time_xyt;
+      }
       std::vector<std::thread> pool;
       for (int w = 0; w < nthreads; ++w)
         pool.emplace_back([&, w] {
@@ -577,6 +662,7 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
   Phase ph;
   make_phase(sim, ph, 0);
   ph.guard = 1;
+  ph.tof_wrap = M::kHost;
   const int nx2 = sim->det_nx, ny2 = sim->det_ny;
   const unsigned xy = ph.xy_size;
   res->grid[0] = (int)ph.num_x; res->grid[1] = (int)ph.num_y; res->grid[2] = (int)ph.num_z;
@@ -592,6 +678,8 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
   if (init_rng_streams(x.data(), a.data(), kThreads, sp, seed_exc)) return -2;
   Sink sk;
   sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
+  std::vector<float> tpx, tpy;
+  setup_time(sim, ph, tpx, tpy, res, sk);
   unsigned long long done = run_threads<M>(ph, sim->number_of_photons, x, a, sk, nthreads, 0);
   res->photons_exc = done;
   res->steps_exc = sk.steps;
@@ -714,6 +802,8 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
   res->flT128 = (unsigned long long *)calloc(2 * (size_t)xy, 8);
   Sink sk;
   sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
+  std::vector<float> tpx, tpy;
+  setup_time(sim, ph, tpx, tpy, res, sk);
   const unsigned long long N = sim->number_of_photons;
   run_photon_threads<M>(ph, mcfl_stream_key(seed_exc, 0), table, N, sk, nullptr, nullptr, 1, nthreads);
   res->photons_exc = N;

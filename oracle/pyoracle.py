@@ -46,6 +46,8 @@ class CResult(ctypes.Structure):
         ("balance", ctypes.c_ulonglong * 6),
         ("steps_exc", ctypes.c_ulonglong),
         ("steps_fl", ctypes.c_ulonglong),
+        ("time_xyt", u64p),
+        ("time_size", ctypes.c_long),
     ]
 
 
@@ -88,6 +90,17 @@ class CSim(ctypes.Structure):
         ("fluor_map", ctypes.POINTER(ctypes.c_float)),
         ("max_fl_voxels", ctypes.c_long),
         ("launch_rng_reuse", ctypes.c_int),
+        ("do_temp_sim", ctypes.c_int),
+        ("tdet_x0", ctypes.c_float),
+        ("tdet_y0", ctypes.c_float),
+        ("tdet_nx", ctypes.c_int),
+        ("tdet_ny", ctypes.c_int),
+        ("tdet_sep_x", ctypes.c_float),
+        ("tdet_sep_y", ctypes.c_float),
+        ("tdet_r", ctypes.c_float),
+        ("tdet_face", ctypes.c_int),
+        ("tdet_bins", ctypes.c_long),
+        ("tdet_max", ctypes.c_ulonglong),
     ]
 
 
@@ -110,6 +123,7 @@ class Result:
     balance: tuple
     steps_exc: int
     steps_fl: int
+    time_xyt: np.ndarray | None = None  # uint64, index ix + nx*(iy + ny*bin)
 
 
 def _to_result(lib, r: CResult) -> Result:
@@ -131,6 +145,7 @@ def _to_result(lib, r: CResult) -> Result:
         flR128=None if not r.flR128 else arr(r.flR128, 2 * xy, np.uint64).reshape(xy, 2),
         flT128=None if not r.flT128 else arr(r.flT128, 2 * xy, np.uint64).reshape(xy, 2),
         balance=tuple(r.balance), steps_exc=r.steps_exc, steps_fl=r.steps_fl,
+        time_xyt=arr(r.time_xyt, r.time_size, np.uint64),
     )
     lib.oracle_free_result(ctypes.byref(r))
     return out

@@ -112,7 +112,8 @@ long run_until_done(SimulationStruct *sim, MemStruct &dev, MemStruct &host, int 
 /* CUDAMCFLmain.cu:60-193 without the printing and the file writing. */
 static unsigned long long do_one_simulation(SimulationStruct *simulation, unsigned long long *x, unsigned int *a,
                                             double *tempfhd, unsigned long long *rd, unsigned long long *tt,
-                                            unsigned long long *fhd_raw, int nthreads) {
+                                            unsigned long long *fhd_raw, int nthreads,
+                                            unsigned long long *time_xyt = nullptr) {
   MemStruct DeviceMem, HostMem;
   const int num_x = (int)(4 * (simulation->esp) * (float)simulation->grid_size);
   const int num_y = (int)(4 * (simulation->esp) * (float)simulation->grid_size);
@@ -142,6 +143,9 @@ static unsigned long long do_one_simulation(SimulationStruct *simulation, unsign
   if (rd) memcpy(rd, HostMem.Rd_xy, xy_size * sizeof(unsigned long long));
   if (tt) memcpy(tt, HostMem.Tt_xy, xy_size * sizeof(unsigned long long));
   if (fhd_raw) memcpy(fhd_raw, HostMem.fhd, (size_t)fhd_size * sizeof(unsigned long long));
+  if (time_xyt)
+    memcpy(time_xyt, HostMem.time_xyt, (size_t)simulation->det.x_temp_numdets * simulation->det.y_temp_numdets *
+                                           simulation->det.temp_bins * sizeof(unsigned long long));
   FreeMemStructs(&HostMem, &DeviceMem);
   return photons_finished;
 }
@@ -212,7 +216,12 @@ extern "C" int ref_run_mci(const char *mci_path, const char *safeprimes_path, un
   res->flT = (double *)calloc(xy_size, 8);
   std::vector<double> Fx(fhd_size > 0 ? fhd_size : 1);
 
-  res->photons_exc = do_one_simulation(sim, x.data(), a.data(), Fx.data(), res->Rd, res->Tt, res->fhd, nthreads);
+  if (sim->do_temp_sim == 1) {
+    res->time_size = (long)sim->det.x_temp_numdets * sim->det.y_temp_numdets * (long)sim->det.temp_bins;
+    res->time_xyt = (unsigned long long *)calloc(res->time_size > 0 ? res->time_size : 1, 8);
+  }
+  res->photons_exc = do_one_simulation(sim, x.data(), a.data(), Fx.data(), res->Rd, res->Tt, res->fhd, nthreads,
+                                       res->time_xyt);
   res->number_of_photons = sim->number_of_photons;
   if (write_files) {
     /* Write_Simulation_Results needs a MemStruct holding the host tallies. */
@@ -220,7 +229,21 @@ extern "C" int ref_run_mci(const char *mci_path, const char *safeprimes_path, un
     memset(&hm, 0, sizeof(hm));
     hm.Rd_xy = res->Rd;
     hm.Tt_xy = res->Tt;
+    std::vector<float> tpx(sim->det.x_temp_numdets + 1), tpy(sim->det.y_temp_numdets + 1);
+    if (sim->do_temp_sim == 1) {
+      const int nxt = sim->det.x_temp_numdets, nyt = sim->det.y_temp_numdets;
+      for (int xi = 0; xi < nxt; xi++)
+        tpx[xi] = xi * sim->det.x_temp_sepdets - ((nxt - 1) * sim->det.x_temp_sepdets) / 2 + sim->det.x0_temp_det;
+      for (int yi = 0; yi < nyt; yi++)
+        tpy[yi] = yi * sim->det.y_temp_sepdets - ((nyt - 1) * sim->det.y_temp_sepdets) / 2 + sim->det.y0_temp_det;
+      hm.tdet_pos_x = tpx.data();
+      hm.tdet_pos_y = tpy.data();
+      hm.time_xyt = res->time_xyt;
+    }
     Write_Simulation_Results(&hm, sim, 0);
+    /* the reference leaves <out>_time.dat open (CUDAMCFLio.cu:168-187); its
+     * process exit flushes it, this driver does it here */
+    fflush(NULL);
     if (sim->fhd_activated == 1) oracle_write_phd(sim->outp_filename, Fx.data(), num_x, num_y, num_z);
   }
 
@@ -291,6 +314,14 @@ extern "C" int ref_parse_mci(const char *mci_path, oracle_sim *out) {
   out->det_dx = sim->det.dx; out->det_dy = sim->det.dy;
   out->det_nx = sim->det.nx; out->det_ny = sim->det.ny;
   out->det_x0 = sim->det.x0; out->det_y0 = sim->det.y0;
+  out->do_temp_sim = sim->do_temp_sim;
+  out->tdet_x0 = sim->det.x0_temp_det; out->tdet_y0 = sim->det.y0_temp_det;
+  out->tdet_nx = (int)sim->det.x_temp_numdets; out->tdet_ny = (int)sim->det.y_temp_numdets;
+  out->tdet_sep_x = sim->det.x_temp_sepdets; out->tdet_sep_y = sim->det.y_temp_sepdets;
+  out->tdet_r = sim->det.temp_det_r;
+  out->tdet_face = (int)sim->det.temp_rort;
+  out->tdet_bins = (long)sim->det.temp_bins;
+  out->tdet_max = (unsigned long long)sim->det.max_temp;
   if (sim->bulk_method == 2) {
     if (sim->n_bulks > ORACLE_MAX_BULKS) return -3;
     for (unsigned i = 0; i < sim->n_bulks + 2; ++i) {

@@ -24,6 +24,8 @@ class Case:
     det: tuple               # dx, dy, nx, ny, x0, y0
     source: tuple = (0.0, 0.0, 0.0)
     do_fl: int = 1
+    # time-resolved detectors: (x0, y0, nx, ny, sep_x, sep_y, radius, face, bins, max_fs) or None
+    temporal: tuple | None = None
 
     @property
     def dims(self):
@@ -63,6 +65,12 @@ class Case:
         lab = np.ascontiguousarray(self.labels.astype(np.int16))
         s.bulk_info = lab.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_short))
         s._keep = lab
+        if self.temporal:
+            x0, y0, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
+            s.do_temp_sim = 1
+            s.tdet_x0, s.tdet_y0, s.tdet_nx, s.tdet_ny = x0, y0, tnx, tny
+            s.tdet_sep_x, s.tdet_sep_y, s.tdet_r, s.tdet_face = sx, sy, r, face
+            s.tdet_bins, s.tdet_max = bins, tmax
         return s
 
     def engine_medium(self, ctx):
@@ -76,7 +84,7 @@ class Case:
         return mc.run_desc(photons or self.photons, source=self.source, det=mc.Detector(x0, y0, dx, dy, nx, ny),
                            photons_per_voxel=self.per_voxel if self.do_fl else 0,
                            fluence=1 if self.do_fl in (1, 2) else 0, seed_exc=seed_exc, seed_fl=seed_fl,
-                           start_weight=self.start_weight())
+                           start_weight=self.start_weight(), tdet=self.temporal)
 
     def write_mci(self, d: str) -> str:
         """Writes <d>/<name>.mci and its bulk file in the reference's grammar."""
@@ -88,8 +96,14 @@ class Case:
         lines = ["# test medium " + self.name, "1.0 # file version", "1 # runs", "2 # method",
                  f"{self.name}-out A", f"{self.photons} # photons", f"{self.per_voxel} # photons per voxel",
                  f"{self.grid} # grid", f"{self.do_fl} # fluorescence", f"{dx} {dy}", f"{dnx} {dny}", f"{x0} {y0}",
-                 "{} {} {}".format(*self.source), "0 # temporal", "0 0", "1 1", "1 1", "0.5", "0", "10", "1000",
-                 f"{len(self.columns)} # bulks", f"{self.esp} # thickness", f"{self.n_out}"]
+                 "{} {} {}".format(*self.source)]
+        if self.temporal:
+            x0, y0, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
+            lines += ["1 # temporal", f"{x0} {y0}", f"{tnx} {tny}", f"{sx} {sy}", f"{r}", f"{face}", f"{bins}",
+                      f"{tmax}"]
+        else:
+            lines += ["0 # temporal", "0 0", "1 1", "1 1", "0.5", "0", "10", "1000"]
+        lines += [f"{len(self.columns)} # bulks", f"{self.esp} # thickness", f"{self.n_out}"]
         for c in self.columns:
             lines.append(" ".join(repr(float(v)) for v in c))
         lines += [f"{self.n_out}", os.path.basename(bulk)]
@@ -163,4 +177,23 @@ def deep(photons=40000, per_voxel=40000) -> Case:
                 1.0, photons, per_voxel, (0.1, 0.1, 20, 20, 0.0, 0.0))
 
 
-ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere}
+def timed(photons=40000, per_voxel=40000, face=0, base=None) -> Case:
+    """mismatch (or another case) with a 3 x 2 array of time-resolved
+    detectors, discs of 0.15 cm 0.25 cm apart, on the entry (face 0) or exit
+    face (1): 40 bins over 0.15 ns (entry) or 0.3 ns (exit)."""
+    c = (base or mismatch)(photons, per_voxel)
+    c.name = c.name + ("_timed" if face == 0 else "_timed_exit")
+    c.temporal = (0.1, -0.05, 3, 2, 0.25, 0.25, 0.15, face, 40, 150000 if face == 0 else 300000)
+    return c
+
+
+def mismatch_timed(photons=40000, per_voxel=40000) -> Case:
+    return timed(photons, per_voxel, 0, mismatch)
+
+
+def glass_timed_exit(photons=40000, per_voxel=40000) -> Case:
+    return timed(photons, per_voxel, 1, glass)
+
+
+ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere, "mismatch_timed": mismatch_timed,
+       "glass_timed_exit": glass_timed_exit}

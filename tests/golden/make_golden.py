@@ -5,7 +5,8 @@ from the reference checkout) on the small media of tests/cases.py.
     python tests/golden/make_golden.py          (needs the reference checkout)
 
 Each fixture holds the raw excitation R/T images, the raw photon hitting
-density and the emission images of one two-phase run, with the seeds and the
+density, the emission images and (for the media with time-resolved
+detectors) the raw time-resolved tallies of one two-phase run, with the seeds and the
 .mci inputs needed to reproduce it.  The multiplier file is the oracle's
 generated safeprimes list (32769 lines).
 """
@@ -27,6 +28,8 @@ FIXTURES = {
     "tiny": dict(photons=40000, per_voxel=33000),
     "mismatch": dict(photons=36000, per_voxel=33000),
     "glass": dict(photons=36000, per_voxel=33000),
+    "mismatch_timed": dict(photons=36000, per_voxel=33000),
+    "glass_timed_exit": dict(photons=36000, per_voxel=33000),
 }
 
 
@@ -42,7 +45,8 @@ def main():
             mci = case.write_mci(d)
             r = ref.run_mci(mci, sp, *SEEDS)
             out = os.path.join(HERE, f"ref_{name}.npz")
-            np.savez_compressed(out, Rd=r.Rd, Tt=r.Tt, fhd=r.fhd, flR=r.flR, flT=r.flT,
+            extra = {} if r.time_xyt is None else {"time_xyt": r.time_xyt}
+            np.savez_compressed(out, Rd=r.Rd, Tt=r.Tt, fhd=r.fhd, flR=r.flR, flT=r.flT, **extra,
                                 photons_exc=r.photons_exc, photons_fl=r.photons_fl, fl_voxels=r.fl_voxels,
                                 seeds=np.array(SEEDS, dtype=np.uint64),
                                 mci=open(mci).read(), bulk=open(mci.replace(".mci", ".bulk")).read())

@@ -24,6 +24,11 @@ def _compare(res, ref, emission=True):
     assert res.stats_exc["done"] == ref.photons_exc
     assert res.stats_exc["steps"] == ref.steps_exc
     assert res.stats_exc["capped"] == 0
+    if ref.time_xyt is not None:
+        assert res.time_xyt is not None and res.time_xyt.ravel().sum() > 0
+        assert np.array_equal(res.time_xyt.ravel(), ref.time_xyt)
+    else:
+        assert res.time_xyt is None
     if emission:
         assert res.fl_voxels == ref.fl_voxels
         assert res.photons_fl == ref.photons_fl

@@ -86,8 +86,10 @@ def test_paired_precision_study_quarter_resolution():
         s = precision.summarize(res)
         for mode in ("fast", "exact"):
             for k in ("R_total", "T_total", "absorbed"):
+                # transmittance through 2.56 cm at mu_s' = 20/cm is ~1e-6: its
+                # relative difference is noise, held by the paired z alone
                 assert abs(s[mode][k]["z"]) < 5.0, (mode, k, s[mode][k])
-                assert abs(s[mode][k]["rel_diff"]) < 5e-3, (mode, k, s[mode][k])
+                assert abs(s[mode][k]["rel_diff"]) < max(5e-3, 5 * s[mode][k]["paired_se_rel"]), (mode, k, s[mode][k])
             assert abs(s[mode]["steps_ratio"] - 1.0) < 5e-3, s[mode]
             assert s[mode]["R_image"]["entries"] > 1000
         assert ctx.get_option("math") == mc.MATH_EXACT

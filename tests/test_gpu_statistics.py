@@ -94,6 +94,29 @@ def test_engine_agrees_with_reference_streams(math, oracle, safeprimes_file):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("math", [mc.MATH_EXACT, mc.MATH_FAST])
+@pytest.mark.parametrize("face", [0, 1])
+def test_time_resolved_detectors_agree_with_reference_streams(math, face, oracle, safeprimes_file):
+    """Time-of-flight histograms of the disc detectors on the entry or exit
+    face, engine against the reference-stream restatement (excitation only),
+    per detector and time bin within 3 sigma."""
+    nthreads = os.cpu_count() or 1
+    case = cases.timed(photons=200_000, per_voxel=0, face=face)
+    case.do_fl = 0
+    sim = case.oracle_sim()
+    ref = [oracle.run_refstream(sim, safeprimes_file, 4000 + b, 1, libm=True, nthreads=nthreads) for b in range(B)]
+    ctx = mc.Context(math=math)
+    med = case.engine_medium(ctx)
+    eng = [_run(ctx, med, case, b, emission=False, reuse=1, seed0=700) for b in range(B)]
+    med.free()
+    ctx.close()
+    a = np.stack([r.time_xyt.ravel().astype(float) for r in eng])
+    b = np.stack([r.time_xyt.astype(float) for r in ref])
+    assert b.sum() > 0
+    stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+
+
+@pytest.mark.gpu
 def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_file):
     """Integrated R, T and absorbed fraction of the fast kernel against the
     reference streams on 1.6e7 reference photons: within 3 sigma and 0.1 %

@@ -20,7 +20,8 @@ from tests import cases
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 FIXTURES = {"tiny": dict(photons=40000, per_voxel=33000), "mismatch": dict(photons=36000, per_voxel=33000),
-            "glass": dict(photons=36000, per_voxel=33000)}
+            "glass": dict(photons=36000, per_voxel=33000), "mismatch_timed": dict(photons=36000, per_voxel=33000),
+            "glass_timed_exit": dict(photons=36000, per_voxel=33000)}
 
 
 def _same(a, b):
@@ -41,9 +42,14 @@ def test_port_reproduces_reference_golden(name, oracle, safeprimes_file, tmp_pat
     assert r.fl_voxels == int(g["fl_voxels"])
     for k in ("Rd", "Tt", "fhd", "flR", "flT"):
         assert _same(getattr(r, k), g[k]), k
+    if "time_xyt" in g:
+        assert g["time_xyt"].sum() > 0
+        assert _same(r.time_xyt, g["time_xyt"])
+    else:
+        assert r.time_xyt is None
 
 
-@pytest.mark.parametrize("name", ["tiny", "glass"])
+@pytest.mark.parametrize("name", ["tiny", "glass", "glass_timed_exit"])
 def test_port_reproduces_reference_build_live(name, oracle, ref_oracle, safeprimes_file, tmp_path):
     case = cases.ALL[name](photons=34000, per_voxel=32800)
     mci = case.write_mci(str(tmp_path))
@@ -52,6 +58,8 @@ def test_port_reproduces_reference_build_live(name, oracle, ref_oracle, safeprim
     b = oracle.run_refstream(sim, safeprimes_file, 4242, 99, libm=True)
     for k in ("Rd", "Tt", "fhd", "flR", "flT"):
         assert _same(getattr(a, k), getattr(b, k)), k
+    if case.temporal:
+        assert _same(a.time_xyt, b.time_xyt)
 
 
 def _sim_fields(s):
@@ -178,4 +186,31 @@ def test_writers_match_reference(mcfl_lib, ref_oracle, safeprimes_file, tmp_path
         assert a == b, suffix
     a = _strip_param(open(d1 / "tiny-out_param.dat").read())
     b = _strip_param(open(d2 / "tiny-out_param.dat").read())
+    assert a == b
+
+
+def test_time_writer_matches_reference(mcfl_lib, ref_oracle, safeprimes_file, tmp_path):
+    """<out>_time.dat of the product's writer equals the reference's for the
+    reference's own time-resolved tallies."""
+    import cudamcfl_gb300 as mc
+    case = cases.mismatch_timed(photons=34000, per_voxel=32800)
+    case.do_fl = 0
+    d1, d2 = tmp_path / "ref", tmp_path / "prod"
+    d1.mkdir()
+    d2.mkdir()
+    mci1 = case.write_mci(str(d1))
+    case.write_mci(str(d2))
+    r = ref_oracle.run_mci(mci1, safeprimes_file, 5, 6, write_files=True)
+    assert r.time_xyt is not None and r.time_xyt.sum() > 0
+    p, n = _product_parse(mcfl_lib, str(d2 / f"{case.name}.mci"))
+    cwd = os.getcwd()
+    os.chdir(d2)
+    try:
+        t = r.time_xyt.copy()
+        assert mcfl_lib.mcfl_write_time(p, mc.u64ptr(t)) == 0
+    finally:
+        os.chdir(cwd)
+        mc.free_simulations(p, n)
+    a = open(d1 / f"{case.name}-out_time.dat").read()
+    b = open(d2 / f"{case.name}-out_time.dat").read()
     assert a == b

@@ -98,6 +98,11 @@ class MediumDesc(ctypes.Structure):
                 ("bulks", ctypes.POINTER(Bulk))]
 
 
+class LayeredDesc(ctypes.Structure):
+    _fields_ = [("n_layers", ctypes.c_int), ("layers", ctypes.POINTER(Layer)), ("inclusion", Inclusion),
+                ("grid_size", ctypes.c_int)]
+
+
 class Detector(ctypes.Structure):
     _fields_ = [("x0", ctypes.c_float), ("y0", ctypes.c_float), ("dx", ctypes.c_float), ("dy", ctypes.c_float),
                 ("nx", ctypes.c_int), ("ny", ctypes.c_int)]
@@ -172,6 +177,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mcfl_medium_free": (None, [vp]),
         "mcfl_medium_bytes": (ctypes.c_size_t, [vp]),
         "mcfl_medium_from_simulation": (ctypes.c_int, [vp, P(Simulation), P(vp)]),
+        "mcfl_medium_create_layered": (ctypes.c_int, [vp, P(LayeredDesc), P(vp)]),
         "mcfl_run": (ctypes.c_int, [vp, vp, P(RunDesc), P(RunOut)]),
         "mcfl_autotune": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_ulonglong, P(ctypes.c_int),
                                          P(ctypes.c_double)]),
@@ -243,6 +249,39 @@ def bulk_from_mci_columns(n: float, mua: float, mus: float, flc: float = 0.0, ab
 
 def outer_bulk(n: float = 1.0) -> Bulk:
     return Bulk(float(np.finfo(np.float32).max), 0.0, 1.0, n, 0.0, 0.0, 0.0, 0.0)
+
+
+def layers_from_mci_columns(n_up: float, slabs, n_down: float) -> list:
+    """The layer table of a layered medium (bulk method 1) from the .mci
+    columns of its slabs (n mua mus flc AbsCExi AbsCEmi eY g thickness),
+    derived as the reference's parser does (CUDAMCFLio.cu:437-477), in single
+    precision: n_slabs + 2 entries, the outer media carrying only n."""
+    f = np.float32
+    out = [Layer(0, 0, 0, 0, 0, f(n_up), 0, 0, 0, 0)]
+    dtot = f(0.0)
+    for n, mua, mus, flc, ax, am, eY, g, thick in slabs:
+        n, mua, mus, flc, ax, am, eY, g, thick = (f(v) for v in (n, mua, mus, flc, ax, am, eY, g, thick))
+        z_min = dtot
+        dtot = f(dtot + thick)
+        mutr = f(np.finfo(np.float32).max) if mus == 0 else f(f(1.0) / f(mua + mus))
+        with np.errstate(invalid="ignore", divide="ignore"):
+            albedof = f(mus / f(f(flc * ax) + mus))
+        out.append(Layer(z_min, dtot, mutr, f(mua + f(flc * ax)), g, n, flc, f(mua + f(flc * am)), eY, albedof))
+    out.append(Layer(0, 0, 0, 0, 0, f(n_down), 0, 0, 0, 0))
+    return out
+
+
+def inclusion_from_mci_columns(x, y, z, r, n, mua, mus, flc=0.0, absc_exi=0.0, absc_emi=0.0, eY=0.0,
+                               g=0.9) -> "Inclusion":
+    """The spherical inclusion of a layered medium from its .mci columns
+    (x y z r n mua mus flc AbsCExi AbsCEmi eY g, CUDAMCFLio.cu:484-500)."""
+    f = np.float32
+    x, y, z, r, n, mua, mus, flc, ax, am, eY, g = (f(v) for v in (x, y, z, r, n, mua, mus, flc, absc_exi, absc_emi,
+                                                                 eY, g))
+    mutr = f(np.finfo(np.float32).max) if mus == 0 else f(f(1.0) / f(mua + mus))
+    with np.errstate(invalid="ignore", divide="ignore"):
+        albedof = f(mus / f(f(flc * ax) + mus))
+    return Inclusion(x, y, z, r, mutr, f(mua + f(flc * ax)), g, n, flc, f(mua + f(flc * am)), eY, albedof)
 
 
 @dataclass
@@ -374,6 +413,18 @@ class Context:
         h = ctypes.c_void_p()
         check(load().mcfl_medium_create(self.handle, ctypes.byref(d), ctypes.byref(h)))
         return Medium(self, h, lab.shape, [])
+
+    def medium_layered(self, layers: list, inclusion: "Inclusion", grid_size: int) -> Medium:
+        """A layered medium with one spherical inclusion (bulk method 1):
+        layers as layers_from_mci_columns returns them."""
+        arr = (Layer * len(layers))(*layers)
+        d = LayeredDesc(len(layers) - 2, ctypes.cast(arr, ctypes.POINTER(Layer)), inclusion, int(grid_size))
+        h = ctypes.c_void_p()
+        check(load().mcfl_medium_create_layered(self.handle, ctypes.byref(d), ctypes.byref(h)))
+        esp = float(np.float32(layers[-2].z_max))
+        g = np.float32(grid_size)
+        n = int(np.rint(np.float32(np.float32(4) * np.float32(esp)) * g))
+        return Medium(self, h, (int(np.float32(esp) * g), n, n), [arr])
 
     def medium_from_simulation(self, sim: Simulation) -> Medium:
         h = ctypes.c_void_p()

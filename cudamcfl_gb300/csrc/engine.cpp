@@ -288,6 +288,74 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
   return MCFL_OK;
 }
 
+extern "C" int mcfl_medium_create_layered(mcfl_ctx *c, const mcfl_layered_desc *d, mcfl_medium **out) {
+  if (!c || !d || !out || !d->layers) return fail(MCFL_E_ARG, "mcfl_medium_create_layered: null argument");
+  *out = nullptr;
+  const int n = d->n_layers;
+  if (n < 1 || n > MCFL_MAX_LAYERS) return fail(MCFL_E_RANGE, "layered medium: n_layers out of range");
+  if (d->grid_size <= 0) return fail(MCFL_E_ARG, "layered medium: grid_size must be positive");
+  for (int i = 1; i <= n; ++i) {
+    const mcfl_layer &l = d->layers[i];
+    if (!(l.z_max > l.z_min) || (i > 1 && l.z_min != d->layers[i - 1].z_max))
+      return fail(MCFL_E_ARG, "layered medium: slabs must be contiguous with z_max > z_min");
+  }
+  if (d->layers[1].z_min != 0.0f) return fail(MCFL_E_ARG, "layered medium: the first slab starts at z = 0");
+  if (!(d->inclusion.r >= 0.0f)) return fail(MCFL_E_ARG, "layered medium: negative inclusion radius");
+  MCFL_CUDA_TRY(cudaSetDevice(c->device));
+  mcfl_medium *m = new mcfl_medium();
+  m->ctx = c;
+  m->layered = true;
+  m->n_layers = n;
+  const float esp = d->layers[n].z_max;
+  const float g = (float)d->grid_size;
+  /* the reference's photon-hitting-density grid (CUDAMCFLtransport.cu:44-45) */
+  m->esp = esp;
+  m->hx = m->hy = 2 * esp;
+  m->gx = m->gy = m->gz = g;
+  m->nx = m->ny = (int)lrintf(4 * esp * g);
+  m->nz = (int)(esp * g);
+  if (m->nx <= 0 || m->nz <= 0 || (unsigned long long)m->nx * m->ny * m->nz >= 0xFFFFFFFFull) {
+    delete m;
+    return fail(MCFL_E_RANGE, "layered medium: bad photon-hitting-density grid");
+  }
+  m->total = (uint32_t)((unsigned long long)m->nx * m->ny * m->nz);
+  /* start weight: the medium above against the first slab (CUDAMCFLio.cu:638-652) */
+  m->bulks.resize(2);
+  std::memset(m->bulks.data(), 0, 2 * sizeof(mcfl_bulk));
+  m->bulks[0].n = d->layers[0].n;
+  m->bulks[1].n = d->layers[1].n;
+  std::vector<float> tab(8 * (size_t)(n + 3), 0.0f);
+  m->z_min.assign((size_t)n + 2, 0.0f);
+  m->z_max.assign((size_t)n + 2, 0.0f);
+  for (int i = 0; i < n + 2; ++i) {
+    const mcfl_layer &l = d->layers[i];
+    float *t = &tab[8 * (size_t)i];
+    const bool slab = i >= 1 && i <= n;
+    t[0] = slab ? l.mutr : 0.0f;
+    t[1] = slab ? l.mua : 0.0f;
+    t[2] = slab ? l.g : 0.0f;
+    t[3] = l.n;
+    t[4] = slab ? l.z_min : 0.0f;
+    t[5] = slab ? l.z_max : 0.0f;
+    m->z_min[i] = t[4];
+    m->z_max[i] = t[5];
+  }
+  float *t = &tab[8 * (size_t)(n + 2)];
+  const mcfl_inclusion &in = d->inclusion;
+  t[0] = in.mutr; t[1] = in.mua; t[2] = in.g; t[3] = in.n;
+  t[4] = in.x; t[5] = in.y; t[6] = in.z; t[7] = in.r;
+  cudaError_t e = m->layer_tab.reserve(tab.size() * 4);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->layer_tab.p, tab.data(), tab.size() * 4, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    delete m;
+    return cuda_fail(e, "mcfl_medium_create_layered");
+  }
+  m->bytes = m->layer_tab.bytes;
+  *out = m;
+  return MCFL_OK;
+}
+
 extern "C" void mcfl_medium_free(mcfl_medium *m) {
   if (!m) return;
   cudaSetDevice(m->ctx->device);

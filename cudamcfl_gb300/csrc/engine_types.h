@@ -78,7 +78,8 @@ typedef struct MCFL_ALIGN(16) McflJob {
   unsigned long long *time_xyt;
   uint64_t tmax;
   float tdet_r;
-  uint32_t tnx, tny, tbins, tdet_face, pad1;
+  uint32_t tnx, tny, tbins, tdet_face;
+  uint32_t start_layer; /* layered media: the layer holding the source */
   /* photons */
   uint64_t key;          /* stream family key */
   uint64_t rng_offset;   /* stream index of the job's photon 0 */
@@ -117,6 +118,14 @@ typedef struct McflMedium {
   unsigned long long *fhd; /* NULL when no job tallies the photon hitting density */
   float hx, hy, esp, gx, gy, gz;
   uint32_t nx, ny, total, last_label;
+  /* Layered medium (the reference's bulk method 1): slabs 1..n_layers between
+   * the media above (0) and below (n_layers+1) and one spherical inclusion.
+   * layer_tab: n_layers+2 entries of two float4, (mutr, mu_a, g, n) and
+   * (z_min, z_max, 0, 0), then the inclusion's (mutr, mu_a, g, n) and
+   * (x, y, z, r).  The geometry above is then the photon-hitting-density
+   * grid's. */
+  const float *layer_tab;
+  uint32_t layered, n_layers;
 } McflMedium;
 
 typedef struct McflLaunch {

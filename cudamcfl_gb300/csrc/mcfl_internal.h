@@ -106,6 +106,11 @@ struct mcfl_medium {
   bool has_fmap = false;
   std::vector<mcfl_bulk> bulks;
   size_t bytes = 0;
+  /* layered medium (bulk method 1) */
+  bool layered = false;
+  int n_layers = 0;
+  mcfl::DevBuf layer_tab;
+  std::vector<float> z_min, z_max; /* per layer, host copies */
 };
 
 struct mcfl_ctx {

@@ -535,8 +535,18 @@ extern "C" int mcfl_write_fl_images(const mcfl_simulation *sim, const double *fl
 
 extern "C" int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_medium **medium) {
   if (!sim) return fail(MCFL_E_ARG, "null simulation");
+  if (sim->bulk_method == 1) {
+    if (!sim->layers) return fail(MCFL_E_ARG, "bulk method 1 without layers");
+    mcfl_layered_desc ld;
+    std::memset(&ld, 0, sizeof(ld));
+    ld.n_layers = (int)sim->n_layers;
+    ld.layers = sim->layers;
+    ld.inclusion = sim->inclusion;
+    ld.grid_size = sim->grid_size;
+    return mcfl_medium_create_layered(ctx, &ld, medium);
+  }
   if (sim->bulk_method != 2 || !sim->bulk_info || !sim->bulks)
-    return fail(MCFL_E_STATE, "only bulk method 2 (voxelized bulk descriptor) runs on the engine");
+    return fail(MCFL_E_STATE, "unknown bulk method");
   mcfl_medium_desc d;
   std::memset(&d, 0, sizeof(d));
   d.nx = sim->num_x;
@@ -557,7 +567,9 @@ extern "C" int mcfl_run_desc_from_simulation(const mcfl_simulation *sim, unsigne
   if (!sim || !run) return fail(MCFL_E_ARG, "null argument");
   std::memset(run, 0, sizeof(*run));
   run->photons = sim->number_of_photons;
-  run->photons_per_voxel = sim->do_fl_sim ? sim->number_of_photons_per_voxel : 0;
+  /* the reference simulates emission for voxelized media only (its gate
+   * albedof < 0 never holds for bulk method 1, CUDAMCFLmain.cu:520,535) */
+  run->photons_per_voxel = sim->do_fl_sim && sim->bulk_method == 2 ? sim->number_of_photons_per_voxel : 0;
   run->fluence = sim->fhd_activated;
   run->seed_exc = seed;
   run->seed_fl = seed + 1;
@@ -640,16 +652,13 @@ extern "C" unsigned long long mcfl_DoOneSimulationFl(const mcfl_simulation *sim,
   return rc == MCFL_OK ? st[MCFL_ST_DONE] : 0ull;
 }
 
-extern "C" int mcfl_run_mci(const char *mci_path, unsigned long long seed) {
-  mcfl_simulation *sims = nullptr;
-  const int n = mcfl_read_simulation_data(mci_path, &sims, 0);
-  if (n <= 0) return MCFL_E_PARSE;
-  mcfl_simulation *sim = &sims[0];
-  int rc = MCFL_OK;
-  mcfl_ctx *c = default_ctx();
+namespace {
+
+/* One simulation of a .mci file: run, then every file the reference writes. */
+int run_one_simulation(mcfl_ctx *c, mcfl_simulation *sim, unsigned long long seed) {
   mcfl_medium *m = nullptr;
-  if (!c) rc = MCFL_E_CUDA;
-  if (rc == MCFL_OK) rc = mcfl_medium_from_simulation(c, sim, &m);
+  int rc = mcfl_medium_from_simulation(c, sim, &m);
+  if (rc != MCFL_OK) return rc;
   const size_t xy = (size_t)sim->det.nx + (size_t)sim->det.nx * sim->det.ny;
   const size_t nv = (size_t)sim->num_x * sim->num_y * sim->num_z;
   std::vector<unsigned long long> Rd(xy), Tt(xy);
@@ -658,26 +667,41 @@ extern "C" int mcfl_run_mci(const char *mci_path, unsigned long long seed) {
   mcfl_run_desc run;
   mcfl_run_out out;
   std::memset(&out, 0, sizeof(out));
-  if (rc == MCFL_OK) {
-    mcfl_run_desc_from_simulation(sim, seed, &run);
-    out.Rd = Rd.data();
-    out.Tt = Tt.data();
-    out.phd = sim->fhd_activated ? phd.data() : nullptr;
-    out.flR = flR.data();
-    out.flT = flT.data();
-    if (run.tdet.nx > 0) {
-      tim.assign((size_t)run.tdet.nx * run.tdet.ny * run.tdet.bins, 0ull);
-      out.time_xyt = tim.data();
-    }
-    const auto t0 = std::chrono::steady_clock::now();
-    rc = mcfl_run(c, m, &run, &out);
-    const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    if (rc == MCFL_OK) rc = mcfl_Write_Simulation_Results(sim, Rd.data(), Tt.data(), secs);
-    if (rc == MCFL_OK && !tim.empty()) rc = mcfl_write_time(sim, tim.data());
+  mcfl_run_desc_from_simulation(sim, seed, &run);
+  out.Rd = Rd.data();
+  out.Tt = Tt.data();
+  out.phd = sim->fhd_activated ? phd.data() : nullptr;
+  out.flR = flR.data();
+  out.flT = flT.data();
+  if (run.tdet.nx > 0) {
+    tim.assign((size_t)run.tdet.nx * run.tdet.ny * run.tdet.bins, 0ull);
+    out.time_xyt = tim.data();
   }
-  if (rc == MCFL_OK && sim->fhd_activated == 1) rc = mcfl_write_phd(sim, phd.data());
-  if (rc == MCFL_OK && sim->do_fl_sim != 0) rc = mcfl_write_fl_images(sim, flR.data(), flT.data());
+  const auto t0 = std::chrono::steady_clock::now();
+  rc = mcfl_run(c, m, &run, &out);
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   mcfl_medium_free(m);
+  if (rc == MCFL_OK) rc = mcfl_Write_Simulation_Results(sim, Rd.data(), Tt.data(), secs);
+  if (rc == MCFL_OK && !tim.empty()) rc = mcfl_write_time(sim, tim.data());
+  if (rc == MCFL_OK && sim->fhd_activated == 1) rc = mcfl_write_phd(sim, phd.data());
+  /* a layered medium never emits: its emission images are zeros, as the
+   * reference writes them */
+  if (rc == MCFL_OK && sim->do_fl_sim != 0) rc = mcfl_write_fl_images(sim, flR.data(), flT.data());
+  return rc;
+}
+
+} // namespace
+
+extern "C" int mcfl_run_mci(const char *mci_path, unsigned long long seed) {
+  mcfl_simulation *sims = nullptr;
+  const int n = mcfl_read_simulation_data(mci_path, &sims, 0);
+  if (n <= 0) return MCFL_E_PARSE;
+  mcfl_ctx *c = default_ctx();
+  int rc = c ? MCFL_OK : MCFL_E_CUDA;
+  /* every run of the file, each with its own outputs and seeds seed + 2i
+   * (the reference parses the runs and simulates only the first,
+   * CUDAMCFLio.cu:272-274, CUDAMCFLmain.cu:340-668) */
+  for (int i = 0; rc == MCFL_OK && i < n; ++i) rc = run_one_simulation(c, &sims[i], seed + 2ull * (unsigned)i);
   mcfl_free_simulation_struct(sims, n);
   return rc;
 }

@@ -72,6 +72,12 @@ void fill_source(McflJob &j, const mcfl_run_desc &r, const mcfl_medium *m) {
   j.src_w = r.source.width;
   j.src_h = r.source.height;
   j.start_weight = r.start_weight ? r.start_weight : default_start_weight(m);
+  if (m->layered) /* LaunchPhoton's search for the source's slab (CUDAMCFLtransport.cu:550-560) */
+    for (int nl = 1; nl <= m->n_layers; ++nl)
+      if (r.source.z < m->z_max[nl] && r.source.z >= m->z_min[nl]) {
+        j.start_layer = (uint32_t)nl;
+        break;
+      }
 }
 
 int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run) {
@@ -91,6 +97,13 @@ int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run)
       return fail(MCFL_E_ARG, "bad time-resolved detectors");
     if ((unsigned long long)td.nx * (unsigned long long)td.ny * (unsigned long long)td.bins >= (1ull << 31))
       return fail(MCFL_E_RANGE, "time-resolved tally too large");
+  }
+  if (m->layered) {
+    if (run->photons_per_voxel) return fail(MCFL_E_ARG, "layered medium: excitation runs only");
+    bool inside = false;
+    for (int nl = 1; nl <= m->n_layers; ++nl)
+      inside = inside || (run->source.z < m->z_max[nl] && run->source.z >= m->z_min[nl]);
+    if (!inside) return fail(MCFL_E_ARG, "layered medium: the source z lies in no slab");
   }
   return MCFL_OK;
 }
@@ -228,6 +241,12 @@ void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool em
   u.ny = (uint32_t)m->ny;
   u.total = m->total;
   u.last_label = (uint32_t)m->n_bulks + 1u;
+  if (m->layered) {
+    u.layered = 1;
+    u.n_layers = (uint32_t)m->n_layers;
+    u.layer_tab = m->layer_tab.as<float>();
+    u.n_labels = 0;
+  }
 }
 
 } // namespace
@@ -683,6 +702,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
 
 int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run, unsigned int voxel,
                                     unsigned long long *R, unsigned long long *T, unsigned long long *stats) {
+  if (m->layered) return fail(MCFL_E_ARG, "layered medium: no emission runs");
   const mcfl_detector &det = run->det;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   cudaStream_t s = c->stream;

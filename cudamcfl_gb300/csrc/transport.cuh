@@ -240,6 +240,7 @@ __device__ __forceinline__ uint32_t find_job(const McflLaunch &L, uint64_t t) {
   return (t >= b && t - b < n) ? slot : 0xffffffffu;
 }
 
+template <bool kLayered>
 __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,
                                               Photon &p, Rng &r, uint32_t &src_idx) {
   mcfl_photon_stream(__ldg((const unsigned long long *)&J->key),
@@ -296,7 +297,7 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     p.dz = MCFL_C(1.0);
     p.weight = __ldg(&J->start_weight);
   }
-  p.label = start_label(m, p);
+  p.label = kLayered ? __ldg(&J->start_layer) : start_label(m, p);
   p.tof = 0;
   /* The reference's first photon on each of its 32768 threads draws its first
    * passes from the stream state its launch started from, because
@@ -304,6 +305,21 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
    * (CUDAMCFLtransport.cu:574-581).  Reproduced on request for photons
    * 0..32767 of a run (of each emitting voxel's run). */
   if (__ldg(&J->launch_rng_reuse) && k_in_run < 32768u) r.x = x_at_launch;
+}
+
+/* The record of a (mutr, mu_a, g, n) entry, built on the device (layered
+ * media). */
+__device__ __forceinline__ Rec rec_of(float4 q) {
+#if MCFL_F64
+  return make_rec(q);
+#else
+  float t[MCFL_LAB_FLOATS];
+  mcfl_label_record(q.x, q.y, q.z, q.w, t);
+  Rec r;
+  r.a = make_float4(t[0], t[1], t[2], t[3]);
+  r.b = make_float4(t[4], t[5], t[6], t[7]);
+  return r;
+#endif
 }
 
 /* Henyey-Greenstein deflection and rotation of the direction
@@ -545,7 +561,7 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
 /* One warp-synchronous persistent loop per thread; see the file comment.
  * kUniform: the medium comes from the launch parameters (constant bank)
  * instead of per-lane registers loaded from the job. */
-template <bool kUniform, bool kTime, int kThreads, int kMinBlocks>
+template <bool kUniform, bool kTime, bool kLayered, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   /* shared memory: kEv x blockDim.x event counters, then (uniform medium)
    * the label records of the medium */
@@ -555,7 +571,18 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   const unsigned tib = threadIdx.x;
   const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (int e = 0; e < kEv; ++e) s_ev[e * blockDim.x + tib] = 0ull;
-  if (kUniform) {
+  if (kLayered) {
+    /* per layer (and, last, the inclusion): its record and its geometry */
+    const float4 *tab = (const float4 *)L.med.layer_tab;
+    for (uint32_t i = tib; i < L.med.n_layers + 3; i += blockDim.x) {
+      const Rec q = rec_of(__ldg(&tab[2 * i]));
+      const float4 g = __ldg(&tab[2 * i + 1]);
+      s_lab[3 * i] = q.a;
+      s_lab[3 * i + 1] = q.b;
+      s_lab[3 * i + 2] = real4{g.x, g.y, g.z, g.w};
+    }
+    __syncthreads();
+  } else if (kUniform) {
 #if MCFL_F64
     for (uint32_t i = tib; i < L.med.n_labels; i += blockDim.x) {
       const Rec q = make_rec(__ldg((const float4 *)L.med.prop + i));
@@ -662,7 +689,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               if (!kUniform) load_med(J, m);
             }
             k = t - __ldg((const unsigned long long *)&J->ticket_begin);
-            launch_photon(J, m, k, L.mult, p, r, src_idx);
+            launch_photon<kLayered>(J, m, k, L.mult, p, r, src_idx);
             if (!kUniform) rc = load_rec(m, p.label);
             pst = 0;
             pst0 = 0;
@@ -677,8 +704,76 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (!alive) continue;
     }
 
-    /* ---- one transport pass (MCd3D loop body) ---- */
     ++pst;
+    if constexpr (kLayered) {
+      /* ---- one transport pass of a layered medium (MCd loop body,
+       * CUDAMCFLtransport.cu:73-233) ---- */
+      const uint32_t nl = L.med.n_layers;
+      const real4 ig = s_lab[3 * (nl + 2) + 2]; /* inclusion x, y, z, r */
+      const real4 lg = s_lab[3 * p.label + 2];  /* z_min, z_max of the photon's layer */
+      const real n_here = s_lab[3 * p.label + 1].w;
+      auto inside = [&]() {
+        return ((p.x - ig.x) * (p.x - ig.x) + (p.y - ig.y) * (p.y - ig.y) + (p.z - ig.z) * (p.z - ig.z)) <=
+               (ig.w * ig.w);
+      };
+      real s;
+      /* outside the inclusion the reference steps 1/mu_t itself, without
+       * sampling (CUDAMCFLtransport.cu:87-89); scattering-free: 2 cm */
+      if (inside()) {
+        const real mutr = s_lab[3 * (nl + 2)].x;
+        s = mutr != FLT_MAX ? -MCFL_LOGF(r.oc()) * mutr : MCFL_C(2.0);
+      } else {
+        const real mutr = s_lab[3 * p.label].x;
+        s = mutr != FLT_MAX ? mutr : MCFL_C(2.0);
+      }
+      int new_layer = (int)p.label;
+      if (p.z + s * p.dz < lg.x) {
+        --new_layer;
+        s = (lg.x - p.z) / p.dz;
+      }
+      if (p.z + s * p.dz >= lg.y) {
+        ++new_layer;
+        s = (lg.y - p.z) / p.dz;
+      }
+      p.x += p.dx * s;
+      p.y += p.dy * s;
+      p.z += p.dz * s;
+      if (kTime) p.tof += tof_fs(s * n_here);
+      if (p.z > lg.y) p.z = lg.y;
+      if (p.z < lg.x) p.z = lg.x;
+      if (m.fhd && MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp) {
+        const uint32_t fi = voxel_index(m, p.x, p.y, p.z);
+        if (fi != f_idx) {
+          if (f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
+          f_idx = fi;
+          f_acc = 0ull;
+        }
+        f_acc += p.weight;
+      }
+      if (new_layer != (int)p.label) {
+        s = MCFL_C(0.0);
+        if (reflect(p, n_here, s_lab[3 * new_layer + 1].w, r)) {
+          p.label = (uint32_t)new_layer;
+          if (new_layer == 0 || new_layer > (int)nl) {
+            const bool top = new_layer == 0;
+            tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+            if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
+            ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+            p.weight = 0u;
+          }
+        }
+      }
+      if (s > MCFL_C(0.0)) {
+        /* rounded to nearest, never a kill (CUDAMCFLtransport.cu:201-215) */
+        const uint32_t e = inside() ? nl + 2 : p.label;
+        const Rec c2 = Rec{s_lab[3 * e], s_lab[3 * e + 1]};
+        const uint32_t w = MCFL_R2U_RN(c2.a.y * MCFL_U2R_RN(p.weight));
+        p.weight -= w;
+        absorbed += w;
+        spin(p, c2, r);
+      }
+    } else {
+    /* ---- one transport pass (MCd3D loop body) ---- */
     real s;
     uint32_t new_bulk;
     uint32_t vi = 0xffffffffu; /* voxel of the end point, when looked up */
@@ -748,6 +843,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       }
       spin(p, c2, r);
     }
+    }
     /* PhotonSurvive */
     if (p.weight <= kWeightRoulette) {
       if (p.weight == 0u) {
@@ -802,18 +898,21 @@ static size_t smem_bytes(int block, bool uniform) {
 /* Kernel variants.  Single medium (occupancy variants: threads per block x
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner; 3 = 256 x 3 carrying
- * the time of flight.  Mixed media: -1 = 256 x 3, -2 = 256 x 2 with the time
- * of flight. */
+ * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
+ * of flight.  Mixed media: -1 = 256 x 3, -2 = 256 x 2 with the time of
+ * flight. */
 typedef void (*TransportKernel)(McflLaunch);
 
 static TransportKernel kernel_of(int variant, int *threads) {
   switch (variant) {
-  case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, 256, 2>;
-  case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, 256, 3>;
-  case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, 256, 4>;
-  case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, 256, 5>;
-  case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, 128, 9>;
-  case 3: *threads = 256; return MCFL_KERNEL_NAME<true, true, 256, 3>;
+  case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, false, 256, 2>;
+  case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, false, 256, 3>;
+  case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 4>;
+  case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 5>;
+  case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, false, 128, 9>;
+  case 3: *threads = 256; return MCFL_KERNEL_NAME<true, true, false, 256, 3>;
+  case 4: *threads = 256; return MCFL_KERNEL_NAME<true, false, true, 256, 4>;
+  case 5: *threads = 256; return MCFL_KERNEL_NAME<true, true, true, 256, 3>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -828,7 +927,11 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
   if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
 #endif
   if (L->max_iters && L->time_on) return cudaErrorNotSupported; /* parked photons carry no time of flight */
-  const int v = L->uniform_medium ? (L->time_on ? 3 : (int)L->variant) : (L->time_on ? -2 : -1);
+  if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
+    return cudaErrorInvalidValue;
+  const int v = L->med.layered ? (L->time_on ? 5 : 4)
+                : L->uniform_medium ? (L->time_on ? 3 : (int)L->variant)
+                                    : (L->time_on ? -2 : -1);
   int t = 0;
   const TransportKernel fn = kernel_of(v, &t);
   if (!fn || block > t) return cudaErrorInvalidValue;

@@ -29,6 +29,7 @@ import json
 import time
 
 import numpy as np
+from scipy.stats import t as _t
 
 from . import MATH_EXACT, MATH_F64, MATH_FAST, SOURCE_WIDEFIELD, Context, run_desc
 from . import media as media_mod
@@ -44,10 +45,22 @@ def _paired(a: np.ndarray, b: np.ndarray):
     return d.mean(axis=0), d.std(axis=0, ddof=1) / np.sqrt(n)
 
 
-def study(ctx: Context, med, rd_for_seed, batches: int, modes=("fast", "exact", "f64"), fluence: bool = True):
+def _block_sum(fhd: np.ndarray, shape, block: int) -> np.ndarray:
+    """Photon hitting density summed over block^3 voxel cubes (the grid's
+    extents must be multiples of block)."""
+    nz, ny, nx = shape
+    if block <= 1:
+        return fhd.astype(np.float64)
+    v = fhd.reshape(nz // block, block, ny // block, block, nx // block, block)
+    return v.sum(axis=(1, 3, 5), dtype=np.float64).ravel()
+
+
+def study(ctx: Context, med, rd_for_seed, batches: int, modes=("fast", "exact", "f64"), fluence: bool = True,
+          fluence_block: int = 1):
     """Runs every build on the same B seeds; returns the per-build batch
-    arrays {mode: {"R": (B, pix), "T": ..., "phd": (B, vox), "A": (B,),
-    "Rall": (B,), "Tall": (B,), "seconds": float, "steps": int}}."""
+    arrays {mode: {"R": (B, pix), "T": ..., "phd": (B, cells), "A": (B,),
+    "Rall": (B,), "Tall": (B,), "seconds": float, "steps": int}}; the photon
+    hitting density is kept summed over fluence_block^3 voxel cells."""
     out = {m: {"R": [], "T": [], "phd": [], "A": [], "Rall": [], "Tall": [], "seconds": 0.0, "steps": 0,
                "photons": 0} for m in modes}
     old = ctx.get_option("math")
@@ -64,7 +77,7 @@ def study(ctx: Context, med, rd_for_seed, batches: int, modes=("fast", "exact", 
                 out[mode]["R"].append(r.Rd.astype(np.float64) / (ONE * n))
                 out[mode]["T"].append(r.Tt.astype(np.float64) / (ONE * n))
                 if fluence and r.fhd is not None:
-                    out[mode]["phd"].append(r.fhd.astype(np.float64) / (ONE * n))
+                    out[mode]["phd"].append(_block_sum(r.fhd, med.shape, fluence_block) / (ONE * n))
                 out[mode]["A"].append(se["absorbed"] / (ONE * n))
                 out[mode]["Rall"].append(se["exit_top"] / (ONE * n))
                 out[mode]["Tall"].append(se["exit_bottom"] / (ONE * n))
@@ -90,8 +103,12 @@ def _field(a: np.ndarray, b: np.ndarray, floor: float = 0.0):
     z = np.zeros_like(d)
     z[ok] = d[ok] / se[ok]
     rel = d / mean_b[keep]
+    # with B batches the paired z follows Student's t with B-1 degrees of
+    # freedom: the 3-sigma gate at its 0.27 % two-sided tail
+    thr = float(_t.isf(0.0027 / 2, max(1, a.shape[0] - 1)))
     return {"entries": int(keep.sum()), "rel_rms": float(np.sqrt(np.mean(rel * rel))),
             "rel_mean": float(np.mean(rel)), "beyond_3se": float(np.mean(np.abs(z[ok]) > 3.0)) if ok.any() else 0.0,
+            "t_threshold": thr, "beyond_t": float(np.mean(np.abs(z[ok]) > thr)) if ok.any() else 0.0,
             "max_abs_z": float(np.max(np.abs(z[ok]))) if ok.any() else 0.0,
             "mean_z": float(np.mean(z[ok])) if ok.any() else 0.0}
 
@@ -103,14 +120,16 @@ def _scalar(a: np.ndarray, b: np.ndarray):
             "paired_se_rel": float(se / m) if m else 0.0, "z": float(d / se) if se > 0 else 0.0}
 
 
-def summarize(res: dict, ref: str = "f64") -> dict:
+def summarize(res: dict, ref: str = "f64", min_photons: float = 20.0) -> dict:
+    """Per build against `ref`: integrated fractions, and the R/T images and
+    fluence over the entries holding at least min_photons photons' weight
+    per batch."""
     out = {}
     for mode, r in res.items():
         if mode == ref:
             continue
         b = res[ref]
-        # pixels/voxels with at least ~100 photons' worth of weight in a batch
-        pix_floor = 100.0 / max(1, r["photons"] // len(r["A"]))
+        pix_floor = min_photons / max(1, r["photons"] // len(r["A"]))
         out[mode] = {
             "R_total": _scalar(r["Rall"], b["Rall"]), "T_total": _scalar(r["Tall"], b["Tall"]),
             "absorbed": _scalar(r["A"], b["A"]),
@@ -143,11 +162,14 @@ def main(argv=None) -> int:
         return run_desc(per_batch, det=m.det, fluence=0 if args.no_fluence else 1, seed_exc=seed, seed_fl=seed + 1,
                         kind=SOURCE_WIDEFIELD, width=w, height=h)
 
-    res = study(ctx, med, rd_for_seed, args.batches, tuple(args.modes.split(",")), fluence=not args.no_fluence)
+    # full size: the fluence compared on 4^3-voxel cells (128 x 128 x 64)
+    res = study(ctx, med, rd_for_seed, args.batches, tuple(args.modes.split(",")), fluence=not args.no_fluence,
+                fluence_block=1 if args.small else 4)
     s = summarize(res)
     s["workload"] = {"medium": "config5" + (" quarter resolution" if args.small else ""),
                      "shape_zyx": list(m.labels.shape), "voxel_cm": m.voxel_cm[0], "photons_per_build": per_batch *
-                     args.batches, "batches": args.batches, "source": f"wide-field {w:.2f} x {h:.2f} cm"}
+                     args.batches, "batches": args.batches, "source": f"wide-field {w:.2f} x {h:.2f} cm",
+                     "fluence_cells": "voxels" if args.small else "4x4x4-voxel cells"}
     print(json.dumps(s), flush=True)
     med.free()
     ctx.close()

@@ -45,6 +45,7 @@ enum {
 
 #define MCFL_STR_LEN 500
 #define MCFL_MAX_BULKS 253
+#define MCFL_MAX_LAYERS 98
 
 /* ---------------------------------------------------------------------- */
 /* Reference data types                                                    */
@@ -172,10 +173,12 @@ int mcfl_write_phd(const mcfl_simulation *sim, const double *fhd);
 int mcfl_write_fl_images(const mcfl_simulation *sim, const double *flR, const double *flT);
 
 /* main, CUDAMCFLmain.cu:290-668: the whole two-phase run of a .mci file
- * (bulk method 2) with every output file the reference writes, both phases
- * seeded from seed (the reference seeds its emission phase from time(NULL),
- * CUDAMCFLmain.cu:412).  Paths resolve against the working directory, as the
- * reference's do. */
+ * (voxelized or layered medium) with every output file the reference writes,
+ * both phases seeded from seed (the reference seeds its emission phase from
+ * time(NULL), CUDAMCFLmain.cu:412).  A file with several runs runs all of
+ * them, run i seeded from seed + 2i, each writing its own outputs (the
+ * reference parses them but simulates only the first).  Paths resolve
+ * against the working directory, as the reference's do. */
 int mcfl_run_mci(const char *mci_path, unsigned long long seed);
 
 /* ---------------------------------------------------------------------- */
@@ -303,6 +306,27 @@ long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
 /* Uses a caller stream (cudaStream_t) for all work of this context; NULL
  * restores the context's own stream. */
 int mcfl_set_stream(mcfl_ctx *ctx, void *stream);
+
+/* Layered medium with one spherical inclusion: the reference's bulk method 1
+ * (LayerStruct/IncStruct of CUDAMCFL.h, transported by MCd,
+ * CUDAMCFLtransport.cu:29-239).  layers: n_layers + 2 entries, [1..n_layers]
+ * the slabs (z_min, z_max, mutr, mua, g, n as the .mci parser fills them),
+ * [0] and [n_layers+1] the media above and below, of which only n is read.
+ * The transport is the reference's as it runs: outside the inclusion every
+ * step is 1/mu_t itself, not a sampled -ln(u)/mu_t (CUDAMCFLtransport.cu:
+ * 87-89); a scattering-free layer or inclusion steps 2 cm; the absorbed
+ * weight rounds to nearest and a zero drop does not kill.  The photon hitting
+ * density is tallied on the reference's grid (4 esp x 4 esp x esp, grid_size
+ * voxels per cm, esp = layers[n_layers].z_max).  Runs on a layered medium are
+ * excitation runs (the reference never simulates emission for it), from a
+ * collimated source whose z lies in a slab. */
+typedef struct mcfl_layered_desc {
+  int n_layers;
+  const mcfl_layer *layers;
+  mcfl_inclusion inclusion;
+  int grid_size;
+} mcfl_layered_desc;
+int mcfl_medium_create_layered(mcfl_ctx *ctx, const mcfl_layered_desc *desc, mcfl_medium **medium);
 
 /* Uploads a medium; it stays resident until mcfl_medium_free, which must
  * come before mcfl_destroy of its context. */

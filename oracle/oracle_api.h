@@ -49,6 +49,14 @@ typedef struct oracle_bulk {
   float mutr, mua, g, n, flc, muaf, eY, albedof;
 } oracle_bulk;
 
+#define ORACLE_MAX_LAYERS 100
+typedef struct oracle_layer {
+  float z_min, z_max, mutr, mua, g, n, flc, muaf, eY, albedof;
+} oracle_layer;
+typedef struct oracle_inclusion {
+  float x, y, z, r, mutr, mua, g, n, flc, muaf, eY, albedof;
+} oracle_inclusion;
+
 typedef struct oracle_sim {
   unsigned long long number_of_photons;
   unsigned int number_of_photons_per_voxel;
@@ -90,6 +98,13 @@ typedef struct oracle_sim {
   int tdet_face;
   long tdet_bins;
   unsigned long long tdet_max;
+  /* Bulk method 1 (CUDAMCFL.h LayerStruct/IncStruct; .mci lines of
+   * CUDAMCFLio.cu:424-511): n_layers slabs (layers[1..n_layers], with
+   * layers[0] and layers[n_layers+1] the media above and below, of which only
+   * n is read) and one spherical inclusion. */
+  int n_layers;
+  oracle_layer layers[ORACLE_MAX_LAYERS + 2];
+  oracle_inclusion inclusion;
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);

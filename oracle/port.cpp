@@ -15,6 +15,8 @@
  *   Rng                    rand_MWC_co/oc        CUDAMCFLrng.cu:17-29
  *   init_rng_streams       init_RNG              CUDAMCFLrng.cu:31-90
  *   run_refstream          DoOneSimulation(Fl) + voxel loop  CUDAMCFLmain.cu:60-288,409-652
+ *   step_layers            MCd loop body (bulk method 1: layers and one
+ *                          spherical inclusion)  CUDAMCFLtransport.cu:73-233
  *
  * Every floating-point expression keeps the reference's operand order and
  * types (including its double-precision literals), so each rounding happens
@@ -140,6 +142,13 @@ struct Phase {
   uint64_t tmax;
   float tdet_r;
   const float *tposx, *tposy;
+  /* bulk method 1: slabs 1..n_layers between the outer media 0 and
+   * n_layers+1, one spherical inclusion; the photon's bulkpos is its layer */
+  int method;
+  unsigned n_layers;
+  oracle_layer layers[ORACLE_MAX_LAYERS + 2];
+  oracle_inclusion incl;
+  uint32_t start_layer;
 };
 
 inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
@@ -206,7 +215,7 @@ void launch_photon(Photon &p, Rng &r, const Phase &ph, float xi, float yi, float
     p.dz = 1.0f;
     p.weight = ph.start_weight;
   }
-  p.bulkpos = start_label(ph, p);
+  p.bulkpos = ph.method == 1 ? ph.start_layer : start_label(ph, p);
   p.tof = 0;
 }
 
@@ -273,6 +282,46 @@ inline unsigned reflect(Photon &p, uint32_t newlb, Rng &r, const Phase &ph) {
   p.dy *= rr;
   p.dz = copysignf(sqrtf(1 - e), p.dz);
   p.bulkpos = newlb;
+  return 0u;
+}
+
+/* Reflect of bulk method 1: the layers' refractive indices, the layer
+ * changes on transmission.  Returns 1 when reflected. */
+inline unsigned reflect_layers(Photon &p, uint32_t newl, Rng &r, const Phase &ph) {
+  const float n1 = ph.layers[p.bulkpos].n, n2 = ph.layers[newl].n;
+  float rr;
+  float cos_angle_i = fabsf(p.dz);
+  if (n1 == n2) {
+    p.bulkpos = newl;
+    return 0u;
+  }
+  if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
+    p.dz *= -1.0f;
+    return 1u;
+  }
+  if (cos_angle_i == 1.0f) {
+    rr = (n1 - n2) / (n1 + n2);
+    if (r.co() <= rr * rr) {
+      p.dz *= -1.0f;
+      return 1u;
+    }
+    p.bulkpos = newl;
+    return 0u;
+  }
+  float e = (n1 * n1) / (n2 * n2) * (1.0f - cos_angle_i * cos_angle_i);
+  rr = 2 * sqrtf((1.0f - cos_angle_i * cos_angle_i) * (1.0f - e) * e * cos_angle_i * cos_angle_i);
+  e = e + (cos_angle_i * cos_angle_i) * (1.0f - 2.0f * e);
+  rr = e * ((1.0f - e - rr) / ((1.0f - e + rr) * (e + rr)));
+  if (r.co() <= rr) {
+    p.dz *= -1.0f;
+    return 1u;
+  }
+  rr = n1 / n2;
+  e = rr * rr * (1.0f - cos_angle_i * cos_angle_i);
+  p.dx *= rr;
+  p.dy *= rr;
+  p.dz = copysignf(sqrtf(1 - e), p.dz);
+  p.bulkpos = newl;
   return 0u;
 }
 
@@ -482,6 +531,86 @@ unsigned step(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
 }
 
+inline bool in_inclusion(const Phase &ph, const Photon &p) {
+  const oracle_inclusion &c = ph.incl;
+  return ((p.x - c.x) * (p.x - c.x) + (p.y - c.y) * (p.y - c.y) + (p.z - c.z) * (p.z - c.z)) <= (c.r * c.r);
+}
+
+/* One pass of the MCd loop body (bulk method 1).  Kept as the reference
+ * runs it: outside the inclusion the step is 1/mu_t itself, not a sampled
+ * -ln(u)/mu_t (CUDAMCFLtransport.cu:87-89); a scattering-free layer or
+ * inclusion steps 2 cm; the weight drop rounds to nearest and never kills. */
+template <class M>
+unsigned step_layers(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
+  float s;
+  const oracle_layer &L = ph.layers[p.bulkpos];
+  sk.steps++;
+  if (in_inclusion(ph, p)) {
+    if (ph.incl.mutr != FLT_MAX) s = -M::log(r.oc()) * ph.incl.mutr;
+    else s = 2.0f;
+  } else {
+    if (L.mutr != FLT_MAX) s = L.mutr;
+    else s = 2.0f;
+  }
+  int new_layer = (int)p.bulkpos;
+  if (p.z + s * p.dz < L.z_min) {
+    new_layer--;
+    s = (L.z_min - p.z) / p.dz;
+  }
+  if (p.z + s * p.dz >= L.z_max) {
+    new_layer++;
+    s = (L.z_max - p.z) / p.dz;
+  }
+  p.x += p.dx * s;
+  p.y += p.dy * s;
+  p.z += p.dz * s;
+  p.tof += tof_u64((double)(s * L.n) / kCcmfs, ph.tof_wrap);
+  if (p.z > L.z_max) p.z = L.z_max;
+  if (p.z < L.z_min) p.z = L.z_min;
+  if (ph.fhd_on == 1 && fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy && p.z < ph.esp)
+    add_guarded(&sk.fhd[voxel_index(ph, p.x, p.y, p.z)], p.weight, ph.guard);
+  if (new_layer != (int)p.bulkpos) {
+    s = 0.0f;
+    /* Reflect with the layers' indices (CUDAMCFLtransport.cu:636-638) */
+    if (reflect_layers(p, (uint32_t)new_layer, r, ph) == 0u) {
+      if (new_layer == 0) {
+        if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y)
+          add_guarded(&sk.Rd[pixel_index(ph, p.x, p.y)], p.weight, ph.guard);
+        if (ph.time_on && ph.tdet_face == 0) tally_time(ph, p, sk);
+        sk.exit_top += p.weight;
+        p.weight = 0;
+      }
+      if (new_layer > (int)ph.n_layers) {
+        if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y)
+          add_guarded(&sk.Tt[pixel_index(ph, p.x, p.y)], p.weight, ph.guard);
+        if (ph.time_on && ph.tdet_face == 1) tally_time(ph, p, sk);
+        sk.exit_bottom += p.weight;
+        p.weight = 0;
+      }
+    }
+  }
+  if (s > 0.0f) {
+    if (in_inclusion(ph, p)) {
+      const uint32_t w = mcfl_f2u_rn(ph.incl.mua * ph.incl.mutr * mcfl_u2f_rn(p.weight));
+      p.weight -= w;
+      sk.absorbed += w;
+      spin<M>(p, ph.incl.g, r);
+    } else {
+      const oracle_layer &Lc = ph.layers[p.bulkpos];
+      const uint32_t w = mcfl_f2u_rn(Lc.mua * Lc.mutr * mcfl_u2f_rn(p.weight));
+      p.weight -= w;
+      sk.absorbed += w;
+      spin<M>(p, Lc.g, r);
+    }
+  }
+  return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+}
+
+template <class M>
+inline unsigned step_any(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
+  return ph.method == 1 ? step_layers<M>(p, r, ph, sk) : step<M>(p, r, ph, sk);
+}
+
 /* ------------------------------------------------------------------------ */
 
 void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
@@ -517,6 +646,19 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
     ph.prop[i] = Prop{b.mutr, emission ? b.muaf : b.mua, b.g, b.n};
   }
   ph.labels = sim->bulk_info;
+  ph.method = sim->bulk_method == 1 ? 1 : 2;
+  if (ph.method == 1) {
+    ph.n_layers = (unsigned)sim->n_layers;
+    for (unsigned i = 0; i < ph.n_layers + 2 && i < ORACLE_MAX_LAYERS + 2; ++i) ph.layers[i] = sim->layers[i];
+    ph.incl = sim->inclusion;
+    ph.start_layer = 0;
+    /* LaunchPhoton's search for the source's layer (CUDAMCFLtransport.cu:550-560) */
+    for (unsigned nl = 1; nl <= ph.n_layers; ++nl)
+      if (sim->zi < ph.layers[nl].z_max && sim->zi >= ph.layers[nl].z_min) {
+        ph.start_layer = nl;
+        break;
+      }
+  }
   ph.fhd_on = emission ? 0 : sim->fhd_activated;
   ph.xi = sim->xi; ph.yi = sim->yi; ph.zi = sim->zi;
   ph.dir = emission ? 0.0f : sim->dir;
@@ -614,7 +756,7 @@ unsigned long long run_threads(const Phase &ph, unsigned long long nphot, std::v
     Photon p = P[t];
     unsigned ii = active[t] ? 0 : kStepsPerLaunch;
     for (; ii < kStepsPerLaunch; ii++) {
-      if (!step<M>(p, r, ph, s)) {
+      if (!step_any<M>(p, r, ph, s)) {
         if (terminated.fetch_add(1) < limit) {
           launch_photon<M>(p, r, ph, ph.xi, ph.yi, ph.zi);
         } else {
@@ -753,7 +895,7 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
       launch_photon<M, true>(p, r, ph, ph.xi, ph.yi, ph.zi);
     }
     if (ph.launch_rng_reuse && k_in_run < kThreads) r.x = x_at_launch;
-    while (step<M>(p, r, ph, sk)) {
+    while (step_any<M>(p, r, ph, sk)) {
     }
   }
 }
@@ -854,13 +996,14 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
 extern "C" int oracle_run_refstream(const oracle_sim *sim, const char *safeprimes_path, unsigned long long seed_exc,
                                     unsigned long long seed_fl, int math_libm, int nthreads, oracle_result *res) {
   memset(res, 0, sizeof(*res));
-  if (sim->bulk_method != 2 || sim->n_bulks > ORACLE_MAX_BULKS) return -1;
+  if ((sim->bulk_method != 1 && sim->bulk_method != 2) || sim->n_bulks > ORACLE_MAX_BULKS) return -1;
+  if (sim->bulk_method == 1 && (sim->n_layers < 1 || sim->n_layers > ORACLE_MAX_LAYERS)) return -1;
   /* With N <= 32768 the reference's relaunch test compares against
    * N - 32768 computed in unsigned 64-bit arithmetic, which wraps: every
    * photon is replaced and the run never ends (the emission phase stops at
    * its 10000-launch cap only after ~2.6e12 passes).  Refuse such inputs. */
   if (sim->number_of_photons <= kThreads) return -4;
-  if (sim->do_fl_sim != 0 && sim->number_of_photons_per_voxel <= kThreads) return -4;
+  if (sim->do_fl_sim != 0 && sim->bulk_method == 2 && sim->number_of_photons_per_voxel <= kThreads) return -4;
   return math_libm ? refstream_impl<LibmMath>(sim, safeprimes_path, seed_exc, seed_fl, nthreads, res)
                    : refstream_impl<PortableMath>(sim, safeprimes_path, seed_exc, seed_fl, nthreads, res);
 }
@@ -869,7 +1012,9 @@ extern "C" int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipli
                                  unsigned long long seed_exc, unsigned long long seed_fl, int math_libm,
                                  int nthreads, oracle_result *res) {
   memset(res, 0, sizeof(*res));
-  if (sim->bulk_method != 2 || sim->n_bulks > ORACLE_MAX_BULKS || n_multipliers != 32768) return -1;
+  if ((sim->bulk_method != 1 && sim->bulk_method != 2) || sim->n_bulks > ORACLE_MAX_BULKS || n_multipliers != 32768)
+    return -1;
+  if (sim->bulk_method == 1 && (sim->n_layers < 1 || sim->n_layers > ORACLE_MAX_LAYERS)) return -1;
   return math_libm ? photon_impl<LibmMath>(sim, multipliers, seed_exc, seed_fl, res, nthreads)
                    : photon_impl<PortableMath>(sim, multipliers, seed_exc, seed_fl, res, nthreads);
 }

@@ -58,6 +58,19 @@ class CBulk(ctypes.Structure):
     _fields_ = [(n, ctypes.c_float) for n in ("mutr", "mua", "g", "n", "flc", "muaf", "eY", "albedof")]
 
 
+MAX_LAYERS = 100
+
+
+class CLayer(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("z_min", "z_max", "mutr", "mua", "g", "n", "flc", "muaf", "eY",
+                                              "albedof")]
+
+
+class CInclusion(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in ("x", "y", "z", "r", "mutr", "mua", "g", "n", "flc", "muaf", "eY",
+                                              "albedof")]
+
+
 class CSim(ctypes.Structure):
     _fields_ = [
         ("number_of_photons", ctypes.c_ulonglong),
@@ -101,6 +114,9 @@ class CSim(ctypes.Structure):
         ("tdet_face", ctypes.c_int),
         ("tdet_bins", ctypes.c_long),
         ("tdet_max", ctypes.c_ulonglong),
+        ("n_layers", ctypes.c_int),
+        ("layers", CLayer * (MAX_LAYERS + 2)),
+        ("inclusion", CInclusion),
     ]
 
 

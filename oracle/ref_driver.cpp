@@ -322,6 +322,21 @@ extern "C" int ref_parse_mci(const char *mci_path, oracle_sim *out) {
   out->tdet_face = (int)sim->det.temp_rort;
   out->tdet_bins = (long)sim->det.temp_bins;
   out->tdet_max = (unsigned long long)sim->det.max_temp;
+  if (sim->bulk_method == 1) {
+    if (sim->n_layers > ORACLE_MAX_LAYERS) return -3;
+    out->n_layers = (int)sim->n_layers;
+    for (unsigned i = 0; i < sim->n_layers + 2; ++i) {
+      const LayerStruct &L = sim->layers[i];
+      /* the parser sets only n of the outer media; the rest is uninitialised */
+      if (i == 0 || i == sim->n_layers + 1) {
+        out->layers[i] = oracle_layer{0, 0, 0, 0, 0, L.n, 0, 0, 0, 0};
+        continue;
+      }
+      out->layers[i] = oracle_layer{L.z_min, L.z_max, L.mutr, L.mua, L.g, L.n, L.flc, L.muaf, L.eY, L.albedof};
+    }
+    const IncStruct &I = sim->inclusion;
+    out->inclusion = oracle_inclusion{I.x, I.y, I.z, I.r, I.mutr, I.mua, I.g, I.n, I.flc, I.muaf, I.eY, I.albedof};
+  }
   if (sim->bulk_method == 2) {
     if (sim->n_bulks > ORACLE_MAX_BULKS) return -3;
     for (unsigned i = 0; i < sim->n_bulks + 2; ++i) {

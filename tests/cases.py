@@ -197,3 +197,113 @@ def glass_timed_exit(photons=40000, per_voxel=40000) -> Case:
 
 ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere, "mismatch_timed": mismatch_timed,
        "glass_timed_exit": glass_timed_exit}
+
+
+@dataclass
+class LayeredCase:
+    """A layered medium with one spherical inclusion (the reference's bulk
+    method 1), excitation only."""
+    name: str
+    grid: int
+    slabs: list              # per slab: (n, mua, mus, flc, AbsCExi, AbsCEmi, eY, g, thickness)
+    n_up: float
+    n_down: float
+    inclusion: tuple         # (x, y, z, r, n, mua, mus, flc, AbsCExi, AbsCEmi, eY, g)
+    photons: int
+    det: tuple               # dx, dy, nx, ny, x0, y0
+    source: tuple = (0.0, 0.0, 0.0)
+    do_fl: int = 2           # photon hitting density on (the reference runs no emission for layers)
+    temporal: tuple | None = None
+    per_voxel: int = 40000
+
+    def layers(self):
+        return mc.layers_from_mci_columns(self.n_up, self.slabs, self.n_down)
+
+    def incl(self):
+        return mc.inclusion_from_mci_columns(*self.inclusion)
+
+    def start_weight(self) -> int:
+        n1 = np.float64(np.float32(self.n_up))
+        n2 = np.float64(np.float32(self.slabs[0][0]))
+        r = (n1 - n2) / (n1 + n2)
+        return int(np.float64(0xFFFFFFFF) * (1 - r * r))
+
+    def oracle_sim(self):
+        s = pyoracle.CSim()
+        s.bulk_method = 1
+        s.number_of_photons = self.photons
+        s.number_of_photons_per_voxel = self.per_voxel
+        s.grid_size = self.grid
+        lay = self.layers()
+        s.esp = lay[-2].z_max
+        s.do_fl_sim = self.do_fl
+        s.fhd_activated = 1 if self.do_fl in (1, 2) else 0
+        s.det_dx, s.det_dy, s.det_nx, s.det_ny, s.det_x0, s.det_y0 = self.det
+        s.xi, s.yi, s.zi = self.source
+        s.dir = 1.0
+        s.n_bulks = 0
+        s.start_weight = self.start_weight()
+        s.n_layers = len(lay) - 2
+        for i, L in enumerate(lay):
+            s.layers[i] = pyoracle.CLayer(*(getattr(L, f) for f, _ in L._fields_))
+        c = self.incl()
+        s.inclusion = pyoracle.CInclusion(*(getattr(c, f) for f, _ in c._fields_))
+        if self.temporal:
+            x0, y0, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
+            s.do_temp_sim = 1
+            s.tdet_x0, s.tdet_y0, s.tdet_nx, s.tdet_ny = x0, y0, tnx, tny
+            s.tdet_sep_x, s.tdet_sep_y, s.tdet_r, s.tdet_face = sx, sy, r, face
+            s.tdet_bins, s.tdet_max = bins, tmax
+        return s
+
+    def engine_medium(self, ctx):
+        return ctx.medium_layered(self.layers(), self.incl(), self.grid)
+
+    def run_desc(self, seed_exc, seed_fl, photons=None):
+        dx, dy, nx, ny, x0, y0 = self.det
+        return mc.run_desc(photons or self.photons, source=self.source, det=mc.Detector(x0, y0, dx, dy, nx, ny),
+                           fluence=1 if self.do_fl in (1, 2) else 0, seed_exc=seed_exc, seed_fl=seed_fl,
+                           start_weight=self.start_weight(), tdet=self.temporal)
+
+    def write_mci(self, d: str) -> str:
+        dx, dy, dnx, dny, x0, y0 = self.det
+        lines = ["# layered test medium " + self.name, "1.0 # file version", "1 # runs", "1 # method",
+                 f"{self.name}-out A", f"{self.photons} # photons", f"{self.per_voxel} # photons per voxel",
+                 f"{self.grid} # grid", f"{self.do_fl} # fluorescence", f"{dx} {dy}", f"{dnx} {dny}", f"{x0} {y0}",
+                 "{} {} {}".format(*self.source)]
+        if self.temporal:
+            x0t, y0t, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
+            lines += ["1 # temporal", f"{x0t} {y0t}", f"{tnx} {tny}", f"{sx} {sy}", f"{r}", f"{face}", f"{bins}",
+                      f"{tmax}"]
+        else:
+            lines += ["0 # temporal", "0 0", "1 1", "1 1", "0.5", "0", "10", "1000"]
+        lines += [f"{len(self.slabs)} # layers", f"{self.n_up}"]
+        lines += [" ".join(repr(float(v)) for v in sl) for sl in self.slabs]
+        lines += [f"{self.n_down}", " ".join(repr(float(v)) for v in self.inclusion)]
+        path = os.path.join(d, self.name + ".mci")
+        with open(path, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        return path
+
+
+def layered(photons=40000, per_voxel=40000) -> LayeredCase:
+    """Two slabs with an index step between them, an absorbing inclusion
+    across the interface, off-centre beam."""
+    return LayeredCase("layered", 10,
+                       [(1.4, 0.1, 90.0, 0.0, 0.0, 0.0, 0.0, 0.9, 0.3),
+                        (1.33, 0.3, 60.0, 0.0, 0.0, 0.0, 0.0, 0.8, 0.5)],
+                       1.0, 1.0, (0.1, -0.05, 0.35, 0.2, 1.4, 0.8, 70.0, 0.0, 0.0, 0.0, 0.0, 0.85),
+                       photons, (0.05, 0.05, 40, 40, 0.0, 0.0), (0.05, 0.02, 0.0), per_voxel=per_voxel)
+
+
+def layered_timed_exit(photons=40000, per_voxel=40000) -> LayeredCase:
+    """layered with a scattering-free inclusion and time-resolved detectors
+    on the exit face."""
+    c = layered(photons, per_voxel)
+    c.name = "layered_timed_exit"
+    c.inclusion = (0.0, 0.0, 0.5, 0.15, 1.5, 0.05, 0.0, 0.0, 0.0, 0.0, 0.0, 0.9)
+    c.temporal = (0.0, 0.0, 2, 2, 0.3, 0.3, 0.2, 1, 30, 300000)
+    return c
+
+
+LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}

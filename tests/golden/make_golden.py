@@ -30,6 +30,8 @@ FIXTURES = {
     "glass": dict(photons=36000, per_voxel=33000),
     "mismatch_timed": dict(photons=36000, per_voxel=33000),
     "glass_timed_exit": dict(photons=36000, per_voxel=33000),
+    "layered": dict(photons=36000, per_voxel=33000),
+    "layered_timed_exit": dict(photons=36000, per_voxel=33000),
 }
 
 
@@ -41,7 +43,7 @@ def main():
         sp = os.path.join(d, "safeprimes_base32.txt")
         o.write_safeprimes(sp, 32769)
         for name, kw in FIXTURES.items():
-            case = cases.ALL[name](**kw)
+            case = {**cases.ALL, **cases.LAYERED}[name](**kw)
             mci = case.write_mci(d)
             r = ref.run_mci(mci, sp, *SEEDS)
             out = os.path.join(HERE, f"ref_{name}.npz")
@@ -49,7 +51,8 @@ def main():
             np.savez_compressed(out, Rd=r.Rd, Tt=r.Tt, fhd=r.fhd, flR=r.flR, flT=r.flT, **extra,
                                 photons_exc=r.photons_exc, photons_fl=r.photons_fl, fl_voxels=r.fl_voxels,
                                 seeds=np.array(SEEDS, dtype=np.uint64),
-                                mci=open(mci).read(), bulk=open(mci.replace(".mci", ".bulk")).read())
+                                mci=open(mci).read(),
+                                bulk=open(mci.replace(".mci", ".bulk")).read() if hasattr(case, "labels") else "")
             print(out, r.photons_exc, r.photons_fl, r.fl_voxels)
 
 

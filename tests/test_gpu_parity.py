@@ -233,3 +233,74 @@ def test_bad_inputs_fail_with_status(gpu_ctx):
         assert e.value.code == mc.E_CAPPED
     finally:
         gpu_ctx.set_option("step_cap", 1 << 24)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(cases.LAYERED))
+def test_layered_exact_kernel_bit_identical_to_oracle(name, gpu_ctx, oracle, table32768):
+    """Layered media (the reference's bulk method 1): R/T images, photon
+    hitting density, weight accounting and time-resolved tallies bit for bit."""
+    case = cases.LAYERED[name](photons=30000)
+    ref = oracle.run_photon(case.oracle_sim(), table32768, 13, 14, libm=False)
+    med = case.engine_medium(gpu_ctx)
+    res = gpu_ctx.run(med, case.run_desc(13, 14))
+    med.free()
+    assert res.fhd.size == ref.fhd.size and ref.Rd.sum() > 0
+    _compare(res, ref, emission=False)
+
+
+@pytest.mark.gpu
+def test_run_mci_on_a_layered_medium(mcfl_lib, oracle, table32768, tmp_path):
+    """A bulk-method-1 .mci through mcfl_run_mci: the reference's files, the
+    excitation tallies equal to the oracle's (same photon streams, the .mci
+    path's launch-number reuse), emission images of zeros as the reference
+    writes them for layered media."""
+    import ctypes
+    import os
+    case = cases.layered(photons=40000)
+    case.do_fl = 1
+    mci = case.write_mci(str(tmp_path))
+    o = case.oracle_sim()
+    o.launch_rng_reuse = 1
+    ref = oracle.run_photon(o, table32768, 4321, 4322, libm=False)
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        assert mcfl_lib.mcfl_run_mci(os.path.basename(mci).encode(), ctypes.c_ulonglong(4321)) == 0
+        for suffix in ("_param.dat", "_Refl.dat", "_Trans.dat", "_PHD-Ascii.dat", "_FlR.dat", "_FlT.dat"):
+            assert os.path.getsize(f"layered-out{suffix}") > 0
+        assert not np.loadtxt("layered-out_FlR.dat").any()
+        refl = np.loadtxt("layered-out_Refl.dat")
+        scale = float(0xFFFFFFFF) * 40000 * np.float32(0.05) * np.float32(0.05)
+        expect = ref.Rd[:40 * 40].reshape(40, 40).astype(np.float64) / scale
+        assert np.allclose(refl, expect, rtol=1e-6, atol=0)
+    finally:
+        os.chdir(cwd)
+
+
+@pytest.mark.gpu
+def test_run_mci_runs_every_simulation_of_a_file(mcfl_lib, tmp_path):
+    """A two-run .mci (voxelized, then layered): run i is seeded from
+    seed + 2i and writes its own files, identical to running it alone."""
+    import ctypes
+    import os
+    a = cases.tiny(photons=40000, per_voxel=33000)
+    a.do_fl = 0
+    b = cases.layered(photons=40000)
+    b.do_fl = 0
+    la = open(a.write_mci(str(tmp_path))).read().splitlines()
+    lb = open(b.write_mci(str(tmp_path))).read().splitlines()
+    (tmp_path / "multi.mci").write_text("\n".join(["# two runs", "1.0 # file version", "2 # runs"] + la[3:] +
+                                                  lb[3:]) + "\n")
+    cwd = os.getcwd()
+    os.chdir(tmp_path)
+    try:
+        assert mcfl_lib.mcfl_run_mci(b"multi.mci", ctypes.c_ulonglong(9)) == 0
+        both = {f: open(f).read() for f in ("tiny-out_Refl.dat", "tiny-out_Trans.dat", "layered-out_Refl.dat",
+                                            "layered-out_Trans.dat")}
+        assert mcfl_lib.mcfl_run_mci(b"tiny.mci", ctypes.c_ulonglong(9)) == 0
+        assert mcfl_lib.mcfl_run_mci(b"layered.mci", ctypes.c_ulonglong(11)) == 0
+        for f, text in both.items():
+            assert open(f).read() == text, f
+    finally:
+        os.chdir(cwd)

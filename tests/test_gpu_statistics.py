@@ -117,6 +117,38 @@ def test_time_resolved_detectors_agree_with_reference_streams(math, face, oracle
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("math", [mc.MATH_EXACT, mc.MATH_FAST])
+def test_layered_medium_agrees_with_reference_streams(math, oracle, safeprimes_file):
+    """Layered medium (bulk method 1) with time-resolved detectors: engine
+    against the reference-stream restatement, R/T, fluence and time bins
+    within 3 sigma."""
+    nthreads = os.cpu_count() or 1
+    case = cases.layered_timed_exit(photons=150_000)
+    sim = case.oracle_sim()
+    ref = [oracle.run_refstream(sim, safeprimes_file, 6000 + b, 1, libm=True, nthreads=nthreads) for b in range(B)]
+    ctx = mc.Context(math=math)
+    med = case.engine_medium(ctx)
+    eng = []
+    for b in range(B):
+        rd = case.run_desc(900 + b, 1)
+        rd.launch_rng_reuse = 1
+        eng.append(ctx.run(med, rd))
+    med.free()
+    ctx.close()
+    xy = case.det[2] * case.det[3]
+    for k in ("Rd", "Tt", "fhd"):
+        a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in eng])
+        b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ref])
+        stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+    stats.gate(np.stack([r.time_xyt.ravel().astype(float) for r in eng]),
+               np.stack([r.time_xyt.astype(float) for r in ref]), frac_max=0.02, min_rel=1e-2)
+    w0 = case.start_weight()
+    fe = _fractions(eng, w0)
+    for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
+        stats.scalar_gate(fe[k], [r.balance[i] / (r.photons_exc * w0) for r in ref])
+
+
+@pytest.mark.gpu
 def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_file):
     """Integrated R, T and absorbed fraction of the fast kernel against the
     reference streams on 1.6e7 reference photons: within 3 sigma and 0.1 %

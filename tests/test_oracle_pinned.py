@@ -21,7 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 GOLDEN = os.path.join(HERE, "golden")
 FIXTURES = {"tiny": dict(photons=40000, per_voxel=33000), "mismatch": dict(photons=36000, per_voxel=33000),
             "glass": dict(photons=36000, per_voxel=33000), "mismatch_timed": dict(photons=36000, per_voxel=33000),
-            "glass_timed_exit": dict(photons=36000, per_voxel=33000)}
+            "glass_timed_exit": dict(photons=36000, per_voxel=33000), "layered": dict(photons=36000, per_voxel=33000),
+            "layered_timed_exit": dict(photons=36000, per_voxel=33000)}
+BUILDERS = {**cases.ALL, **cases.LAYERED}
 
 
 def _same(a, b):
@@ -32,7 +34,7 @@ def _same(a, b):
 @pytest.mark.parametrize("name", sorted(FIXTURES))
 def test_port_reproduces_reference_golden(name, oracle, safeprimes_file, tmp_path):
     g = np.load(os.path.join(GOLDEN, f"ref_{name}.npz"))
-    case = cases.ALL[name](**FIXTURES[name])
+    case = BUILDERS[name](**FIXTURES[name])
     # the fixture was made from the .mci this case writes
     mci = case.write_mci(str(tmp_path))
     assert open(mci).read() == str(g["mci"])
@@ -49,9 +51,9 @@ def test_port_reproduces_reference_golden(name, oracle, safeprimes_file, tmp_pat
         assert r.time_xyt is None
 
 
-@pytest.mark.parametrize("name", ["tiny", "glass", "glass_timed_exit"])
+@pytest.mark.parametrize("name", ["tiny", "glass", "glass_timed_exit", "layered_timed_exit"])
 def test_port_reproduces_reference_build_live(name, oracle, ref_oracle, safeprimes_file, tmp_path):
-    case = cases.ALL[name](photons=34000, per_voxel=32800)
+    case = BUILDERS[name](photons=34000, per_voxel=32800)
     mci = case.write_mci(str(tmp_path))
     sim = ref_oracle.parse_mci(mci)
     a = ref_oracle.run_mci(mci, safeprimes_file, 4242, 99)
@@ -80,11 +82,39 @@ def test_case_builder_matches_reference_parser(name, ref_oracle, tmp_path):
     a, b = _sim_fields(parsed), _sim_fields(built)
     for k in ("number_of_photons", "number_of_photons_per_voxel", "n_bulks", "start_weight", "grid_size", "esp",
               "xi", "yi", "zi", "dir", "fhd_activated", "do_fl_sim", "det_dx", "det_dy", "det_nx", "det_ny",
-              "det_x0", "det_y0", "bulks"):
+              "det_x0", "det_y0", "bulks") + (TEMPORAL if case.temporal else ("do_temp_sim",)):
         assert a[k] == b[k], k
     n = int(np.prod(case.labels.shape))
     pa = np.ctypeslib.as_array(parsed.bulk_info, shape=(n,))
     assert np.array_equal(pa, case.labels.ravel().astype(np.int16))
+
+
+TEMPORAL = ("do_temp_sim", "tdet_x0", "tdet_y0", "tdet_nx", "tdet_ny", "tdet_sep_x", "tdet_sep_y", "tdet_r",
+            "tdet_face", "tdet_bins", "tdet_max")
+
+
+def _floats(st):
+    return [np.float32(getattr(st, f)).tobytes() for f, _ in st._fields_]
+
+
+@pytest.mark.parametrize("name", sorted(cases.LAYERED))
+def test_layered_case_builder_matches_reference_parser(name, ref_oracle, tmp_path):
+    """Layered media: the layer table, the inclusion and the temporal
+    detectors built in Python equal what the reference's parser reads from
+    the .mci text (outer media: n only, the parser leaves the rest unset)."""
+    case = cases.LAYERED[name]()
+    mci = case.write_mci(str(tmp_path))
+    parsed = ref_oracle.parse_mci(mci)
+    built = case.oracle_sim()
+    for k in ("number_of_photons", "start_weight", "grid_size", "esp", "xi", "yi", "zi", "dir", "fhd_activated",
+              "do_fl_sim", "det_dx", "det_dy", "det_nx", "det_ny", "det_x0", "det_y0", "n_layers") + \
+            (TEMPORAL if case.temporal else ("do_temp_sim",)):
+        assert getattr(parsed, k) == getattr(built, k), k
+    n = parsed.n_layers
+    for i in range(1, n + 1):
+        assert _floats(parsed.layers[i]) == _floats(built.layers[i]), i
+    assert parsed.layers[0].n == built.layers[0].n and parsed.layers[n + 1].n == built.layers[n + 1].n
+    assert _floats(parsed.inclusion) == _floats(built.inclusion)
 
 
 def _product_parse(lib, mci):

@@ -421,10 +421,10 @@ class Context:
         d = LayeredDesc(len(layers) - 2, ctypes.cast(arr, ctypes.POINTER(Layer)), inclusion, int(grid_size))
         h = ctypes.c_void_p()
         check(load().mcfl_medium_create_layered(self.handle, ctypes.byref(d), ctypes.byref(h)))
-        esp = float(np.float32(layers[-2].z_max))
+        esp = np.float32(layers[-2].z_max)
         g = np.float32(grid_size)
-        n = int(np.rint(np.float32(np.float32(4) * np.float32(esp)) * g))
-        return Medium(self, h, (int(np.float32(esp) * g), n, n), [arr])
+        n = int(np.float32(np.float32(4) * esp) * g)
+        return Medium(self, h, (int(esp * g), n, n), [arr])
 
     def medium_from_simulation(self, sim: Simulation) -> Medium:
         h = ctypes.c_void_p()

@@ -312,7 +312,7 @@ extern "C" int mcfl_medium_create_layered(mcfl_ctx *c, const mcfl_layered_desc *
   m->esp = esp;
   m->hx = m->hy = 2 * esp;
   m->gx = m->gy = m->gz = g;
-  m->nx = m->ny = (int)lrintf(4 * esp * g);
+  m->nx = m->ny = (int)(4 * esp * g); /* the size main allocates, CUDAMCFLmain.cu:340-342 */
   m->nz = (int)(esp * g);
   if (m->nx <= 0 || m->nz <= 0 || (unsigned long long)m->nx * m->ny * m->nz >= 0xFFFFFFFFull) {
     delete m;

@@ -269,6 +269,12 @@ extern "C" int mcfl_read_simulation_data(const char *filename, mcfl_simulation *
       I.albedof = ft[6] / (ft[7] * ft[8] + ft[6]);
       n1 = s.layers[0].n;
       n2 = s.layers[1].n;
+      /* the photon-hitting-density grid main sizes for either method
+       * (CUDAMCFLmain.cu:340-342) */
+      const float g = (float)s.grid_size;
+      s.num_x = (int)(4 * s.esp * g);
+      s.num_y = (int)(4 * s.esp * g);
+      s.num_z = (int)(s.esp * g);
     } else if (s.bulk_method == 2) {
       if (!read_ints(1, it, f)) return parse_error(f, "number of bulk descriptors");
       if (it[0] < 1 || it[0] > MCFL_MAX_BULKS) return parse_error(f, "number of bulk descriptors");

@@ -136,11 +136,14 @@ def _ref_sample(path):
     return p
 
 
-@pytest.mark.parametrize("src", ["case:tiny", "case:mismatch", "case:glass", "ref:sample2.mci"])
+@pytest.mark.parametrize("src", ["case:tiny", "case:mismatch", "case:glass", "case:mismatch_timed", "lay:layered",
+                                 "lay:layered_timed_exit", "ref:sample2.mci"])
 def test_product_parser_matches_reference_parser(src, mcfl_lib, ref_oracle, tmp_path):
     import cudamcfl_gb300 as mc
     if src.startswith("case:"):
         mci = cases.ALL[src[5:]]().write_mci(str(tmp_path))
+    elif src.startswith("lay:"):
+        mci = cases.LAYERED[src[4:]]().write_mci(str(tmp_path))
     else:
         mci = _ref_sample(src[4:])
     ref = ref_oracle.parse_mci(mci)
@@ -155,6 +158,24 @@ def test_product_parser_matches_reference_parser(src, mcfl_lib, ref_oracle, tmp_
         for k, rk in (("dx", "det_dx"), ("dy", "det_dy"), ("x0", "det_x0"), ("y0", "det_y0")):
             assert np.float32(getattr(s.det, k)).tobytes() == np.float32(getattr(ref, rk)).tobytes(), k
         assert (s.det.nx, s.det.ny) == (ref.det_nx, ref.det_ny)
+        if ref.do_temp_sim:
+            for k, rk in (("x0_temp_det", "tdet_x0"), ("y0_temp_det", "tdet_y0"), ("x_temp_sepdets", "tdet_sep_x"),
+                          ("y_temp_sepdets", "tdet_sep_y"), ("temp_det_r", "tdet_r")):
+                assert np.float32(getattr(s.det, k)).tobytes() == np.float32(getattr(ref, rk)).tobytes(), k
+            assert (s.det.x_temp_numdets, s.det.y_temp_numdets, s.det.temp_rort, s.det.temp_bins, s.det.max_temp) == \
+                (ref.tdet_nx, ref.tdet_ny, ref.tdet_face, ref.tdet_bins, ref.tdet_max)
+        if s.bulk_method == 1:
+            assert s.n_layers == ref.n_layers
+            for i in range(1, s.n_layers + 1):
+                for f, _ in mc.Layer._fields_:
+                    assert np.float32(getattr(s.layers[i], f)).tobytes() == \
+                        np.float32(getattr(ref.layers[i], f)).tobytes(), (i, f)
+            for i in (0, s.n_layers + 1):
+                assert np.float32(s.layers[i].n) == np.float32(ref.layers[i].n)
+            for f, _ in mc.Inclusion._fields_:
+                assert np.float32(getattr(s.inclusion, f)).tobytes() == \
+                    np.float32(getattr(ref.inclusion, f)).tobytes(), f
+            return
         for i in range(s.n_bulks + 2):
             for f, _ in mc.Bulk._fields_:
                 assert np.float32(getattr(s.bulks[i], f)).tobytes() == \

@@ -118,7 +118,7 @@ class RunDesc(ctypes.Structure):
     _fields_ = [("photons", ctypes.c_ulonglong), ("photons_per_voxel", ctypes.c_uint), ("fluence", ctypes.c_int),
                 ("seed_exc", ctypes.c_ulonglong), ("seed_fl", ctypes.c_ulonglong), ("start_weight", ctypes.c_uint),
                 ("source", Source), ("det", Detector), ("launch_rng_reuse", ctypes.c_int),
-                ("tdet", TimeDetectors)]
+                ("tdet", TimeDetectors), ("photon_offset", ctypes.c_ulonglong)]
 
 
 _u64p = ctypes.POINTER(ctypes.c_ulonglong)

@@ -140,6 +140,7 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
     j.T = d_T + (size_t)i * xy;
     j.stats = d_stats + (size_t)i * MCFL_ST_COUNT;
     j.key = mcfl_stream_key(r.seed_exc, 0);
+    j.rng_offset = r.photon_offset;
     j.launch_rng_reuse = r.launch_rng_reuse ? 1u : 0u;
     j.ticket_begin = tickets;
     j.photons = r.photons;

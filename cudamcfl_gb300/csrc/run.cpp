@@ -303,6 +303,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   je.fhd = fluence ? c->fhd.as<unsigned long long>() : nullptr;
   je.stats = c->stats.as<unsigned long long>();
   je.key = mcfl_stream_key(run->seed_exc, 0);
+  je.rng_offset = run->photon_offset;
   je.photons = run->photons;
   je.launch_rng_reuse = run->launch_rng_reuse ? 1u : 0u;
   if (timed) {
@@ -501,6 +502,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     j.T = c->bT.as<unsigned long long>() + i * xy;
     j.stats = c->bstats.as<unsigned long long>() + i * (size_t)MCFL_ST_COUNT;
     j.key = mcfl_stream_key(runs[i].seed_exc, 0);
+    j.rng_offset = runs[i].photon_offset;
     j.launch_rng_reuse = runs[i].launch_rng_reuse ? 1u : 0u;
     j.ticket_begin = schedule == MCFL_SCHEDULE_BATCHED ? tickets : 0;
     j.photons = runs[i].photons;

@@ -156,7 +156,7 @@ int mcfl_server::upload(Request &r) {
   j.stats = r.stats.as<unsigned long long>();
   j.key = mcfl_stream_key(r.run.seed_exc, 0);
   j.launch_rng_reuse = r.run.launch_rng_reuse ? 1u : 0u;
-  j.rng_offset = 0;
+  j.rng_offset = r.run.photon_offset;
   j.ticket_begin = r.ticket_begin;
   j.photons = r.run.photons;
   return MCFL_OK;

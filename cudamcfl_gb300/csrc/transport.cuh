@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   };
   auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * blockDim.x + tib] += v; };
 
-  if (L.max_iters && L.saved) {
+  if (!kUniform && L.max_iters && L.saved) {
     const McflSaved sv = L.saved[gtid];
     if (sv.alive) {
       job = sv.job;
@@ -667,7 +667,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   }
 
   for (uint32_t it = 0;; ++it) {
-    if (L.max_iters && it >= L.max_iters) break;
+    /* single-medium launches always run to the end of their tickets */
+    if (!kUniform && L.max_iters && it >= L.max_iters) break;
     /* one vote per pass while every lane carries a photon */
     if (__ballot_sync(kFull, !alive)) {
     const bool need = !alive && !exhausted;
@@ -805,10 +806,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       s = MCFL_C(100.0);
       new_bulk = move_to_first_boundary<kTime>(p, m, s);
     }
+    Rec cur = c; /* the record of the photon's label after the boundary */
     if (new_bulk != p.label) {
       const Rec cn = kUniform ? Rec{s_lab[2 * new_bulk], s_lab[2 * new_bulk + 1]} : load_rec(m, new_bulk);
       if (reflect(p, c.b.w, cn.b.w, r)) {
         p.label = new_bulk;
+        cur = cn;
         if (!kUniform) rc = cn;
       }
     }
@@ -832,7 +835,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       s = MCFL_C(0.0);
     }
     if (s > MCFL_C(0.0)) {
-      const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
+      const Rec c2 = cur;
       const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
       if (w > 0u) {
         p.weight -= w;
@@ -868,7 +871,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   }
   if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
 
-  if (L.max_iters && L.saved) {
+  if (!kUniform && L.max_iters && L.saved) {
     McflSaved sv;
     sv.alive = alive ? 1u : 0u;
     if (alive) {
@@ -927,6 +930,7 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
   if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
 #endif
   if (L->max_iters && L->time_on) return cudaErrorNotSupported; /* parked photons carry no time of flight */
+  if (L->max_iters && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
   if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
     return cudaErrorInvalidValue;
   const int v = L->med.layered ? (L->time_on ? 5 : 4)

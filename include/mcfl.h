@@ -265,6 +265,11 @@ typedef struct mcfl_run_desc {
    * numbers (default of the engine API; the .mci path sets 1). */
   int launch_rng_reuse;
   mcfl_time_detectors tdet; /* mcfl_run only; zero: none */
+  /* Index of the excitation run's first photon in the stream family of
+   * seed_exc: photon k of the run draws stream photon_offset + k, so runs
+   * over disjoint index ranges of one seed (on one GPU or several) sum to the
+   * run over their union bit for bit.  0 for a whole run. */
+  unsigned long long photon_offset;
 } mcfl_run_desc;
 
 #define MCFL_NSTATS 9

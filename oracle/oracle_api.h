@@ -105,6 +105,9 @@ typedef struct oracle_sim {
   int n_layers;
   oracle_layer layers[ORACLE_MAX_LAYERS + 2];
   oracle_inclusion inclusion;
+  /* photon only: index of the excitation run's first photon in its stream
+   * family (runs over disjoint index ranges sum to the run over their union) */
+  unsigned long long photon_offset;
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);

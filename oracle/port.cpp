@@ -876,10 +876,10 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
 
 template <class M>
 void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint64_t k0, uint64_t k1, Sink &sk,
-                      const uint32_t *vox, const uint64_t *voxq, unsigned nv) {
+                      const uint32_t *vox, const uint64_t *voxq, unsigned nv, uint64_t offset = 0) {
   for (uint64_t k = k0; k < k1; ++k) {
     Rng r;
-    mcfl_photon_stream(key, k, table, &r.x, &r.a);
+    mcfl_photon_stream(key, offset + k, table, &r.x, &r.a);
     const uint64_t x_at_launch = r.x;
     const uint64_t k_in_run = vox ? k % nv : k;
     Photon p;
@@ -904,9 +904,9 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
  * independent of the thread count. */
 template <class M>
 void run_photon_threads(const Phase &ph, uint64_t key, const uint32_t *table, uint64_t n, Sink &sk,
-                        const uint32_t *vox, const uint64_t *voxq, unsigned nv, int nthreads) {
+                        const uint32_t *vox, const uint64_t *voxq, unsigned nv, int nthreads, uint64_t offset = 0) {
   if (nthreads <= 1 || n < 4096) {
-    run_photon_range<M>(ph, key, table, 0, n, sk, vox, voxq, nv);
+    run_photon_range<M>(ph, key, table, 0, n, sk, vox, voxq, nv, offset);
     return;
   }
   std::vector<Sink> local(nthreads, sk);
@@ -916,7 +916,7 @@ void run_photon_threads(const Phase &ph, uint64_t key, const uint32_t *table, ui
   for (int w = 0; w < nthreads; ++w)
     pool.emplace_back([&, w] {
       const uint64_t k0 = std::min<uint64_t>(n, (uint64_t)w * chunk), k1 = std::min<uint64_t>(n, k0 + chunk);
-      run_photon_range<M>(ph, key, table, k0, k1, local[w], vox, voxq, nv);
+      run_photon_range<M>(ph, key, table, k0, k1, local[w], vox, voxq, nv, offset);
     });
   for (auto &t : pool) t.join();
   for (auto &l : local) {
@@ -947,7 +947,8 @@ int photon_impl(const oracle_sim *sim, const uint32_t *table, uint64_t seed_exc,
   std::vector<float> tpx, tpy;
   setup_time(sim, ph, tpx, tpy, res, sk);
   const unsigned long long N = sim->number_of_photons;
-  run_photon_threads<M>(ph, mcfl_stream_key(seed_exc, 0), table, N, sk, nullptr, nullptr, 1, nthreads);
+  run_photon_threads<M>(ph, mcfl_stream_key(seed_exc, 0), table, N, sk, nullptr, nullptr, 1, nthreads,
+                        sim->photon_offset);
   res->photons_exc = N;
   res->steps_exc = sk.steps;
   res->balance[0] = sk.absorbed; res->balance[1] = sk.exit_top; res->balance[2] = sk.exit_bottom;

@@ -117,6 +117,7 @@ class CSim(ctypes.Structure):
         ("n_layers", ctypes.c_int),
         ("layers", CLayer * (MAX_LAYERS + 2)),
         ("inclusion", CInclusion),
+        ("photon_offset", ctypes.c_ulonglong),
     ]
 
 

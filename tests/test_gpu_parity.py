@@ -304,3 +304,116 @@ def test_run_mci_runs_every_simulation_of_a_file(mcfl_lib, tmp_path):
             assert open(f).read() == text, f
     finally:
         os.chdir(cwd)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("photons,per_voxel", [(1, 1), (31, 1), (33, 2), (1000, 3)])
+def test_ragged_photon_counts_bit_identical(photons, per_voxel, gpu_ctx, oracle, table32768):
+    """Budgets far below one photon per thread and not a multiple of a warp:
+    one photon, a part of a warp, a warp and one."""
+    case = cases.mismatch(photons=photons, per_voxel=per_voxel)
+    ref = oracle.run_photon(case.oracle_sim(), table32768, 3, 4, libm=False)
+    med = case.engine_medium(gpu_ctx)
+    res = gpu_ctx.run(med, case.run_desc(3, 4))
+    med.free()
+    _compare(res, ref)
+    assert res.stats_exc["done"] == photons
+
+
+@pytest.mark.gpu
+def test_hundred_labels_bit_identical(gpu_ctx, oracle, table32768):
+    """100 bulk descriptors (the oracle's maximum; the engine's shared label
+    table holds 256) scattered over the grid."""
+    rng = np.random.default_rng(7)
+    nz, ny, nx = 20, 40, 40
+    lab = rng.integers(1, 101, size=(nz, ny, nx)).astype(np.uint8)
+    bulks = [mc.outer_bulk(1.0)]
+    for i in range(100):
+        bulks.append(mc.bulk_from_mci_columns(1.3 + 0.002 * i, rng.uniform(0.05, 1.0), rng.uniform(20, 120),
+                                              1.0 if i % 3 == 0 else 0.0, 0.05, 0.02, 0.1, rng.uniform(0.6, 0.95)))
+    bulks.append(mc.outer_bulk(1.0))
+    det = mc.Detector(0.0, 0.0, 0.05, 0.05, 32, 32)
+    from oracle import pyoracle
+    sim = pyoracle.sim_from_arrays(lab, bulks, half_x=1.0, half_y=1.0, thickness=0.5, vox_per_cm=[20.0, 20.0, 40.0],
+                                   photons=20000, per_voxel=5, det=(0.05, 0.05, 32, 32, 0.0, 0.0))
+    ref = oracle.run_photon(sim, table32768, 17, 18, libm=False)
+    med = gpu_ctx.medium(lab, bulks, vox_per_cm=(20.0, 20.0, 40.0), half_x=1.0, half_y=1.0, thickness=0.5)
+    res = gpu_ctx.run(med, mc.run_desc(20000, det=det, photons_per_voxel=5, fluence=1, seed_exc=17, seed_fl=18,
+                                       start_weight=sim.start_weight))
+    med.free()
+    _compare(res, ref)
+    assert ref.fl_voxels > 0
+
+
+@pytest.mark.gpu
+def test_large_grid_bit_identical(gpu_ctx, oracle, table32768):
+    """A 1024 x 1024 x 64 grid (67M voxels): the index arithmetic at the
+    sizes of the large precision-study medium."""
+    nz, ny, nx = 64, 1024, 1024
+    lab = np.ones((nz, ny, nx), dtype=np.uint8)
+    lab[8:40, 400:600, 450:650] = 2
+    bulks = [mc.outer_bulk(1.0), mc.bulk_from_mci_columns(1.4, 0.1, 30.0, g=0.9),
+             mc.bulk_from_mci_columns(1.4, 0.3, 50.0, 1.0, 0.05, 0.02, 0.1, 0.85), mc.outer_bulk(1.0)]
+    det = mc.Detector(0.0, 0.0, 0.1, 0.1, 50, 50)
+    from oracle import pyoracle
+    sim = pyoracle.sim_from_arrays(lab, bulks, half_x=2.56, half_y=2.56, thickness=0.64,
+                                   vox_per_cm=[200.0, 200.0, 100.0], photons=4000, per_voxel=0,
+                                   det=(0.1, 0.1, 50, 50, 0.0, 0.0), do_fl=2)
+    ref = oracle.run_photon(sim, table32768, 5, 6, libm=False)
+    med = gpu_ctx.medium(lab, bulks, vox_per_cm=(200.0, 200.0, 100.0), half_x=2.56, half_y=2.56, thickness=0.64)
+    res = gpu_ctx.run(med, mc.run_desc(4000, det=det, fluence=1, seed_exc=5, seed_fl=6,
+                                       start_weight=sim.start_weight))
+    med.free()
+    _compare(res, ref, emission=False)
+
+
+@pytest.mark.gpu
+def test_time_and_layer_inputs_fail_with_status(gpu_ctx):
+    case = cases.mismatch_timed()
+    med = case.engine_medium(gpu_ctx)
+    rd = case.run_desc(1, 2)
+    rd.tdet.bins = 0
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.run(med, rd)
+    assert e.value.code == mc.E_ARG
+    rd = case.run_desc(1, 2)
+    rd.tdet.face = 2
+    with pytest.raises(mc.McflError):
+        gpu_ctx.run(med, rd)
+    med.free()
+    lc = cases.layered()
+    lm = lc.engine_medium(gpu_ctx)
+    rd = lc.run_desc(1, 2)
+    rd.source.z = 5.0  # below every slab
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.run(lm, rd)
+    assert e.value.code == mc.E_ARG
+    rd = lc.run_desc(1, 2)
+    rd.photons_per_voxel = 100  # no emission in layered media
+    with pytest.raises(mc.McflError):
+        gpu_ctx.run(lm, rd)
+    lm.free()
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.medium_layered(lc.layers()[:1] + lc.layers()[-1:], lc.incl(), 10)  # no slab
+    assert e.value.code == mc.E_RANGE
+
+
+@pytest.mark.gpu
+def test_photon_offset_shards_sum_to_the_whole_run(gpu_ctx):
+    """Runs over disjoint photon index ranges of one seed (photon_offset) sum
+    to the run over their union, bit for bit: the decomposition a multi-GPU
+    run would use."""
+    case = cases.mismatch(photons=30000, per_voxel=0)
+    case.do_fl = 2
+    med = case.engine_medium(gpu_ctx)
+    whole = gpu_ctx.run(med, case.run_desc(7, 8))
+    parts = []
+    for off, n in ((0, 7000), (7000, 23000)):
+        rd = case.run_desc(7, 8, photons=n)
+        rd.photon_offset = off
+        parts.append(gpu_ctx.run(med, rd))
+    med.free()
+    for k in ("Rd", "Tt", "fhd"):
+        assert np.array_equal(getattr(parts[0], k) + getattr(parts[1], k), getattr(whole, k)), k
+    for k in STAT_ORDER + ("steps", "done"):
+        assert parts[0].stats_exc[k] + parts[1].stats_exc[k] == whole.stats_exc[k], k

@@ -400,6 +400,31 @@ def main():
                         f"log-uniform budgets 1e6..5e7 scaled by {scale} ({tot:.3g} photons), own R/T images each",
             "batched_photons_per_s": tot / (ms_b / 1e3), "plain_photons_per_s": tot / (ms_p / 1e3),
             "batched_over_plain": ms_p / ms_b, "batched_ms": ms_b, "plain_ms": ms_p}
+        # the same kind of sweep over several media in one launch (mixed-media kernel)
+        c2 = media.config2(seed=2)
+        med2 = ctx.medium(c2.labels, c2.bulks, voxel_cm=c2.voxel_cm, fluor_map=c2.fluor_map)
+        c2b = media.config2(seed=7)
+        med3 = ctx.medium(c2b.labels, c2b.bulks, voxel_cm=c2b.voxel_cm, fluor_map=c2b.fluor_map)
+        pool = [med1, med2, med3]
+        rng = np.random.default_rng(11)
+        mruns, mmeds = [], []
+        for i in range(96):
+            k = i % 3
+            b = int(np.exp(rng.uniform(np.log(1e5), np.log(5e6))))
+            x, y = rng.uniform(-1.0, 1.0, 2)
+            mruns.append(mc.run_desc(b, source=(float(x), float(y), 0.0), det=c1.det, seed_exc=20_000 + i))
+            mmeds.append(pool[k])
+        mc.batch_run(ctx, mmeds[:6], mruns[:6], mc.SCHEDULE_BATCHED, images=False)
+        _, mb = mc.batch_run(ctx, mmeds, mruns, mc.SCHEDULE_BATCHED, images=False)
+        _, mp = mc.batch_run(ctx, mmeds, mruns, mc.SCHEDULE_PLAIN, images=False)
+        mt = sum(r.photons for r in mruns)
+        result["batching"]["mixed_media"] = {
+            "workload": f"96 Gaussian beams over 3 media (the sphere medium and two seeded config-2 media) in one "
+                        f"launch, log-uniform budgets 1e5..5e6 ({mt:.3g} photons)",
+            "batched_photons_per_s": mt / (mb / 1e3), "plain_photons_per_s": mt / (mp / 1e3),
+            "batched_over_plain": mp / mb}
+        med3.free()
+        med2.free()
         med1.free()
 
     # --- continuous-batching server ---

@@ -199,6 +199,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         "mcfl_run_mci": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_ulonglong]),
         "mcfl_batch_run": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_int, ctypes.c_int, P(RunOut),
                                           P(ctypes.c_float)]),
+        "mcfl_batch_run_media": (ctypes.c_int, [vp, P(vp), P(RunDesc), ctypes.c_int, ctypes.c_int, P(RunOut),
+                                                P(ctypes.c_float)]),
         "mcfl_run_plain": (ctypes.c_int, [vp, vp, P(RunDesc), ctypes.c_longlong, P(RunOut)]),
         "mcfl_server_create": (ctypes.c_int, [vp, P(ServerOpts), P(vp)]),
         "mcfl_server_submit": (ctypes.c_int, [vp, P(MediumDesc), P(RunDesc), P(ctypes.c_ulonglong)]),
@@ -520,10 +522,11 @@ def _alloc_out(xy, nv=0, images=True, fluence=False):
     return out, keep
 
 
-def batch_run(ctx: "Context", medium: "Medium", runs: list, schedule: int = SCHEDULE_BATCHED,
+def batch_run(ctx: "Context", medium, runs: list, schedule: int = SCHEDULE_BATCHED,
               images: bool = True):
-    """Runs excitation-only simulations on one medium.  Returns (list of
-    dicts with Rd, Tt, R, T, stats; GPU ms)."""
+    """Runs excitation-only simulations on one medium, or on a medium each
+    when `medium` is a list (one per run).  Returns (list of dicts with Rd,
+    Tt, R, T, stats; GPU ms)."""
     n = len(runs)
     arr = (RunDesc * n)(*runs)
     outs = (RunOut * n)()
@@ -534,7 +537,12 @@ def batch_run(ctx: "Context", medium: "Medium", runs: list, schedule: int = SCHE
         outs[i] = o
         keeps.append(k)
     ms = ctypes.c_float()
-    check(load().mcfl_batch_run(ctx.handle, medium.handle, arr, n, schedule, outs, ctypes.byref(ms)))
+    if isinstance(medium, (list, tuple)):
+        assert len(medium) == n
+        handles = (ctypes.c_void_p * n)(*[m.handle for m in medium])
+        check(load().mcfl_batch_run_media(ctx.handle, handles, arr, n, schedule, outs, ctypes.byref(ms)))
+    else:
+        check(load().mcfl_batch_run(ctx.handle, medium.handle, arr, n, schedule, outs, ctypes.byref(ms)))
     res = []
     for i in range(n):
         d = dict(keeps[i])

@@ -465,14 +465,22 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
 
 /* ---------------------------------------------------------------- batch */
 
-extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *runs, int n, int schedule,
-                              mcfl_run_out *outs, float *gpu_ms) {
-  if (n <= 0 || !runs) return fail(MCFL_E_ARG, "mcfl_batch_run: empty batch");
+extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media, const mcfl_run_desc *runs, int n,
+                                    int schedule, mcfl_run_out *outs, float *gpu_ms) {
+  if (n <= 0 || !runs || !media) return fail(MCFL_E_ARG, "mcfl_batch_run: empty batch");
   if (schedule != MCFL_SCHEDULE_BATCHED && schedule != MCFL_SCHEDULE_PLAIN)
     return fail(MCFL_E_ARG, "mcfl_batch_run: unknown schedule");
   const mcfl_detector det = runs[0].det;
+  /* one medium for every run: the single-medium kernel; several: the
+   * mixed-media kernel, each job carrying its medium */
+  const mcfl_medium *m = media[0];
+  bool uniform = true;
+  for (int i = 0; i < n; ++i) uniform = uniform && media[i] == m;
   for (int i = 0; i < n; ++i) {
-    int rc = check_run(c, m, &runs[i]);
+    if (!media[i]) return fail(MCFL_E_ARG, "mcfl_batch_run: null medium");
+    if (!uniform && media[i]->layered)
+      return fail(MCFL_E_ARG, "mcfl_batch_run: layered media batch with their own medium only");
+    int rc = check_run(c, media[i], &runs[i]);
     if (rc) return rc;
     if (runs[i].photons_per_voxel || runs[i].fluence || runs[i].tdet.nx)
       return fail(MCFL_E_ARG, "mcfl_batch_run: excitation images only (no fluence, emission or time detectors)");
@@ -495,9 +503,9 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   unsigned long long tickets = 0;
   for (int i = 0; i < n; ++i) {
     McflJob &j = jobs[i];
-    fill_medium(j, m, false);
+    fill_medium(j, media[i], false);
     fill_detector(j, runs[i].det);
-    fill_source(j, runs[i], m);
+    fill_source(j, runs[i], media[i]);
     j.R = c->bR.as<unsigned long long>() + i * xy;
     j.T = c->bT.as<unsigned long long>() + i * xy;
     j.stats = c->bstats.as<unsigned long long>() + i * (size_t)MCFL_ST_COUNT;
@@ -508,8 +516,9 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     j.photons = runs[i].photons;
     tickets += runs[i].photons;
   }
-  int block = 0;
-  const int grid = c->grid_for(true, &block);
+  int block = 0, block_one = 0;
+  const int grid = c->grid_for(uniform, &block);
+  const int grid_one = c->grid_for(true, &block_one); /* plain schedule: one medium per launch */
   float ms = 0.f;
   if (schedule == MCFL_SCHEDULE_BATCHED) {
     auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -524,7 +533,7 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = (uint32_t)n;
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
-      set_uniform(c, L, m, false, nullptr);
+      if (uniform) set_uniform(c, L, m, false, nullptr);
       if ((e = record_event(c->ev[0], st))) return e;
       if ((e = launch_fn(c->math)(&L, grid, block, st)))
         return e;
@@ -532,10 +541,11 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       if ((e = record_event(c->ev[1], st))) return e;
       return cudaMemcpyAsync(c->h_out, c->bstats.p, N * MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, st);
     };
-    const std::string key =
+    std::string key =
         ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
-                 c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window});
+                 c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window,
+                 (unsigned long long)uniform});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
@@ -553,8 +563,8 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
       L.n_jobs = 1;
       L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
       L.ticket_end = runs[i].photons;
-      set_uniform(c, L, m, false, nullptr);
-      MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
+      set_uniform(c, L, media[i], false, nullptr);
+      MCFL_CUDA_TRY(c->launch_transport(L, grid_one, block_one));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
     }
     MCFL_CUDA_TRY(cudaEventRecord(c->ev[1], s));
@@ -598,6 +608,13 @@ extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   }
   if (capped) return fail(MCFL_E_CAPPED, "photons reached the per-photon pass cap");
   return MCFL_OK;
+}
+
+extern "C" int mcfl_batch_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *runs, int n, int schedule,
+                              mcfl_run_out *outs, float *gpu_ms) {
+  if (n <= 0 || !runs) return fail(MCFL_E_ARG, "mcfl_batch_run: empty batch");
+  std::vector<const mcfl_medium *> media((size_t)n, m);
+  return mcfl_batch_run_media(c, media.data(), runs, n, schedule, outs, gpu_ms);
 }
 
 /* ---------------------------------------------------------------- plain */

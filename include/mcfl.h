@@ -369,6 +369,13 @@ enum {
 int mcfl_batch_run(mcfl_ctx *ctx, const mcfl_medium *medium, const mcfl_run_desc *runs, int n, int schedule,
                    mcfl_run_out *outs, float *gpu_ms);
 
+/* mcfl_batch_run with a medium per simulation (media[i] for runs[i]): many
+ * sources, media and budgets in one persistent launch, replayed as a CUDA
+ * graph; jobs on different media run the mixed-media kernel variant (each job
+ * carries its medium).  Layered media batch only with their own medium. */
+int mcfl_batch_run_media(mcfl_ctx *ctx, const mcfl_medium *const *media, const mcfl_run_desc *runs, int n,
+                         int schedule, mcfl_run_out *outs, float *gpu_ms);
+
 /* The two-phase run with its emission phase scheduled as the reference's
  * voxel loop does it (CUDAMCFLmain.cu:471-594): one launch and host wait per
  * emitting voxel.  With max_voxels > 0 only the first max_voxels emitting

@@ -40,6 +40,34 @@ def test_batched_equals_plain_equals_alone(gpu_ctx):
 
 
 @pytest.mark.gpu
+def test_batch_over_many_media_equals_alone(gpu_ctx):
+    """Sources on four different media (voxelized, mismatched, glass and
+    sphere) with uneven budgets in one launch of the mixed-media kernel, and
+    in the plain schedule: each equals its run alone, bit for bit."""
+    chosen = [cases.tiny(), cases.mismatch(), cases.glass(), cases.sphere()]
+    meds = [c.engine_medium(gpu_ctx) for c in chosen]
+    det = mc.Detector(0.0, 0.0, 0.1, 0.1, 20, 20)
+    runs, media_of = [], []
+    budgets = [4000, 25000, 900, 12000, 7000, 3000, 16000, 1]
+    for i, b in enumerate(budgets):
+        k = i % len(chosen)
+        runs.append(mc.run_desc(b, source=(0.05 * k, -0.02 * k, 0.0), det=det, seed_exc=300 + i,
+                                start_weight=chosen[k].start_weight()))
+        media_of.append(meds[k])
+    bat, _ = mc.batch_run(gpu_ctx, media_of, runs, mc.SCHEDULE_BATCHED)
+    pla, _ = mc.batch_run(gpu_ctx, media_of, runs, mc.SCHEDULE_PLAIN)
+    for i, rd in enumerate(runs):
+        one = _alone(gpu_ctx, media_of[i], rd)
+        for r in (bat[i], pla[i]):
+            assert np.array_equal(r["Rd"], one.Rd) and np.array_equal(r["Tt"], one.Tt)
+            assert r["stats"]["done"] == budgets[i]
+            assert r["stats"]["absorbed"] == one.stats_exc["absorbed"]
+            assert r["stats"]["steps"] == one.stats_exc["steps"]
+    for m in meds:
+        m.free()
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("name", ["tiny", "sphere"])
 def test_plain_per_voxel_emission_equals_batched(name, gpu_ctx):
     case = cases.ALL[name](photons=20000, per_voxel=300)

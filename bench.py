@@ -496,6 +496,7 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
     sctx = mcm.Context(device=device, math=ctx_main.get_option("math"))
     srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048)
     ids, plain_ms_est = [], 0.0
+    arrivals = []  # (offset s, pool index, run desc) to replay through a FIFO
     t_start = time.perf_counter()
     t_next = t_start
     n = 0
@@ -512,16 +513,30 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
         rd = mcm.run_desc(photons, det=det, seed_exc=20_000 + n, kind=mcm.SOURCE_WIDEFIELD if wide else
                           mcm.SOURCE_GAUSS_BEAM, width=4.0, height=4.0, fluence=0)
         ids.append((srv.submit(lab, bulks, vox, rd, fluor_map=fmap), photons))
+        arrivals.append((now - t_start, lab, bulks, vox, fmap, rd))
         n += 1
         t_next += rng.exponential(1.0 / lam)
     for rid, _ in ids:
         srv.wait(rid, -1)
     mtr = srv.metrics()
-    for rid, _ in ids:
-        srv.result(rid)
+    served_lat = [srv.result(rid)["latency_ms"] for rid, _ in ids]
     srv.close()
     photons_total = sum(p for _, p in ids)
     served = photons_total / mtr["span_s"] if mtr["span_s"] > 0 else None
+
+    # the same arrivals through a FIFO that runs one request at a time
+    # (upload, run, read back), the plain schedule a queue alone gives
+    fifo_lat = []
+    t0 = time.perf_counter()
+    for off, lab, bulks, vox, fmap, rd in arrivals:
+        now = time.perf_counter() - t0
+        if now < off:
+            time.sleep(off - now)
+        med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
+        sctx.run(med, rd, images=False, raw=True)
+        med.free()
+        fifo_lat.append(1e3 * (time.perf_counter() - t0 - off))
+    fifo_span = time.perf_counter() - t0
 
     # saturation: the same kind of requests all queued at once (served), and
     # one request per launch after another (plain), same requests both ways
@@ -551,7 +566,12 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
     sctx.close()
     burst_photons = sum(b[4].photons for b in burst)
     return {"requests": len(ids), "arrival_rate_per_s": lam, "target_load": 0.8, "p50_ms": mtr["p50_ms"],
-            "p99_ms": mtr["p99_ms"], "max_ms": mtr["max_ms"], "photons_per_s": served,
+            "p99_ms": mtr["p99_ms"], "max_ms": mtr["max_ms"], "mean_ms": float(np.mean(served_lat)),
+            "photons_per_s": served,
+            "fifo": {"p50_ms": float(np.percentile(fifo_lat, 50)), "p99_ms": float(np.percentile(fifo_lat, 99)),
+                     "mean_ms": float(np.mean(fifo_lat)),
+                     "max_ms": float(np.max(fifo_lat)), "photons_per_s": photons_total / fifo_span,
+                     "note": "the same arrivals, one request at a time in arrival order"},
             "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
             "slices": mtr["slices"],
             "saturated": {"requests": len(burst), "photons": burst_photons,

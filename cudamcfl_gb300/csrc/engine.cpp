@@ -68,7 +68,8 @@ int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time) {
   *blk = block;
   *bps = 0;
   *regs = 0;
-  const int v = uniform ? (time ? 3 : variant) : (time ? -2 : -1);
+  const int mixed = mixed_variant == 1 ? -3 : mixed_variant == 2 ? -4 : -1;
+  const int v = uniform ? (time ? 3 : variant) : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
@@ -161,6 +162,9 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
   } else if (k == "variant") {
     if (v < 0 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant: 0..2");
     c->variant = (int)v;
+  } else if (k == "mixed_variant") {
+    if (v < 0 || v > 2) return fail(MCFL_E_ARG, "mixed_variant: 0..2");
+    c->mixed_variant = (int)v;
   } else if (k == "blocks_per_sm") {
     if (v < 0 || v > 64) return fail(MCFL_E_ARG, "blocks_per_sm: 0..64");
     c->blocks_per_sm = (int)v;
@@ -194,6 +198,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "block") return c->block;
   if (k == "blocks_per_sm") return c->blocks_per_sm;
   if (k == "variant") return c->variant;
+  if (k == "mixed_variant") return c->mixed_variant;
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;
   if (k == "graphs") return c->use_graphs;

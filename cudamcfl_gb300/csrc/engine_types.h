@@ -84,6 +84,7 @@ typedef struct MCFL_ALIGN(16) McflJob {
   uint64_t key;          /* stream family key */
   uint64_t rng_offset;   /* stream index of the job's photon 0 */
   uint64_t ticket_begin; /* first global ticket */
+  uint64_t photon_base;  /* job photon index of ticket_begin (a server slice hands out a job's photons in parts) */
   uint64_t photons;      /* photons in the job */
 } McflJob;
 
@@ -136,6 +137,14 @@ typedef struct McflLaunch {
   unsigned long long *ticket_counter;
   uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */
   const unsigned long long *ticket_end_dev; /* ticket end written by an earlier kernel */
+  /* A second ticket queue (mixed-media launches): one warp in four draws
+   * from the first queue, the others from the second, each from the other
+   * once its own is exhausted.  NULL order2: one queue. */
+  const uint32_t *order2;
+  unsigned long long *ticket_counter2;
+  uint64_t ticket_end2;
+  uint32_t n_jobs2;
+  uint32_t pad3;
   const uint32_t *mult; /* 32768 MWC multipliers */
   McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */

@@ -140,6 +140,7 @@ struct mcfl_ctx {
   int math = MCFL_MATH_EXACT;
   int block = 256;   /* threads per block, clamped to the variant's bound */
   int variant = 0;   /* occupancy variant of the single-medium kernel */
+  int mixed_variant = 2; /* occupancy variant of the mixed-media kernel (128 x 7 measured fastest) */
   int blocks_per_sm = 0;
   uint32_t step_cap = 1u << 24;
   int l2_window = 0;            /* 1: persisting-L2 window over the medium's labels */

@@ -51,7 +51,9 @@ struct Request {
   mcfl_medium *medium = nullptr;
   DevBuf R, T, fhd, stats;
   int slot = -1;
-  uint64_t ticket_begin = 0;
+  uint64_t ticket_begin = 0; /* in the current slice */
+  uint64_t started = 0;      /* photons handed to the GPU so far */
+  unsigned queue = 0;        /* ticket queue of the current slice */
   /* results */
   bool done = false;
   int status = MCFL_OK;
@@ -74,7 +76,8 @@ struct mcfl_server {
   mcfl_ctx *ctx = nullptr;
   size_t budget = 0, used = 0;
   unsigned slots = 64;
-  uint32_t slice_iters = 2048;
+  uint32_t slice_iters = 2048; /* passes per slice while requests wait */
+  uint32_t slice_cur = 2048;   /* grows to 8 x slice_iters while none waits */
   std::mutex mu;
   std::condition_variable cv, cv_done;
   std::deque<std::shared_ptr<Request>> queue;
@@ -201,9 +204,9 @@ int mcfl_server::admit_locked(std::vector<std::shared_ptr<Request>> &to_upload) 
 void mcfl_server::loop() {
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
-  unsigned long long counter_now = 0;
   for (;;) {
     std::vector<std::shared_ptr<Request>> fresh;
+    bool waiting = false;
     {
       std::unique_lock<std::mutex> lk(mu);
       bool have_active = false;
@@ -214,11 +217,14 @@ void mcfl_server::loop() {
         continue;
       }
       admit_locked(fresh);
+      waiting = !queue.empty();
     }
+    /* Short slices let waiting requests in soon; with nobody waiting the
+     * slices lengthen, which saves the per-slice host round trips. */
+    slice_cur = (waiting || !fresh.empty()) ? slice_iters : std::min(slice_cur * 2u, slice_iters * 8u);
     for (auto &r : fresh) {
       r->t_admit = Clock::now();
-      r->ticket_begin = std::max<uint64_t>(tickets_end, counter_now);
-      tickets_end = r->ticket_begin + r->run.photons;
+      r->started = 0;
       int rc = upload(*r);
       if (rc != MCFL_OK) {
         std::lock_guard<std::mutex> lk(mu);
@@ -230,38 +236,99 @@ void mcfl_server::loop() {
         cv_done.notify_all();
       }
     }
-    /* slots in ticket order */
-    unsigned n = 0;
+    /* Tickets of this slice, in two queues: the oldest admitted request
+     * alone in the second (three warps in four); in the first (one warp in
+     * four) the requests at most an eighth of its remaining size, shortest
+     * remaining first; each warp turns to the other queue once its own is
+     * exhausted.  Larger requests wait for the head, in admission order.  So
+     * a small request arriving behind a large one starts at once on a
+     * quarter of the GPU, and large requests keep their admission order and
+     * at least three quarters of the GPU.  Photon k of a request still draws the stream of index k,
+     * whatever slice or queue hands it out. */
+    unsigned n = 0, n_active = 0;
+    int head = -1;
+    std::vector<uint32_t> h_stat_slot;
     for (unsigned i = 0; i < slots; ++i)
-      if (active[i]) h_order[n++] = i;
-    if (n == 0) continue;
-    std::sort(h_order, h_order + n, [&](uint32_t a, uint32_t b) { return h_jobs[a].ticket_begin < h_jobs[b].ticket_begin; });
+      if (active[i]) {
+        ++n_active;
+        h_stat_slot.push_back(i);
+        if (active[i]->started < active[i]->run.photons) {
+          h_order[n++] = i;
+          if (head < 0 || active[i]->t_admit < active[head]->t_admit ||
+              (active[i]->t_admit == active[head]->t_admit && active[i]->id < active[head]->id))
+            head = (int)i;
+        }
+      }
+    if (n_active == 0) continue;
+    unsigned n0 = n, n2 = 0;
+    if (n > 1) { /* the head leaves the first queue for the second */
+      const uint64_t head_left = active[head]->run.photons - active[head]->started;
+      unsigned w = 0;
+      for (unsigned i = 0; i < n; ++i) {
+        const Request &r = *active[h_order[i]];
+        if ((int)h_order[i] != head && (r.run.photons - r.started) * 8 <= head_left) h_order[w++] = h_order[i];
+      }
+      n0 = w;
+      if (n0 == 0) {
+        h_order[0] = (uint32_t)head;
+        n0 = 1;
+      } else {
+        h_order[n0] = (uint32_t)head;
+        n2 = 1;
+      }
+    }
+    std::sort(h_order, h_order + n0, [&](uint32_t a, uint32_t b) {
+      const uint64_t ra = active[a]->run.photons - active[a]->started, rb = active[b]->run.photons - active[b]->started;
+      return ra != rb ? ra < rb : a < b;
+    });
+    uint64_t tickets = 0, tickets2 = 0;
+    for (unsigned i = 0; i < n0 + n2; ++i) {
+      Request &r = *active[h_order[i]];
+      McflJob &j = h_jobs[h_order[i]];
+      uint64_t &tk = i < n0 ? tickets : tickets2;
+      r.ticket_begin = tk;
+      r.queue = i < n0 ? 0 : 1;
+      j.ticket_begin = tk;
+      j.photon_base = r.started;
+      j.photons = r.run.photons - r.started;
+      tk += j.photons;
+    }
+    tickets_end = tickets;
+    const uint64_t tickets_end2 = tickets2;
     const auto t0 = Clock::now();
+    cudaMemsetAsync(counter.p, 0, 16, s);
     cudaMemcpyAsync(slot_jobs.p, h_jobs, slots * sizeof(McflJob), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(order.p, h_order, n * 4, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(order.p, h_order, (size_t)(n0 + n2) * 4, cudaMemcpyHostToDevice, s);
     McflLaunch L;
     std::memset(&L, 0, sizeof(L));
     L.jobs = slot_jobs.as<McflJob>();
     L.order = order.as<uint32_t>();
-    L.n_jobs = n;
-    L.max_iters = slice_iters;
+    L.n_jobs = n0;
+    if (n2) {
+      L.order2 = order.as<uint32_t>() + n0;
+      L.n_jobs2 = n2;
+      L.ticket_counter2 = counter.as<unsigned long long>() + 1;
+      L.ticket_end2 = tickets_end2;
+    }
+    L.max_iters = slice_cur;
+    L.variant = (uint32_t)ctx->mixed_variant;
     L.ticket_counter = counter.as<unsigned long long>();
     L.ticket_end = tickets_end;
     L.mult = ctx->mult.as<uint32_t>();
     L.saved = parked.as<McflSaved>();
     L.step_cap = ctx->step_cap;
     cudaError_t e = ctx->launch_transport(L, grid, block);
-    cudaMemcpyAsync(h_read, counter.p, 8, cudaMemcpyDeviceToHost, s);
-    for (unsigned i = 0; i < n; ++i) {
-      Request &r = *active[h_order[i]];
-      cudaMemcpyAsync(h_read + 1 + (size_t)i * MCFL_ST_COUNT, r.stats.p, MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(h_read, counter.p, 16, cudaMemcpyDeviceToHost, s);
+    for (unsigned i = 0; i < n_active; ++i) {
+      Request &r = *active[h_stat_slot[i]];
+      cudaMemcpyAsync(h_read + 2 + (size_t)i * MCFL_ST_COUNT, r.stats.p, MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     const auto t1 = Clock::now();
     busy_s += std::chrono::duration<double>(t1 - t0).count();
     ++slices;
-    inflight_sum += n;
-    max_inflight = std::max<unsigned long long>(max_inflight, n);
+    inflight_sum += n_active;
+    max_inflight = std::max<unsigned long long>(max_inflight, n_active);
     if (e != cudaSuccess) {
       std::lock_guard<std::mutex> lk(mu);
       fatal = cuda_fail(e, "server slice");
@@ -279,11 +346,18 @@ void mcfl_server::loop() {
       cv_done.notify_all();
       return;
     }
-    counter_now = h_read[0];
-    for (unsigned i = 0; i < n; ++i) {
-      const uint32_t slot = h_order[i];
+    /* warps may draw past a queue's end */
+    const uint64_t drawn[2] = {std::min<uint64_t>(h_read[0], tickets_end), std::min<uint64_t>(h_read[1], tickets_end2)};
+    for (unsigned i = 0; i < n0 + n2; ++i) {
+      Request &r = *active[h_order[i]];
+      const uint64_t c = drawn[r.queue];
+      const uint64_t handed = c > r.ticket_begin ? c - r.ticket_begin : 0;
+      r.started += std::min<uint64_t>(handed, r.run.photons - r.started);
+    }
+    for (unsigned i = 0; i < n_active; ++i) {
+      const uint32_t slot = h_stat_slot[i];
       std::shared_ptr<Request> r = active[slot];
-      const unsigned long long *st = h_read + 1 + (size_t)i * MCFL_ST_COUNT;
+      const unsigned long long *st = h_read + 2 + (size_t)i * MCFL_ST_COUNT;
       if (st[MCFL_ST_DONE] < r->run.photons) continue;
       const size_t xy = (size_t)r->run.det.nx + (size_t)r->run.det.nx * r->run.det.ny;
       r->Rd.resize(xy);
@@ -327,6 +401,7 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   sv->budget = opts && opts->hbm_budget_bytes ? (size_t)opts->hbm_budget_bytes : free_b / 2;
   sv->slots = opts && opts->max_jobs ? (unsigned)opts->max_jobs : 64u;
   sv->slice_iters = opts && opts->slice_passes ? (uint32_t)opts->slice_passes : 2048u;
+  sv->slice_cur = sv->slice_iters;
   if (sv->slots > 4096) {
     delete sv;
     return fail(MCFL_E_RANGE, "max_jobs above 4096");
@@ -336,13 +411,13 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   const size_t threads = (size_t)sv->grid * sv->block;
   cudaError_t e = sv->slot_jobs.reserve(sv->slots * sizeof(McflJob));
   if (!e) e = sv->order.reserve(sv->slots * 4);
-  if (!e) e = sv->counter.reserve(8);
+  if (!e) e = sv->counter.reserve(16); /* the two queues' ticket counters */
   if (!e) e = sv->parked.reserve(threads * sizeof(McflSaved));
   if (!e) e = cudaMemset(sv->counter.p, 0, 8);
   if (!e) e = cudaMemset(sv->parked.p, 0, threads * sizeof(McflSaved));
   if (!e) e = cudaHostAlloc((void **)&sv->h_jobs, sv->slots * sizeof(McflJob), cudaHostAllocDefault);
   if (!e) e = cudaHostAlloc((void **)&sv->h_order, sv->slots * 4, cudaHostAllocDefault);
-  if (!e) e = cudaHostAlloc((void **)&sv->h_read, (1 + (size_t)sv->slots * MCFL_ST_COUNT) * 8, cudaHostAllocDefault);
+  if (!e) e = cudaHostAlloc((void **)&sv->h_read, (2 + (size_t)sv->slots * MCFL_ST_COUNT) * 8, cudaHostAllocDefault);
   if (e) {
     mcfl_server_destroy(sv);
     return cuda_fail(e, "mcfl_server_create");

@@ -223,20 +223,20 @@ __device__ __forceinline__ uint32_t start_label(const Med &m, const Photon &p) {
   return m.last;
 }
 
-__device__ __forceinline__ uint32_t slot_at(const McflLaunch &L, uint32_t i) { return L.order ? __ldg(&L.order[i]) : i; }
+__device__ __forceinline__ uint32_t slot_at(const uint32_t *order, uint32_t i) { return order ? __ldg(&order[i]) : i; }
 
-/* Locates the job slot owning global ticket t (binary search over the slots
- * in ticket order). */
-__device__ __forceinline__ uint32_t find_job(const McflLaunch &L, uint64_t t) {
-  if (L.n_jobs == 0) return 0xffffffffu;
-  uint32_t lo = 0, hi = L.n_jobs - 1;
+/* Locates the job slot owning ticket t of a queue (binary search over its
+ * slots in ticket order). */
+__device__ __forceinline__ uint32_t find_job(const McflJob *jobs, const uint32_t *order, uint32_t n_jobs, uint64_t t) {
+  if (n_jobs == 0) return 0xffffffffu;
+  uint32_t lo = 0, hi = n_jobs - 1;
   while (lo < hi) {
     uint32_t mid = (lo + hi + 1) >> 1;
-    if (__ldg((const unsigned long long *)&L.jobs[slot_at(L, mid)].ticket_begin) <= t) lo = mid;
+    if (__ldg((const unsigned long long *)&jobs[slot_at(order, mid)].ticket_begin) <= t) lo = mid;
     else hi = mid - 1;
   }
-  const uint32_t slot = slot_at(L, lo);
-  const McflJob *J = &L.jobs[slot];
+  const uint32_t slot = slot_at(order, lo);
+  const McflJob *J = &jobs[slot];
   const uint64_t b = __ldg((const unsigned long long *)&J->ticket_begin);
   const uint64_t n = __ldg((const unsigned long long *)&J->photons);
   return (t >= b && t - b < n) ? slot : 0xffffffffu;
@@ -598,7 +598,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   }
 
   const uint64_t ticket_end = L.ticket_end_dev ? *L.ticket_end_dev : L.ticket_end;
-  bool alive = false, exhausted = false;
+  bool alive = false;
+  /* the warp's ticket queue and which queues it found exhausted (warp-uniform;
+   * a missing second queue counts as exhausted) */
+  const bool two_queues = !kUniform && L.order2 != nullptr;
+  uint32_t q = two_queues ? (((gtid >> 5) & 3u) != 0u ? 1u : 0u) : 0u;
+  bool ex0 = false, ex1 = !two_queues;
   Photon p;
   Rng r;
   Med m = {};
@@ -666,17 +671,21 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (!kUniform && L.max_iters && it >= L.max_iters) break;
     /* one vote per pass while every lane carries a photon */
     if (__ballot_sync(kFull, !alive)) {
-    const bool need = !alive && !exhausted;
+    const bool need = !alive && !(ex0 && ex1);
     const unsigned nm = __ballot_sync(kFull, need);
     if (nm) {
+      if (q ? ex1 : ex0) q ^= 1u;
+      unsigned long long *ctr = q ? L.ticket_counter2 : L.ticket_counter;
+      const uint64_t end = q ? L.ticket_end2 : ticket_end;
       const int leader = __ffs(nm) - 1;
       unsigned long long base = 0ull;
-      if ((int)lane == leader) base = atomicAdd(L.ticket_counter, (unsigned long long)__popc(nm));
+      if ((int)lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(nm));
       base = __shfl_sync(kFull, base, leader);
+      bool over = false;
       if (need) {
         const uint64_t t = base + (uint64_t)__popc(nm & ((1u << lane) - 1u));
-        if (t < ticket_end) {
-          const uint32_t j = find_job(L, t);
+        if (t < end) {
+          const uint32_t j = q ? find_job(L.jobs, L.order2, L.n_jobs2, t) : find_job(L.jobs, L.order, L.n_jobs, t);
           if (j != 0xffffffffu) {
             if (j != job) {
               flush_stats();
@@ -684,7 +693,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               J = &L.jobs[j];
               if (!kUniform) load_med(J, m);
             }
-            k = t - __ldg((const unsigned long long *)&J->ticket_begin);
+            k = __ldg((const unsigned long long *)&J->photon_base) +
+                (t - __ldg((const unsigned long long *)&J->ticket_begin));
             launch_photon<kLayered>(J, m, k, L.mult, p, r, src_idx);
             if (!kUniform) rc = load_rec(m, p.label);
             pst = 0;
@@ -692,11 +702,15 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             alive = true;
           }
         } else {
-          exhausted = true;
+          over = true;
         }
       }
+      if (__any_sync(kFull, over)) {
+        if (q) ex1 = true;
+        else ex0 = true;
+      }
     }
-    if (__all_sync(kFull, !alive)) break;
+    if (__all_sync(kFull, !alive) && ex0 && ex1) break;
     if (!alive) continue;
     }
 
@@ -884,14 +898,19 @@ static size_t smem_bytes(int block, bool uniform) {
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
- * of flight.  Mixed media: -1 = 256 x 3, -2 = 256 x 2 with the time of
- * flight. */
+ * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
+ * -2 = 256 x 2 with the time of flight. */
 typedef void (*TransportKernel)(McflLaunch);
+
+/* Mixed-media occupancy variants: 0 = 256 x 3, 1 = 256 x 4, 2 = 128 x 7. */
+static int mixed_variant_code(uint32_t v) { return v == 1 ? -3 : v == 2 ? -4 : -1; }
 
 static TransportKernel kernel_of(int variant, int *threads) {
   switch (variant) {
   case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, false, 256, 2>;
   case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, false, 256, 3>;
+  case -3: *threads = 256; return MCFL_KERNEL_NAME<false, false, false, 256, 4>;
+  case -4: *threads = 128; return MCFL_KERNEL_NAME<false, false, false, 128, 7>;
   case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 4>;
   case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 5>;
   case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, false, 128, 9>;
@@ -917,7 +936,8 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
     return cudaErrorInvalidValue;
   const int v = L->med.layered ? (L->time_on ? 5 : 4)
                 : L->uniform_medium ? (L->time_on ? 3 : (int)L->variant)
-                                    : (L->time_on ? -2 : -1);
+                : L->time_on        ? -2
+                                    : mixed_variant_code(L->variant);
   int t = 0;
   const TransportKernel fn = kernel_of(v, &t);
   if (!fn || block > t) return cudaErrorInvalidValue;

@@ -302,6 +302,9 @@ const char *mcfl_last_error(void);
 /* Options: "math" (MCFL_MATH_*), "block" (threads per block, at most the
  * variant's bound), "variant" (occupancy variant of the single-medium kernel:
  * 0 = 256 threads x 4 blocks per SM, 1 = 256 x 5, 2 = 128 x 9),
+ * "mixed_variant" (occupancy variant of the mixed-media kernel that batches
+ * over several media and the server run: 0 = 256 x 3, 1 = 256 x 4,
+ * 2 = 128 x 7, the default),
  * "blocks_per_sm" (0 = occupancy maximum), "step_cap" (passes per photon),
  * "l2_window" (1: persisting L2 access window on the labels and tallies).
  * The launch shape of the reference is fixed (CUDAMCFL.h:18-20). */

@@ -674,9 +674,15 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     const bool need = !alive && !(ex0 && ex1);
     const unsigned nm = __ballot_sync(kFull, need);
     if (nm) {
-      if (q ? ex1 : ex0) q ^= 1u;
-      unsigned long long *ctr = q ? L.ticket_counter2 : L.ticket_counter;
-      const uint64_t end = q ? L.ticket_end2 : ticket_end;
+      unsigned long long *ctr = L.ticket_counter;
+      uint64_t end = ticket_end;
+      if constexpr (!kUniform) {
+        if (q ? ex1 : ex0) q ^= 1u;
+        if (q) {
+          ctr = L.ticket_counter2;
+          end = L.ticket_end2;
+        }
+      }
       const int leader = __ffs(nm) - 1;
       unsigned long long base = 0ull;
       if ((int)lane == leader) base = atomicAdd(ctr, (unsigned long long)__popc(nm));
@@ -685,7 +691,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       if (need) {
         const uint64_t t = base + (uint64_t)__popc(nm & ((1u << lane) - 1u));
         if (t < end) {
-          const uint32_t j = q ? find_job(L.jobs, L.order2, L.n_jobs2, t) : find_job(L.jobs, L.order, L.n_jobs, t);
+          const uint32_t j = (!kUniform && q) ? find_job(L.jobs, L.order2, L.n_jobs2, t)
+                                              : find_job(L.jobs, L.order, L.n_jobs, t);
           if (j != 0xffffffffu) {
             if (j != job) {
               flush_stats();
@@ -706,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         }
       }
       if (__any_sync(kFull, over)) {
-        if (q) ex1 = true;
+        if (!kUniform && q) ex1 = true;
         else ex0 = true;
       }
     }

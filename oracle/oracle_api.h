@@ -108,6 +108,9 @@ typedef struct oracle_sim {
   /* photon only: index of the excitation run's first photon in its stream
    * family (runs over disjoint index ranges sum to the run over their union) */
   unsigned long long photon_offset;
+  /* photon only, voxelized media: 1 = voxel-boundary ("exact") stepping
+   * instead of the reference's whole-step-in-the-start-voxel transport */
+  int exact_stepping;
 } oracle_sim;
 
 void oracle_free_result(oracle_result *r);

@@ -112,6 +112,9 @@ struct Photon {
   uint32_t weight;
   uint32_t bulkpos;
   uint64_t tof; /* time of flight [fs] */
+  /* voxel-boundary stepping: the photon's voxel, or ingrid = 0 outside the
+   * grid's lateral extent (the medium of label 1) */
+  int ix, iy, iz, ingrid;
 };
 
 /* Everything one transport phase reads (the reference's __constant__ set). */
@@ -149,6 +152,7 @@ struct Phase {
   oracle_layer layers[ORACLE_MAX_LAYERS + 2];
   oracle_inclusion incl;
   uint32_t start_layer;
+  int exact; /* voxel-boundary stepping (photon mode, voxelized media) */
 };
 
 inline unsigned voxel_index(const Phase &ph, float x, float y, float z) {
@@ -606,9 +610,205 @@ unsigned step_layers(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
 }
 
+/* ------------------------- voxel-boundary stepping ------------------------ */
+
+/* The photon's voxel from its position (voxel-boundary stepping). */
+inline void locate(Photon &p, const Phase &ph) {
+  if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy) {
+    p.ix = (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
+    p.iy = (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
+    p.iz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
+    p.ingrid = 1;
+  } else {
+    p.ix = p.iy = p.iz = 0;
+    p.ingrid = 0;
+  }
+}
+
+/* Fresnel reflection / refraction at a voxel face whose normal is axis a
+ * (0, 1, 2 = x, y, z): the reference's Reflect with that axis in place of z.
+ * Returns 1 when transmitted. */
+inline unsigned refract_axis(Photon &p, int a, float n1, float n2, Rng &r) {
+  float *d[3] = {&p.dx, &p.dy, &p.dz};
+  float &dn = *d[a], &t1 = *d[(a + 1) % 3], &t2 = *d[(a + 2) % 3];
+  float rr;
+  const float cos_angle_i = fabsf(dn);
+  if (n1 == n2) return 1u;
+  if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
+    dn *= -1.0f;
+    return 0u;
+  }
+  if (cos_angle_i == 1.0f) {
+    rr = (n1 - n2) / (n1 + n2);
+    if (r.co() <= rr * rr) {
+      dn *= -1.0f;
+      return 0u;
+    }
+    return 1u;
+  }
+  float e = (n1 * n1) / (n2 * n2) * (1.0f - cos_angle_i * cos_angle_i);
+  rr = 2 * sqrtf((1.0f - cos_angle_i * cos_angle_i) * (1.0f - e) * e * cos_angle_i * cos_angle_i);
+  e = e + (cos_angle_i * cos_angle_i) * (1.0f - 2.0f * e);
+  rr = e * ((1.0f - e - rr) / ((1.0f - e + rr) * (e + rr)));
+  if (r.co() <= rr) {
+    dn *= -1.0f;
+    return 0u;
+  }
+  rr = n1 / n2;
+  e = rr * rr * (1.0f - cos_angle_i * cos_angle_i);
+  t1 *= rr;
+  t2 *= rr;
+  dn = copysignf(sqrtf(1 - e), dn);
+  return 1u;
+}
+
+/* Distance along direction component d from coordinate c to plane b
+ * (FLT_MAX when the photon does not move towards it), never negative. */
+inline float plane_dist(float b, float c, float d) {
+  if (d == 0.0f) return FLT_MAX;
+  const float t = (b - c) / d;
+  return t > 0.0f ? t : 0.0f;
+}
+
+/* One pass with voxel-boundary stepping: an optical depth -ln(u) is spent
+ * voxel by voxel with each voxel's mu_t, the label is taken where the photon
+ * is, Fresnel acts at every face between different indices with that face's
+ * normal, scattering-free voxels are crossed without interaction.  The pass
+ * ends at the interaction (PHD tally, weight drop and spin as the reference's
+ * pass) or at an exit. */
+template <class M>
+unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
+  const uint32_t last = ph.last_bulk;
+  sk.steps++;
+  float tau = -M::log(r.oc());
+  const int cap = 16 + 4 * (int)(ph.num_x + ph.num_y + ph.num_z);
+  for (int it = 0;; ++it) {
+    if (it >= cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
+      sk.w0_loss += p.weight;
+      p.weight = 0u;
+      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+    }
+    const Prop &pr = ph.prop[p.bulkpos];
+    const bool glass = pr.mutr == FLT_MAX;
+    float db = FLT_MAX;
+    int axis = -1;
+    float t;
+    if (p.ingrid) {
+      const float bx = (float)(p.dx > 0.0f ? p.ix + 1 : p.ix) / ph.gx - ph.hx;
+      t = plane_dist(bx, p.x, p.dx);
+      if (t < db) { db = t; axis = 0; }
+      const float by = (float)(p.dy > 0.0f ? p.iy + 1 : p.iy) / ph.gy - ph.hy;
+      t = plane_dist(by, p.y, p.dy);
+      if (t < db) { db = t; axis = 1; }
+      const int kz = p.dz > 0.0f ? p.iz + 1 : p.iz;
+      const float bz = kz == 0 ? 0.0f : (kz == (int)ph.num_z ? ph.esp : (float)kz / ph.gz);
+      t = plane_dist(bz, p.z, p.dz);
+      if (t < db) { db = t; axis = 2; }
+    } else {
+      t = plane_dist(p.dz > 0.0f ? ph.esp : 0.0f, p.z, p.dz);
+      if (t < db) { db = t; axis = 2; }
+      /* re-entry through a lateral face of the grid */
+      if ((p.x <= -ph.hx && p.dx > 0.0f) || (p.x >= ph.hx && p.dx < 0.0f)) {
+        t = plane_dist(p.dx > 0.0f ? -ph.hx : ph.hx, p.x, p.dx);
+        const float yc = p.y + p.dy * t;
+        if (t < db && fabsf(yc) < ph.hy) { db = t; axis = 0; }
+      }
+      if ((p.y <= -ph.hy && p.dy > 0.0f) || (p.y >= ph.hy && p.dy < 0.0f)) {
+        t = plane_dist(p.dy > 0.0f ? -ph.hy : ph.hy, p.y, p.dy);
+        const float xc = p.x + p.dx * t;
+        if (t < db && fabsf(xc) < ph.hx) { db = t; axis = 1; }
+      }
+    }
+    if (!glass) {
+      const float s_int = tau * pr.mutr;
+      if (s_int <= db) { /* the interaction happens in this voxel */
+        p.x += p.dx * s_int;
+        p.y += p.dy * s_int;
+        p.z += p.dz * s_int;
+        break;
+      }
+    }
+    if (axis < 0) { /* a scattering-free region with no face ahead */
+      sk.w0_loss += p.weight;
+      p.weight = 0u;
+      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+    }
+    p.x += p.dx * db;
+    p.y += p.dy * db;
+    p.z += p.dz * db;
+    if (!glass) {
+      tau -= db / pr.mutr;
+      if (tau < 0.0f) tau = 0.0f;
+    }
+    /* the region across the face */
+    int nix = p.ix, niy = p.iy, niz = p.iz, nin = p.ingrid;
+    uint32_t next;
+    if (p.ingrid) {
+      if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
+      else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
+      else niz += p.dz > 0.0f ? 1 : -1;
+      if (niz < 0) next = 0;
+      else if (niz >= (int)ph.num_z) next = last;
+      else if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
+        next = 1;
+        nin = 0;
+      } else {
+        next = (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
+      }
+    } else if (axis == 2) {
+      next = p.dz > 0.0f ? last : 0;
+    } else {
+      nin = 1;
+      nix = axis == 0 ? (p.dx > 0.0f ? 0 : (int)ph.num_x - 1)
+                      : (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
+      niy = axis == 1 ? (p.dy > 0.0f ? 0 : (int)ph.num_y - 1)
+                      : (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
+      niz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
+      next = (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
+    }
+    if (next != p.bulkpos && !refract_axis(p, axis, pr.n, ph.prop[next].n, r)) continue; /* reflected */
+    p.bulkpos = next;
+    p.ix = nix;
+    p.iy = niy;
+    p.iz = niz;
+    p.ingrid = nin;
+    if (next == 0 || next == last) {
+      const bool top = next == 0;
+      if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
+        const unsigned idx = pixel_index(ph, p.x, p.y);
+        if (top) {
+          if (sk.R128) add128(&sk.R128[2 * (size_t)idx], p.weight, sk.voxel_q);
+          else add_guarded(&sk.Rd[idx], p.weight, ph.guard);
+        } else {
+          if (sk.T128) add128(&sk.T128[2 * (size_t)idx], p.weight, sk.voxel_q);
+          else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
+        }
+      }
+      (top ? sk.exit_top : sk.exit_bottom) += p.weight;
+      p.weight = 0u;
+      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+    }
+  }
+  /* the interaction */
+  if (ph.fhd_on == 1 && p.ingrid)
+    add_guarded(&sk.fhd[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)], p.weight, ph.guard);
+  const Prop &pr = ph.prop[p.bulkpos];
+  uint32_t w = mcfl_f2u_ru(pr.mua * pr.mutr * mcfl_u2f_rn(p.weight));
+  if (w > 0) {
+    p.weight -= w;
+    sk.absorbed += w;
+  } else {
+    sk.w0_loss += p.weight;
+    p.weight = 0u;
+  }
+  spin<M>(p, pr.g, r);
+  return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+}
+
 template <class M>
 inline unsigned step_any(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
-  return ph.method == 1 ? step_layers<M>(p, r, ph, sk) : step<M>(p, r, ph, sk);
+  if (ph.method == 1) return step_layers<M>(p, r, ph, sk);
+  return ph.exact ? step_exact<M>(p, r, ph, sk) : step<M>(p, r, ph, sk);
 }
 
 /* ------------------------------------------------------------------------ */
@@ -647,6 +847,7 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
   }
   ph.labels = sim->bulk_info;
   ph.method = sim->bulk_method == 1 ? 1 : 2;
+  ph.exact = ph.method == 2 ? sim->exact_stepping : 0;
   if (ph.method == 1) {
     ph.n_layers = (unsigned)sim->n_layers;
     for (unsigned i = 0; i < ph.n_layers + 2 && i < ORACLE_MAX_LAYERS + 2; ++i) ph.layers[i] = sim->layers[i];
@@ -891,8 +1092,13 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
       float zi = ((float)iz / ph.gz);
       sk.voxel_q = voxq[k / nv];
       launch_photon<M, true>(p, r, ph, xi, yi, zi);
+      p.ix = (int)ix;
+      p.iy = (int)iy;
+      p.iz = (int)iz;
+      p.ingrid = 1;
     } else {
       launch_photon<M, true>(p, r, ph, ph.xi, ph.yi, ph.zi);
+      locate(p, ph);
     }
     if (ph.launch_rng_reuse && k_in_run < kThreads) r.x = x_at_launch;
     while (step_any<M>(p, r, ph, sk)) {

@@ -118,6 +118,7 @@ class CSim(ctypes.Structure):
         ("layers", CLayer * (MAX_LAYERS + 2)),
         ("inclusion", CInclusion),
         ("photon_offset", ctypes.c_ulonglong),
+        ("exact_stepping", ctypes.c_int),
     ]
 
 

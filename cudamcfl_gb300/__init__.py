@@ -118,7 +118,7 @@ class RunDesc(ctypes.Structure):
     _fields_ = [("photons", ctypes.c_ulonglong), ("photons_per_voxel", ctypes.c_uint), ("fluence", ctypes.c_int),
                 ("seed_exc", ctypes.c_ulonglong), ("seed_fl", ctypes.c_ulonglong), ("start_weight", ctypes.c_uint),
                 ("source", Source), ("det", Detector), ("launch_rng_reuse", ctypes.c_int),
-                ("tdet", TimeDetectors), ("photon_offset", ctypes.c_ulonglong)]
+                ("tdet", TimeDetectors), ("photon_offset", ctypes.c_ulonglong), ("exact_stepping", ctypes.c_int)]
 
 
 _u64p = ctypes.POINTER(ctypes.c_ulonglong)
@@ -621,9 +621,12 @@ class Server:
 
 def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per_voxel: int = 0, fluence: int = 0,
              seed_exc: int = 1, seed_fl: int = 2, start_weight: int = 0, kind: int = SOURCE_GAUSS_BEAM,
-             width: float = 0.0, height: float = 0.0, launch_rng_reuse: int = 0, tdet: tuple | None = None) -> RunDesc:
+             width: float = 0.0, height: float = 0.0, launch_rng_reuse: int = 0, tdet: tuple | None = None,
+             exact_stepping: int = 0) -> RunDesc:
     """tdet: time-resolved detectors (x0, y0, nx, ny, sep_x, sep_y, radius,
-    face, bins, max_fs), or None."""
+    face, bins, max_fs), or None.  exact_stepping: 1 for voxel-boundary
+    stepping (mu_t spent voxel by voxel, Fresnel with each face's normal),
+    0 for the reference's stepping."""
     r = RunDesc()
     r.photons = photons
     r.photons_per_voxel = photons_per_voxel
@@ -634,6 +637,7 @@ def run_desc(photons: int, *, source=(0.0, 0.0, 0.0), det: Detector, photons_per
     r.source = Source(kind, *[float(v) for v in source], width, height)
     r.det = det
     r.launch_rng_reuse = launch_rng_reuse
+    r.exact_stepping = exact_stepping
     if tdet:
         x0, y0, tnx, tny, sx, sy, rad, face, bins, tmax = tdet
         r.tdet = TimeDetectors(tnx, tny, x0, y0, sx, sy, rad, face, bins, tmax)

@@ -14,6 +14,7 @@
  * All scratch lives in grow-only buffers of the context, so repeated runs
  * allocate nothing.
  */
+#include <atomic>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,18 +65,23 @@ void DevBuf::release() {
 using namespace mcfl;
 
 
-int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time) {
+unsigned long long next_medium_serial() {
+  static std::atomic<unsigned long long> counter{0};
+  return ++counter;
+}
+
+int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool exact) {
   *blk = block;
   *bps = 0;
   *regs = 0;
   const int mixed = mixed_variant == 1 ? -3 : mixed_variant == 2 ? -4 : -1;
-  const int v = uniform ? (time ? 3 : variant) : (time ? -2 : mixed);
+  const int v = exact ? 6 : uniform ? (time ? 3 : variant) : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
-int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out, bool time) {
+int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out, bool time, bool exact) {
   int blk = 0, bps = 0, regs = 0;
-  if (attr(uniform, &blk, &bps, &regs, time) != 0 || bps <= 0) bps = 1;
+  if (attr(uniform, &blk, &bps, &regs, time, exact) != 0 || bps <= 0) bps = 1;
   if (blocks_per_sm > 0 && blocks_per_sm < bps) bps = blocks_per_sm;
   if (bps_out) *bps_out = bps;
   if (block_out) *block_out = blk;
@@ -241,6 +247,7 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
     if (d->labels[i] > (unsigned)d->n_bulks + 1u) return fail(MCFL_E_ARG, "medium: label beyond n_bulks+1");
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   mcfl_medium *m = new mcfl_medium();
+  m->serial = next_medium_serial();
   m->ctx = c;
   m->nx = d->nx;
   m->ny = d->ny;
@@ -308,6 +315,7 @@ extern "C" int mcfl_medium_create_layered(mcfl_ctx *c, const mcfl_layered_desc *
   if (!(d->inclusion.r >= 0.0f)) return fail(MCFL_E_ARG, "layered medium: negative inclusion radius");
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   mcfl_medium *m = new mcfl_medium();
+  m->serial = next_medium_serial();
   m->ctx = c;
   m->layered = true;
   m->n_layers = n;

@@ -151,7 +151,7 @@ typedef struct McflLaunch {
   uint32_t uniform_medium; /* 1: every job uses med (and fhd_on agrees with med.fhd) */
   uint32_t variant;        /* occupancy variant of the single-medium kernel */
   uint32_t time_on;        /* 1: carry the time of flight (some job has time-resolved detectors) */
-  uint32_t pad2;
+  uint32_t exact_step;     /* 1: voxel-boundary stepping (single voxelized medium) */
   float l2_hit_ratio;      /* host side: persisting-L2 window over [l2_base, +l2_bytes) when l2_bytes > 0 */
   const void *l2_base;
   unsigned long long l2_bytes;

@@ -96,8 +96,13 @@ void time_positions(const mcfl_time_detectors &td, float *px, float *py);
 
 } // namespace mcfl
 
+unsigned long long next_medium_serial();
+
 struct mcfl_medium {
   mcfl_ctx *ctx = nullptr;
+  /* distinct for every medium a process creates: recorded graphs carry the
+   * medium's geometry by value, and a freed medium's address can come back */
+  unsigned long long serial = 0;
   mcfl::DevBuf labels, prop_exc, prop_emi, lab_exc, lab_emi, fl, fmap;
   int nx = 0, ny = 0, nz = 0;
   uint32_t total = 0;
@@ -151,8 +156,8 @@ struct mcfl_ctx {
 
   /* Grid (SMs x resident blocks) and threads per block of the single-medium
    * (uniform) or mixed-media kernel under the current options. */
-  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr, bool time = false);
-  int attr(bool uniform, int *block, int *bps, int *regs, bool time = false);
+  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr, bool time = false, bool exact = false);
+  int attr(bool uniform, int *block, int *bps, int *regs, bool time = false, bool exact = false);
   cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
 };
 

@@ -102,6 +102,7 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
   for (int i = 0; i < n; ++i) {
     const mcfl_run_desc &r = runs[i];
     if (r.photons == 0 || r.photons_per_voxel || r.fluence) return fail(MCFL_E_ARG, "noalloc: excitation images only");
+    if (r.tdet.nx || r.exact_stepping) return fail(MCFL_E_ARG, "noalloc: the reference's stepping, no time detectors");
     if (r.start_weight == 0) return fail(MCFL_E_ARG, "noalloc: start_weight must be given");
     if (r.det.nx != det.nx || r.det.ny != det.ny) return fail(MCFL_E_ARG, "noalloc: detectors must share a size");
     if (r.source.kind != MCFL_SOURCE_GAUSS_BEAM && r.source.kind != MCFL_SOURCE_WIDEFIELD)

@@ -98,6 +98,10 @@ int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run)
     if ((unsigned long long)td.nx * (unsigned long long)td.ny * (unsigned long long)td.bins >= (1ull << 31))
       return fail(MCFL_E_RANGE, "time-resolved tally too large");
   }
+  if (run->exact_stepping) {
+    if (m->layered) return fail(MCFL_E_ARG, "exact stepping: voxelized media only");
+    if (td.nx != 0) return fail(MCFL_E_ARG, "exact stepping: no time-resolved detectors");
+  }
   if (m->layered) {
     if (run->photons_per_voxel) return fail(MCFL_E_ARG, "layered medium: excitation runs only");
     bool inside = false;
@@ -335,8 +339,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
 
   unsigned long long *cnt = c->counters.as<unsigned long long>();
+  const bool exact = run->exact_stepping != 0;
   int block = 0, block_exc = 0;
-  const int grid = c->grid_for(true, &block);
+  const int grid = c->grid_for(true, &block, nullptr, false, exact);
   const int grid_exc = timed ? c->grid_for(true, &block_exc, nullptr, true) : grid;
   if (!timed) block_exc = block;
   const unsigned long long photons = run->photons;
@@ -364,6 +369,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.ticket_end = photons;
     set_uniform(c, L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
     L.time_on = timed ? 1u : 0u;
+    L.exact_step = exact ? 1u : 0u;
     REC(record_event(c->ev[0], st));
     REC(launch_fn(c->math)(&L, grid_exc, block_exc, st));
     ++*k;
@@ -397,7 +403,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
                                    (unsigned long long)block, c->step_cap, (unsigned long long)c->variant,
                                    (unsigned long long)c->l2_window, tsize, (unsigned long long)grid_exc,
-                                   (unsigned long long)block_exc});
+                                   (unsigned long long)block_exc, (unsigned long long)exact, m->serial});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
   if (rc != MCFL_OK) return rc;
 
@@ -476,6 +482,11 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
   const mcfl_medium *m = media[0];
   bool uniform = true;
   for (int i = 0; i < n; ++i) uniform = uniform && media[i] == m;
+  const bool exact = runs[0].exact_stepping != 0;
+  for (int i = 0; i < n; ++i)
+    if ((runs[i].exact_stepping != 0) != exact)
+      return fail(MCFL_E_ARG, "mcfl_batch_run: the runs of a batch share the stepping");
+  if (exact && !uniform) return fail(MCFL_E_ARG, "mcfl_batch_run: exact stepping over one medium only");
   for (int i = 0; i < n; ++i) {
     if (!media[i]) return fail(MCFL_E_ARG, "mcfl_batch_run: null medium");
     if (!uniform && media[i]->layered)
@@ -517,8 +528,8 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
     tickets += runs[i].photons;
   }
   int block = 0, block_one = 0;
-  const int grid = c->grid_for(uniform, &block);
-  const int grid_one = c->grid_for(true, &block_one); /* plain schedule: one medium per launch */
+  const int grid = c->grid_for(uniform, &block, nullptr, false, exact);
+  const int grid_one = c->grid_for(true, &block_one, nullptr, false, exact); /* plain schedule: one medium per launch */
   float ms = 0.f;
   if (schedule == MCFL_SCHEDULE_BATCHED) {
     auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -535,6 +546,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.ticket_end = tickets;
       if (uniform) set_uniform(c, L, m, false, nullptr);
       else L.variant = (uint32_t)c->mixed_variant;
+      L.exact_step = exact ? 1u : 0u;
       if ((e = record_event(c->ev[0], st))) return e;
       if ((e = launch_fn(c->math)(&L, grid, block, st)))
         return e;
@@ -546,7 +558,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
         ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
                  c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window,
-                 (unsigned long long)uniform});
+                 (unsigned long long)uniform, (unsigned long long)exact, m->serial});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
@@ -565,6 +577,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
       L.ticket_end = runs[i].photons;
       set_uniform(c, L, media[i], false, nullptr);
+      L.exact_step = exact ? 1u : 0u;
       MCFL_CUDA_TRY(c->launch_transport(L, grid_one, block_one));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
     }
@@ -685,7 +698,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   MCFL_CUDA_TRY(cudaMemcpyAsync(c->jobs.p, c->h_jobs, NL * sizeof(McflJob), cudaMemcpyHostToDevice, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(c->bcnt.p, 0, NL * 8 + 8, s));
   int block = 0;
-  const int grid = c->grid_for(true, &block);
+  const int grid = c->grid_for(true, &block, nullptr, false, run->exact_stepping != 0);
   MCFL_CUDA_TRY(cudaEventRecord(c->ev[2], s));
   for (size_t i = 0; i < NL; ++i) {
     McflLaunch L = base_launch(c);
@@ -694,6 +707,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
     L.ticket_end = run->photons_per_voxel;
     set_uniform(c, L, m, true, nullptr);
+    L.exact_step = run->exact_stepping ? 1u : 0u;
     MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
     MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulationFl */
   }
@@ -762,8 +776,9 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   L.ticket_counter = c->counters.as<unsigned long long>();
   L.ticket_end = run->photons;
   set_uniform(c, L, m, false, nullptr);
+  L.exact_step = run->exact_stepping ? 1u : 0u;
   int block = 0;
-  const int grid = c->grid_for(true, &block);
+  const int grid = c->grid_for(true, &block, nullptr, false, run->exact_stepping != 0);
   MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
   std::vector<unsigned long long> r(2 * xy), t(2 * xy);
   MCFL_CUDA_TRY(cudaMemcpyAsync(r.data(), c->R128.p, xy * 16, cudaMemcpyDeviceToHost, s));

@@ -433,6 +433,7 @@ extern "C" int mcfl_server_submit(mcfl_server *sv, const mcfl_medium_desc *mediu
   if (!sv || !medium || !run || !id) return fail(MCFL_E_ARG, "mcfl_server_submit: null argument");
   if (run->photons_per_voxel) return fail(MCFL_E_ARG, "server requests are excitation runs (photons_per_voxel = 0)");
   if (run->tdet.nx) return fail(MCFL_E_ARG, "server requests carry no time-resolved detectors (use mcfl_run)");
+  if (run->exact_stepping) return fail(MCFL_E_ARG, "server requests use the reference's stepping (exact stepping: mcfl_run)");
   if (run->photons == 0 || run->det.nx <= 0 || run->det.ny <= 0) return fail(MCFL_E_ARG, "bad run");
   if (!medium->labels || !medium->bulks || medium->n_bulks < 1 || medium->n_bulks > MCFL_MAX_BULKS)
     return fail(MCFL_E_ARG, "bad medium");

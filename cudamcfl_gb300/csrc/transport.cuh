@@ -138,6 +138,9 @@ struct Photon {
   real x, y, z, dx, dy, dz;
   uint32_t weight, label;
   uint64_t tof; /* time of flight [fs], time-of-flight kernels only */
+  /* voxel-boundary stepping only: the photon's voxel, or ingrid = 0 outside
+   * the grid's lateral extent (the medium of label 1) */
+  int ix, iy, iz, ingrid;
 };
 
 /* Time-of-flight increment (unsigned long)(v / c) of a path of optical
@@ -162,6 +165,7 @@ struct Med {
   unsigned long long *fhd;
   real hx, hy, esp, gx, gy, gz;
   uint32_t nx, ny, total, last;
+  uint32_t nz; /* voxel-boundary stepping only */
 };
 
 __device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
@@ -242,7 +246,20 @@ __device__ __forceinline__ uint32_t find_job(const McflJob *jobs, const uint32_t
   return (t >= b && t - b < n) ? slot : 0xffffffffu;
 }
 
-template <bool kLayered>
+/* The photon's voxel from its position (voxel-boundary stepping). */
+__device__ __forceinline__ void locate(Photon &p, const Med &m) {
+  if (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy) {
+    p.ix = (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
+    p.iy = (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
+    p.iz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
+    p.ingrid = 1;
+  } else {
+    p.ix = p.iy = p.iz = 0;
+    p.ingrid = 0;
+  }
+}
+
+template <int kMode>
 __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,
                                               Photon &p, Rng &r, uint32_t &src_idx) {
   mcfl_photon_stream(__ldg((const unsigned long long *)&J->key),
@@ -299,8 +316,19 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
     p.dz = MCFL_C(1.0);
     p.weight = __ldg(&J->start_weight);
   }
-  p.label = kLayered ? __ldg(&J->start_layer) : start_label(m, p);
+  p.label = kMode == 1 ? __ldg(&J->start_layer) : start_label(m, p);
   p.tof = 0;
+  if (kMode == 2) {
+    if (kind == MCFL_SRC_VOXELS) {
+      const uint32_t v = __ldg(&J->src_vox[src_idx]);
+      p.ix = (int)(v % m.nx);
+      p.iy = (int)((v / m.nx) % m.ny);
+      p.iz = (int)(v / (m.nx * m.ny));
+      p.ingrid = 1;
+    } else {
+      locate(p, m);
+    }
+  }
   /* The reference's first photon on each of its 32768 threads draws its first
    * passes from the stream state its launch started from, because
    * LaunchPhoton_Global does not store the advanced state
@@ -415,6 +443,61 @@ __device__ __forceinline__ bool reflect(Photon &p, real n1, real n2, Rng &r) {
   p.dy *= rr;
   p.dz = MCFL_COPYSIGN(MCFL_SQRT(1 - e), p.dz);
   return true;
+}
+
+/* Voxel-boundary stepping: distance along direction component d from
+ * coordinate c to plane b (FLT_MAX when the photon does not move towards it),
+ * never negative. */
+__device__ __forceinline__ real plane_dist(real b, real c, real d) {
+  if (d == MCFL_C(0.0)) return FLT_MAX;
+  const real t = (b - c) / d;
+  return t > MCFL_C(0.0) ? t : MCFL_C(0.0);
+}
+
+/* Fresnel reflection / refraction at a voxel face whose normal is axis a
+ * (0, 1, 2 = x, y, z): reflect() with that axis in place of z.  Returns true
+ * when the photon crosses. */
+__device__ __forceinline__ bool refract_axis(Photon &p, int a, real n1, real n2, Rng &r) {
+  /* the normal component and the two tangential ones, by value (no local
+   * memory), written back below */
+  real dn = a == 0 ? p.dx : (a == 1 ? p.dy : p.dz);
+  real t1 = a == 0 ? p.dy : (a == 1 ? p.dz : p.dx);
+  real t2 = a == 0 ? p.dz : (a == 1 ? p.dx : p.dy);
+  bool cross;
+  real rr;
+  const real cos_angle_i = MCFL_FABS(dn);
+  if (n1 == n2) return true;
+  if (n2 * n2 < n1 * n1 * (1 - cos_angle_i * cos_angle_i)) {
+    dn *= -MCFL_C(1.0);
+    cross = false;
+  } else if (cos_angle_i == MCFL_C(1.0)) {
+    rr = (n1 - n2) / (n1 + n2);
+    cross = !(r.co() <= rr * rr);
+    if (!cross) dn *= -MCFL_C(1.0);
+  } else {
+    real e = (n1 * n1) / (n2 * n2) * (MCFL_C(1.0) - cos_angle_i * cos_angle_i);
+    rr = 2 * MCFL_SQRT((MCFL_C(1.0) - cos_angle_i * cos_angle_i) * (MCFL_C(1.0) - e) * e * cos_angle_i * cos_angle_i);
+    e = e + (cos_angle_i * cos_angle_i) * (MCFL_C(1.0) - MCFL_C(2.0) * e);
+    rr = e * ((MCFL_C(1.0) - e - rr) / ((MCFL_C(1.0) - e + rr) * (e + rr)));
+    cross = !(r.co() <= rr);
+    if (!cross) {
+      dn *= -MCFL_C(1.0);
+    } else {
+      rr = n1 / n2;
+      e = rr * rr * (MCFL_C(1.0) - cos_angle_i * cos_angle_i);
+      t1 *= rr;
+      t2 *= rr;
+      dn = MCFL_COPYSIGN(MCFL_SQRT(1 - e), dn);
+    }
+  }
+  if (a == 0) {
+    p.dx = dn; p.dy = t1; p.dz = t2;
+  } else if (a == 1) {
+    p.dy = dn; p.dz = t1; p.dx = t2;
+  } else {
+    p.dz = dn; p.dx = t1; p.dy = t2;
+  }
+  return cross;
 }
 
 /* Scattering-free voxels: march in half-voxel steps to the next label, then
@@ -563,8 +646,12 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
 /* One warp-synchronous persistent loop per thread; see the file comment.
  * kUniform: the medium comes from the launch parameters (constant bank)
  * instead of per-lane registers loaded from the job. */
-template <bool kUniform, bool kTime, bool kLayered, int kThreads, int kMinBlocks>
+/* kMode: 0 = the reference's voxelized transport (MCd3D), 1 = layered media
+ * (MCd), 2 = voxel-boundary ("exact") stepping. */
+template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
+  constexpr bool kLayered = kMode == 1;
+  constexpr bool kExactStep = kMode == 2;
   /* shared memory: kEv x blockDim.x event counters, then (uniform medium)
    * the label records of the medium */
   extern __shared__ unsigned long long s_ev[];
@@ -625,6 +712,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     m.ny = L.med.ny;
     m.total = L.med.total;
     m.last = L.med.last_label;
+    if (kExactStep) m.nz = m.total / (m.nx * m.ny);
   }
   Rec rc = {}; /* general kernel: the record of the photon's label, in registers */
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
@@ -702,7 +790,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             }
             k = __ldg((const unsigned long long *)&J->photon_base) +
                 (t - __ldg((const unsigned long long *)&J->ticket_begin));
-            launch_photon<kLayered>(J, m, k, L.mult, p, r, src_idx);
+            launch_photon<kMode>(J, m, k, L.mult, p, r, src_idx);
             if (!kUniform) rc = load_rec(m, p.label);
             pst = 0;
             pst0 = 0;
@@ -722,7 +810,125 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
 
     ++pst;
-    if constexpr (kLayered) {
+    if constexpr (kExactStep) {
+      /* ---- one pass with voxel-boundary stepping: the optical depth
+       * -ln(u) is spent voxel by voxel with each voxel's mu_t, the label is
+       * the one where the photon is, Fresnel acts at every face between
+       * different indices with that face's normal, scattering-free voxels
+       * are crossed without interaction.  The pass ends at the interaction
+       * (PHD tally, weight drop, spin, as the reference's pass) or at an
+       * exit. ---- */
+      real tau = -MCFL_LOGF(r.oc());
+      const int cap = 16 + 4 * (int)(m.nx + m.ny + m.nz);
+      bool interact = false;
+      for (int itv = 0;; ++itv) {
+        const Rec c = Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]};
+        const bool glass = c.a.x == FLT_MAX;
+        real db = FLT_MAX;
+        int axis = -1;
+        real t;
+        if (itv >= cap) break; /* cannot reach an interaction: lost below */
+        if (p.ingrid) {
+          const real bx = (real)(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix) / m.gx - m.hx;
+          t = plane_dist(bx, p.x, p.dx);
+          if (t < db) { db = t; axis = 0; }
+          const real by = (real)(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy) / m.gy - m.hy;
+          t = plane_dist(by, p.y, p.dy);
+          if (t < db) { db = t; axis = 1; }
+          const int kz = p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz;
+          const real bz = kz == 0 ? MCFL_C(0.0) : (kz == (int)m.nz ? m.esp : (real)kz / m.gz);
+          t = plane_dist(bz, p.z, p.dz);
+          if (t < db) { db = t; axis = 2; }
+        } else {
+          t = plane_dist(p.dz > MCFL_C(0.0) ? m.esp : MCFL_C(0.0), p.z, p.dz);
+          if (t < db) { db = t; axis = 2; }
+          if ((p.x <= -m.hx && p.dx > MCFL_C(0.0)) || (p.x >= m.hx && p.dx < MCFL_C(0.0))) {
+            t = plane_dist(p.dx > MCFL_C(0.0) ? -m.hx : m.hx, p.x, p.dx);
+            const real yc = p.y + p.dy * t;
+            if (t < db && MCFL_FABS(yc) < m.hy) { db = t; axis = 0; }
+          }
+          if ((p.y <= -m.hy && p.dy > MCFL_C(0.0)) || (p.y >= m.hy && p.dy < MCFL_C(0.0))) {
+            t = plane_dist(p.dy > MCFL_C(0.0) ? -m.hy : m.hy, p.y, p.dy);
+            const real xc = p.x + p.dx * t;
+            if (t < db && MCFL_FABS(xc) < m.hx) { db = t; axis = 1; }
+          }
+        }
+        if (!glass) {
+          const real s_int = tau * c.a.x;
+          if (s_int <= db) {
+            p.x += p.dx * s_int;
+            p.y += p.dy * s_int;
+            p.z += p.dz * s_int;
+            interact = true;
+            break;
+          }
+        }
+        if (axis < 0) break; /* scattering-free with no face ahead: lost below */
+        p.x += p.dx * db;
+        p.y += p.dy * db;
+        p.z += p.dz * db;
+        if (!glass) {
+          tau -= db / c.a.x;
+          if (tau < MCFL_C(0.0)) tau = MCFL_C(0.0);
+        }
+        int nix = p.ix, niy = p.iy, niz = p.iz, nin = p.ingrid;
+        uint32_t next;
+        if (p.ingrid) {
+          if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
+          else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
+          else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
+          if (niz < 0) next = 0u;
+          else if (niz >= (int)m.nz) next = m.last;
+          else if (nix < 0 || nix >= (int)m.nx || niy < 0 || niy >= (int)m.ny) {
+            next = 1u;
+            nin = 0;
+          } else {
+            next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
+          }
+        } else if (axis == 2) {
+          next = p.dz > MCFL_C(0.0) ? m.last : 0u;
+        } else {
+          nin = 1;
+          nix = axis == 0 ? (p.dx > MCFL_C(0.0) ? 0 : (int)m.nx - 1)
+                          : (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
+          niy = axis == 1 ? (p.dy > MCFL_C(0.0) ? 0 : (int)m.ny - 1)
+                          : (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
+          niz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
+          next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
+        }
+        if (next != p.label && !refract_axis(p, axis, c.b.w, s_lab[2 * next + 1].w, r)) continue;
+        p.label = next;
+        p.ix = nix;
+        p.iy = niy;
+        p.iz = niz;
+        p.ingrid = nin;
+        if (next == 0u || next == m.last) {
+          const bool top = next == 0u;
+          tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+          ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+          p.weight = 0u;
+          break;
+        }
+      }
+      if (interact) {
+        if (m.fhd && p.ingrid)
+          atomicAdd(&m.fhd[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)],
+                    (unsigned long long)p.weight);
+        const Rec c2 = Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]};
+        const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
+        if (w > 0u) {
+          p.weight -= w;
+          absorbed += w;
+        } else {
+          ev_add(MCFL_ST_W0_LOSS, p.weight);
+          p.weight = 0u;
+        }
+        spin(p, c2, r);
+      } else if (p.weight) { /* lost without interaction (cap or no face ahead) */
+        ev_add(MCFL_ST_W0_LOSS, p.weight);
+        p.weight = 0u;
+      }
+    } else if constexpr (kLayered) {
       /* ---- one transport pass of a layered medium (MCd loop body,
        * CUDAMCFLtransport.cu:73-233) ---- */
       const uint32_t nl = L.med.n_layers;
@@ -905,7 +1111,7 @@ static size_t smem_bytes(int block, bool uniform) {
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
- * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
+ * of flight; voxel-boundary stepping 6 = 256 x 4.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
  * -2 = 256 x 2 with the time of flight. */
 typedef void (*TransportKernel)(McflLaunch);
 
@@ -914,16 +1120,17 @@ static int mixed_variant_code(uint32_t v) { return v == 1 ? -3 : v == 2 ? -4 : -
 
 static TransportKernel kernel_of(int variant, int *threads) {
   switch (variant) {
-  case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, false, 256, 2>;
-  case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, false, 256, 3>;
-  case -3: *threads = 256; return MCFL_KERNEL_NAME<false, false, false, 256, 4>;
-  case -4: *threads = 128; return MCFL_KERNEL_NAME<false, false, false, 128, 7>;
-  case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 4>;
-  case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, false, 256, 5>;
-  case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, false, 128, 9>;
-  case 3: *threads = 256; return MCFL_KERNEL_NAME<true, true, false, 256, 3>;
-  case 4: *threads = 256; return MCFL_KERNEL_NAME<true, false, true, 256, 4>;
-  case 5: *threads = 256; return MCFL_KERNEL_NAME<true, true, true, 256, 3>;
+  case -2: *threads = 256; return MCFL_KERNEL_NAME<false, true, 0, 256, 2>;
+  case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 3>;
+  case -3: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 4>;
+  case -4: *threads = 128; return MCFL_KERNEL_NAME<false, false, 0, 128, 7>;
+  case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4>;
+  case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5>;
+  case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9>;
+  case 3: *threads = 256; return MCFL_KERNEL_NAME<true, true, 0, 256, 3>;
+  case 4: *threads = 256; return MCFL_KERNEL_NAME<true, false, 1, 256, 4>;
+  case 5: *threads = 256; return MCFL_KERNEL_NAME<true, true, 1, 256, 3>;
+  case 6: *threads = 256; return MCFL_KERNEL_NAME<true, false, 2, 256, 4>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -941,7 +1148,8 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
   if (L->max_iters && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
   if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
     return cudaErrorInvalidValue;
-  const int v = L->med.layered ? (L->time_on ? 5 : 4)
+  const int v = L->exact_step ? 6
+                : L->med.layered ? (L->time_on ? 5 : 4)
                 : L->uniform_medium ? (L->time_on ? 3 : (int)L->variant)
                 : L->time_on        ? -2
                                     : mixed_variant_code(L->variant);

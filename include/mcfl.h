@@ -270,6 +270,17 @@ typedef struct mcfl_run_desc {
    * over disjoint index ranges of one seed (on one GPU or several) sum to the
    * run over their union bit for bit.  0 for a whole run. */
   unsigned long long photon_offset;
+  /* 1: voxel-boundary stepping: the optical depth -ln(u) of a pass is spent
+   * voxel by voxel with each voxel's mu_t, the hitting density and the
+   * weight drop use the voxel where the interaction happens, Fresnel acts at
+   * every face between different refractive indices with that face's
+   * normal, and scattering-free voxels are crossed without interaction.
+   * 0: the reference's stepping (the whole pass with the start voxel's mu_t,
+   * the label looked up at the end point, z as the Fresnel normal;
+   * CUDAMCFLtransport.cu:280-352).  Voxelized media; mcfl_run (excitation
+   * and emission) and mcfl_batch_run over one medium; not with time-resolved
+   * detectors, and not through the server or the allocation-free entry. */
+  int exact_stepping;
 } mcfl_run_desc;
 
 #define MCFL_NSTATS 9

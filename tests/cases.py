@@ -26,6 +26,8 @@ class Case:
     do_fl: int = 1
     # time-resolved detectors: (x0, y0, nx, ny, sep_x, sep_y, radius, face, bins, max_fs) or None
     temporal: tuple | None = None
+    # 1: voxel-boundary stepping in both the oracle and the engine
+    exact_stepping: int = 0
 
     @property
     def dims(self):
@@ -65,6 +67,7 @@ class Case:
         lab = np.ascontiguousarray(self.labels.astype(np.int16))
         s.bulk_info = lab.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_short))
         s._keep = lab
+        s.exact_stepping = self.exact_stepping
         if self.temporal:
             x0, y0, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
             s.do_temp_sim = 1
@@ -84,7 +87,8 @@ class Case:
         return mc.run_desc(photons or self.photons, source=self.source, det=mc.Detector(x0, y0, dx, dy, nx, ny),
                            photons_per_voxel=self.per_voxel if self.do_fl else 0,
                            fluence=1 if self.do_fl in (1, 2) else 0, seed_exc=seed_exc, seed_fl=seed_fl,
-                           start_weight=self.start_weight(), tdet=self.temporal)
+                           start_weight=self.start_weight(), tdet=self.temporal,
+                           exact_stepping=self.exact_stepping)
 
     def write_mci(self, d: str) -> str:
         """Writes <d>/<name>.mci and its bulk file in the reference's grammar."""
@@ -193,6 +197,16 @@ def mismatch_timed(photons=40000, per_voxel=40000) -> Case:
 
 def glass_timed_exit(photons=40000, per_voxel=40000) -> Case:
     return timed(photons, per_voxel, 1, glass)
+
+
+def exact(base):
+    """A case with voxel-boundary stepping in both the oracle and the engine."""
+    def make(photons=40000, per_voxel=40000) -> Case:
+        c = base(photons, per_voxel)
+        c.name = c.name + "_exact"
+        c.exact_stepping = 1
+        return c
+    return make
 
 
 ALL = {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere, "mismatch_timed": mismatch_timed,
@@ -307,3 +321,7 @@ def layered_timed_exit(photons=40000, per_voxel=40000) -> LayeredCase:
 
 
 LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}
+
+# voxel-boundary stepping (no time-resolved detectors on this path)
+EXACT = {n + "_exact": exact(f) for n, f in {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere,
+                                              "deep": deep}.items()}

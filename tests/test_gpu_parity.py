@@ -417,3 +417,71 @@ def test_photon_offset_shards_sum_to_the_whole_run(gpu_ctx):
         assert np.array_equal(getattr(parts[0], k) + getattr(parts[1], k), getattr(whole, k)), k
     for k in STAT_ORDER + ("steps", "done"):
         assert parts[0].stats_exc[k] + parts[1].stats_exc[k] == whole.stats_exc[k], k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(cases.EXACT))
+def test_voxel_boundary_stepping_bit_identical_to_oracle(name, gpu_ctx, oracle, table32768):
+    """Voxel-boundary stepping (mu_t spent voxel by voxel, Fresnel with each
+    face's normal, scattering-free voxels crossed): the exact-math kernel
+    against the oracle's restatement, excitation and emission, bit for bit."""
+    case = cases.EXACT[name](photons=20000, per_voxel=500)
+    ref = oracle.run_photon(case.oracle_sim(), table32768, 11, 22, libm=False)
+    med = case.engine_medium(gpu_ctx)
+    res = gpu_ctx.run(med, case.run_desc(11, 22))
+    med.free()
+    _compare(res, ref)
+    assert ref.fl_voxels > 0
+
+
+@pytest.mark.gpu
+def test_voxel_boundary_stepping_inputs_fail_with_status(gpu_ctx):
+    """Exact stepping has no time-resolved tallies and no layered media; a
+    batch shares one stepping; the server runs the reference's stepping."""
+    tc = cases.mismatch_timed()
+    med = tc.engine_medium(gpu_ctx)
+    rd = tc.run_desc(1, 2)
+    rd.exact_stepping = 1
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.run(med, rd)
+    assert e.value.code == mc.E_ARG
+    a = cases.mismatch().run_desc(1, 2)
+    a.photons_per_voxel, a.fluence = 0, 0
+    b = cases.mismatch().run_desc(3, 4)
+    b.photons_per_voxel, b.fluence = 0, 0
+    b.exact_stepping = 1
+    with pytest.raises(mc.McflError) as e:
+        mc.batch_run(gpu_ctx, med, [a, b])
+    assert e.value.code == mc.E_ARG
+    med.free()
+    lc = cases.layered()
+    lm = lc.engine_medium(gpu_ctx)
+    rd = lc.run_desc(1, 2)
+    rd.exact_stepping = 1
+    with pytest.raises(mc.McflError) as e:
+        gpu_ctx.run(lm, rd)
+    assert e.value.code == mc.E_ARG
+    lm.free()
+
+
+@pytest.mark.gpu
+def test_voxel_boundary_stepping_batch_equals_alone(gpu_ctx):
+    """Batched and plain schedules of exact-stepping runs equal each run
+    alone, bit for bit."""
+    case = cases.mismatch()
+    med = case.engine_medium(gpu_ctx)
+    dx, dy, nx, ny, x0, y0 = case.det
+    det = mc.Detector(x0, y0, dx, dy, nx, ny)
+    budgets = [5000, 17000, 1, 900]
+    runs = [mc.run_desc(b, source=(0.1 * i - 0.15, 0.05, 0.0), det=det, seed_exc=40 + i,
+                        start_weight=case.start_weight(), exact_stepping=1) for i, b in enumerate(budgets)]
+    bat, _ = mc.batch_run(gpu_ctx, med, runs, mc.SCHEDULE_BATCHED)
+    pla, _ = mc.batch_run(gpu_ctx, med, runs, mc.SCHEDULE_PLAIN)
+    for i, rd in enumerate(runs):
+        one = gpu_ctx.run(med, rd, images=True, raw=True)
+        for r in (bat[i], pla[i]):
+            assert np.array_equal(r["Rd"], one.Rd) and np.array_equal(r["Tt"], one.Tt)
+            assert r["stats"]["done"] == budgets[i]
+            assert r["stats"]["steps"] == one.stats_exc["steps"]
+            assert r["stats"]["absorbed"] == one.stats_exc["absorbed"]
+    med.free()

@@ -160,3 +160,19 @@ def test_server_rejects_request_above_budget(gpu_ctx):
     finally:
         srv.close()
         ctx2.close()
+
+
+@pytest.mark.gpu
+def test_recorded_graph_follows_a_new_medium_at_a_reused_address(gpu_ctx, oracle, table32768):
+    """Media freed and created in turn (the allocator may hand a new medium
+    the old one's address; the label counts differ) never replay the previous
+    medium's recorded graph: every run equals the oracle."""
+    from tests.test_gpu_parity import _compare
+    for make in (cases.tiny, cases.glass, cases.tiny, cases.mismatch, cases.glass):
+        case = make(photons=3000, per_voxel=0)
+        case.do_fl = 2
+        ref = oracle.run_photon(case.oracle_sim(), table32768, 12, 13, libm=False)
+        med = case.engine_medium(gpu_ctx)
+        res = gpu_ctx.run(med, case.run_desc(12, 13))
+        med.free()
+        _compare(res, ref, emission=False)

@@ -182,3 +182,33 @@ def test_integrated_within_0p1_percent_of_reference_streams(oracle, safeprimes_f
             assert out["rel_diff"] < 1e-3, (reuse, k, out)
     med.free()
     ctx.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("math", [mc.MATH_EXACT, mc.MATH_FAST])
+def test_voxel_boundary_stepping_agrees_with_independent_slab_mc(math):
+    """Two index-mismatched slabs as a laterally wide voxel grid: the engine's
+    voxel-boundary stepping gives the reflectance, transmittance and absorbed
+    fraction of the independent layered-slab Monte Carlo (tests/slab_mc.py)
+    within 3 sigma."""
+    from tests import slab_mc
+    layers = [(0.04, 1.0, 100.0, 0.9, 1.37), (0.06, 0.5, 80.0, 0.8, 1.5)]
+    lab = np.ones((10, 8, 8), np.uint8)
+    lab[4:] = 2
+    bulks = [mc.outer_bulk(1.0)] + [mc.bulk_from_mci_columns(l[4], l[1], l[2], g=l[3]) for l in layers] + \
+        [mc.outer_bulk(1.0)]
+    ctx = mc.Context(math=math)
+    try:
+        med = ctx.medium(lab, bulks, vox_per_cm=(0.1, 0.1, 100.0), half_x=40.0, half_y=40.0, thickness=0.1)
+        det = mc.Detector(0.0, 0.0, 0.1, 0.1, 10, 10)
+        runs = [mc.run_desc(200_000, det=det, seed_exc=77 + b, exact_stepping=1) for b in range(B)]
+        res, _ = mc.batch_run(ctx, med, runs)
+        med.free()
+    finally:
+        ctx.close()
+    n1, n2 = np.float64(np.float32(1.0)), np.float64(np.float32(1.37))
+    w0 = int(np.float64(0xFFFFFFFF) * (1 - ((n1 - n2) / (n1 + n2)) ** 2))
+    eng = np.array([[r["stats"][k] / (200_000 * w0) for k in ("exit_top", "exit_bottom", "absorbed")] for r in res])
+    ref = np.array([slab_mc.run(layers, 1.0, 1.0, 20000, 4100 + b) for b in range(B)])
+    for i in range(3):
+        stats.scalar_gate(eng[:, i], ref[:, i])

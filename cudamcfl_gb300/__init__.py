@@ -46,7 +46,7 @@ class McflError(RuntimeError):
 # ----------------------------------------------------------------- structs
 
 class Bulk(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_float) for n in ("mutr", "mua", "g", "n", "flc", "muaf", "eY", "albedof")]
+    _fields_ = [(n, ctypes.c_float) for n in ("mutr", "mua", "g", "n", "flc", "muaf", "eY", "albedof", "mus")]
 
 
 class Layer(ctypes.Structure):
@@ -246,11 +246,11 @@ def bulk_from_mci_columns(n: float, mua: float, mus: float, flc: float = 0.0, ab
     mutr = f(np.finfo(np.float32).max) if mus == 0 else f(f(1.0) / f(mua + mus))
     with np.errstate(invalid="ignore", divide="ignore"):  # mus = flc = 0 gives 0/0 = NaN, as in the reference
         albedof = f(mus / f(f(flc * ax) + mus))
-    return Bulk(mutr, f(mua + f(flc * ax)), g, n, flc, f(mua + f(flc * am)), eY, albedof)
+    return Bulk(mutr, f(mua + f(flc * ax)), g, n, flc, f(mua + f(flc * am)), eY, albedof, mus)
 
 
 def outer_bulk(n: float = 1.0) -> Bulk:
-    return Bulk(float(np.finfo(np.float32).max), 0.0, 1.0, n, 0.0, 0.0, 0.0, 0.0)
+    return Bulk(float(np.finfo(np.float32).max), 0.0, 1.0, n, 0.0, 0.0, 0.0, 0.0, 0.0)
 
 
 def layers_from_mci_columns(n_up: float, slabs, n_down: float) -> list:

@@ -264,6 +264,14 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
   const int nl = d->n_bulks + 2;
   std::vector<float> pe(4 * (size_t)nl), pm(4 * (size_t)nl), fl(2 * (size_t)nl);
   std::vector<float> le(MCFL_LAB_FLOATS * (size_t)nl), lm(MCFL_LAB_FLOATS * (size_t)nl);
+  std::vector<float> pex(pe.size()), pmx(pm.size()), lex(le.size()), lmx(lm.size());
+  /* voxel-boundary stepping spends the optical depth with the physical mu_t
+   * of the phase's wavelength, the fluorophore's absorption included; the
+   * reference's stepping keeps 1/(mua + mus) of the .mci column at both */
+  auto inv_mut = [](float mua, float mus) {
+    const float mut = mua + mus;
+    return mut == 0.0f ? FLT_MAX : 1.0f / mut;
+  };
   for (int i = 0; i < nl; ++i) {
     const mcfl_bulk &b = d->bulks[i];
     pe[4 * i + 0] = b.mutr; pe[4 * i + 1] = b.mua; pe[4 * i + 2] = b.g; pe[4 * i + 3] = b.n;
@@ -271,6 +279,11 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
     fl[2 * i + 0] = b.eY; fl[2 * i + 1] = b.albedof;
     mcfl_label_record(b.mutr, b.mua, b.g, b.n, &le[MCFL_LAB_FLOATS * (size_t)i]);
     mcfl_label_record(b.mutr, b.muaf, b.g, b.n, &lm[MCFL_LAB_FLOATS * (size_t)i]);
+    const float tx = inv_mut(b.mua, b.mus), tm = inv_mut(b.muaf, b.mus);
+    pex[4 * i + 0] = tx; pex[4 * i + 1] = b.mua; pex[4 * i + 2] = b.g; pex[4 * i + 3] = b.n;
+    pmx[4 * i + 0] = tm; pmx[4 * i + 1] = b.muaf; pmx[4 * i + 2] = b.g; pmx[4 * i + 3] = b.n;
+    mcfl_label_record(tx, b.mua, b.g, b.n, &lex[MCFL_LAB_FLOATS * (size_t)i]);
+    mcfl_label_record(tm, b.muaf, b.g, b.n, &lmx[MCFL_LAB_FLOATS * (size_t)i]);
   }
   cudaError_t e = m->labels.reserve(total);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->labels.p, d->labels, total, cudaMemcpyHostToDevice, c->stream);
@@ -282,6 +295,14 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->lab_exc.p, le.data(), le.size() * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = m->lab_emi.reserve(lm.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->lab_emi.p, lm.data(), lm.size() * 4, cudaMemcpyHostToDevice, c->stream);
+  auto put = [&](mcfl::DevBuf &dst, const std::vector<float> &src) {
+    cudaError_t r = dst.reserve(src.size() * 4);
+    return r == cudaSuccess ? cudaMemcpyAsync(dst.p, src.data(), src.size() * 4, cudaMemcpyHostToDevice, c->stream) : r;
+  };
+  if (e == cudaSuccess) e = put(m->prop_exc_x, pex);
+  if (e == cudaSuccess) e = put(m->prop_emi_x, pmx);
+  if (e == cudaSuccess) e = put(m->lab_exc_x, lex);
+  if (e == cudaSuccess) e = put(m->lab_emi_x, lmx);
   if (e == cudaSuccess) e = m->fl.reserve(fl.size() * 4);
   if (e == cudaSuccess) e = cudaMemcpyAsync(m->fl.p, fl.data(), fl.size() * 4, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess && d->fluor_map) {
@@ -295,7 +316,8 @@ extern "C" int mcfl_medium_create(mcfl_ctx *c, const mcfl_medium_desc *d, mcfl_m
     return cuda_fail(e, "mcfl_medium_create");
   }
   m->bytes = m->labels.bytes + m->prop_exc.bytes + m->prop_emi.bytes + m->lab_exc.bytes + m->lab_emi.bytes +
-             m->fl.bytes + m->fmap.bytes;
+             m->prop_exc_x.bytes + m->prop_emi_x.bytes + m->lab_exc_x.bytes + m->lab_emi_x.bytes + m->fl.bytes +
+             m->fmap.bytes;
   *out = m;
   return MCFL_OK;
 }

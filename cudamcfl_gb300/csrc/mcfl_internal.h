@@ -104,6 +104,15 @@ struct mcfl_medium {
    * medium's geometry by value, and a freed medium's address can come back */
   unsigned long long serial = 0;
   mcfl::DevBuf labels, prop_exc, prop_emi, lab_exc, lab_emi, fl, fmap;
+  /* voxel-boundary stepping: 1/mu_t with mu_t = mua + mus at excitation and
+   * muaf + mus at emission (the fluorophore's absorption included) */
+  mcfl::DevBuf prop_exc_x, prop_emi_x, lab_exc_x, lab_emi_x;
+  const float *prop_of(bool emission, bool exact) const {
+    return (exact ? (emission ? prop_emi_x : prop_exc_x) : (emission ? prop_emi : prop_exc)).as<float>();
+  }
+  const float *lab_of(bool emission, bool exact) const {
+    return (exact ? (emission ? lab_emi_x : lab_exc_x) : (emission ? lab_emi : lab_exc)).as<float>();
+  }
   int nx = 0, ny = 0, nz = 0;
   uint32_t total = 0;
   float hx = 0, hy = 0, esp = 0, gx = 0, gy = 0, gz = 0;

@@ -90,6 +90,7 @@ void set_bulk(mcfl_bulk &b, const float *t) {
   b.g = t[7];
   b.mutr = t[2] == 0.0f ? FLT_MAX : 1.0f / (t[1] + t[2]);
   b.albedof = t[2] / (t[3] * t[4] + t[2]);
+  b.mus = t[2];
 }
 
 void set_outer(mcfl_bulk &b, float n) {

@@ -36,10 +36,12 @@ unsigned int default_start_weight(const mcfl_medium *m) {
   return (unsigned int)((double)0xFFFFFFFF * (1 - r));
 }
 
-void fill_medium(McflJob &j, const mcfl_medium *m, bool emission) {
+/* exact: the label records of voxel-boundary stepping (mu_t with the
+ * fluorophore's absorption at the phase's wavelength) */
+void fill_medium(McflJob &j, const mcfl_medium *m, bool emission, bool exact = false) {
   j.labels = m->labels.as<uint8_t>();
-  j.prop = emission ? m->prop_emi.as<float>() : m->prop_exc.as<float>();
-  j.lab = emission ? m->lab_emi.as<float>() : m->lab_exc.as<float>();
+  j.prop = m->prop_of(emission, exact);
+  j.lab = m->lab_of(emission, exact);
   j.hx = m->hx;
   j.hy = m->hy;
   j.esp = m->esp;
@@ -221,7 +223,8 @@ McflLaunch base_launch(mcfl_ctx *c) {
 
 /* Every job of the launch uses medium m with one photon-hitting-density
  * tally (or none): the medium travels in the kernel parameters. */
-void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool emission, unsigned long long *fhd) {
+void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool emission, unsigned long long *fhd,
+                 bool exact = false) {
   L.uniform_medium = 1;
   if (c->l2_window && c->l2_max_window) {
     const size_t bytes = std::min<size_t>(m->labels.bytes, c->l2_max_window);
@@ -231,8 +234,8 @@ void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool em
   }
   McflMedium &u = L.med;
   u.labels = m->labels.as<uint8_t>();
-  u.prop = emission ? m->prop_emi.as<float>() : m->prop_exc.as<float>();
-  u.lab = emission ? m->lab_emi.as<float>() : m->lab_exc.as<float>();
+  u.prop = m->prop_of(emission, exact);
+  u.lab = m->lab_of(emission, exact);
   u.n_labels = (uint32_t)m->n_bulks + 2u;
   u.fhd = fhd;
   u.hx = m->hx;
@@ -298,7 +301,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   McflJob *jobs = c->h_jobs;
   std::memset(jobs, 0, 2 * sizeof(McflJob));
   McflJob &je = jobs[0];
-  fill_medium(je, m, false);
+  fill_medium(je, m, false, run->exact_stepping != 0);
   fill_detector(je, det);
   fill_source(je, *run, m);
   je.fhd_on = fluence ? 1u : 0u;
@@ -324,7 +327,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   }
   if (emission) {
     McflJob &jf = jobs[1];
-    fill_medium(jf, m, true);
+    fill_medium(jf, m, true, run->exact_stepping != 0);
     fill_detector(jf, det);
     jf.src_kind = MCFL_SRC_VOXELS;
     jf.src_vox = c->vox.as<uint32_t>();
@@ -367,7 +370,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
     L.n_jobs = 1;
     L.ticket_counter = cnt + 0;
     L.ticket_end = photons;
-    set_uniform(c, L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr);
+    set_uniform(c, L, m, false, fluence ? c->fhd.as<unsigned long long>() : nullptr, exact);
     L.time_on = timed ? 1u : 0u;
     L.exact_step = exact ? 1u : 0u;
     REC(record_event(c->ev[0], st));
@@ -385,7 +388,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       Lf.jobs = c->jobs.as<McflJob>() + 1;
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
-      set_uniform(c, Lf, m, true, nullptr);
+      set_uniform(c, Lf, m, true, nullptr, exact);
       REC(record_event(c->ev[2], st));
       REC(launch_fn(c->math)(&Lf, grid, block, st));
       ++*k;
@@ -514,7 +517,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
   unsigned long long tickets = 0;
   for (int i = 0; i < n; ++i) {
     McflJob &j = jobs[i];
-    fill_medium(j, media[i], false);
+    fill_medium(j, media[i], false, exact);
     fill_detector(j, runs[i].det);
     fill_source(j, runs[i], media[i]);
     j.R = c->bR.as<unsigned long long>() + i * xy;
@@ -544,7 +547,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.n_jobs = (uint32_t)n;
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
-      if (uniform) set_uniform(c, L, m, false, nullptr);
+      if (uniform) set_uniform(c, L, m, false, nullptr, exact);
       else L.variant = (uint32_t)c->mixed_variant;
       L.exact_step = exact ? 1u : 0u;
       if ((e = record_event(c->ev[0], st))) return e;
@@ -576,7 +579,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.n_jobs = 1;
       L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
       L.ticket_end = runs[i].photons;
-      set_uniform(c, L, media[i], false, nullptr);
+      set_uniform(c, L, media[i], false, nullptr, exact);
       L.exact_step = exact ? 1u : 0u;
       MCFL_CUDA_TRY(c->launch_transport(L, grid_one, block_one));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
@@ -678,7 +681,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   MCFL_CUDA_TRY(ensure_pinned(c, NL + 2, 2 * MCFL_ST_COUNT + 8));
   McflJob t;
   std::memset(&t, 0, sizeof(t));
-  fill_medium(t, m, true);
+  fill_medium(t, m, true, run->exact_stepping != 0);
   fill_detector(t, det);
   t.src_kind = MCFL_SRC_VOXELS;
   t.per_voxel = run->photons_per_voxel;
@@ -706,7 +709,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
     L.n_jobs = 1;
     L.ticket_counter = c->bcnt.as<unsigned long long>() + i;
     L.ticket_end = run->photons_per_voxel;
-    set_uniform(c, L, m, true, nullptr);
+    set_uniform(c, L, m, true, nullptr, run->exact_stepping != 0);
     L.exact_step = run->exact_stepping ? 1u : 0u;
     MCFL_CUDA_TRY(c->launch_transport(L, grid, block));
     MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulationFl */
@@ -757,7 +760,7 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   MCFL_CUDA_TRY(cudaMemsetAsync(c->counters.p, 0, 8, s));
   McflJob j;
   std::memset(&j, 0, sizeof(j));
-  fill_medium(j, m, false);
+  fill_medium(j, m, false, run->exact_stepping != 0);
   fill_detector(j, det);
   j.src_kind = MCFL_SRC_VOXELS;
   j.src_vox = c->vox.as<uint32_t>();
@@ -775,7 +778,7 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   L.n_jobs = 1;
   L.ticket_counter = c->counters.as<unsigned long long>();
   L.ticket_end = run->photons;
-  set_uniform(c, L, m, false, nullptr);
+  set_uniform(c, L, m, false, nullptr, run->exact_stepping != 0);
   L.exact_step = run->exact_stepping ? 1u : 0u;
   int block = 0;
   const int grid = c->grid_for(true, &block, nullptr, false, run->exact_stepping != 0);

@@ -53,10 +53,15 @@ enum {
 
 /* BulkStruct, CUDAMCFL.h:116-127.  Entry 0 is the medium above the slab,
  * entry n_bulks+1 the medium below; mutr = 1/(mua + mus) or FLT_MAX when
- * mus = 0.  mua is the excitation absorption (mua + flc*AbsCExi), muaf the
- * emission absorption (mua + flc*AbsCEmi), albedof = mus/(flc*AbsCExi + mus). */
+ * mus = 0 (mua of the .mci column, without the fluorophore: the reference's
+ * mu_t at both wavelengths).  mua is the excitation absorption
+ * (mua + flc*AbsCExi), muaf the emission absorption (mua + flc*AbsCEmi),
+ * albedof = mus/(flc*AbsCExi + mus).  mus (not in BulkStruct) is the
+ * scattering coefficient: voxel-boundary stepping takes mu_t = mua + mus at
+ * excitation and muaf + mus at emission from it (0 with mua = 0: transparent). */
 typedef struct mcfl_bulk {
   float mutr, mua, g, n, flc, muaf, eY, albedof;
+  float mus;
 } mcfl_bulk;
 
 /* LayerStruct, CUDAMCFL.h:38-52 (bulk method 1). */
@@ -271,7 +276,9 @@ typedef struct mcfl_run_desc {
    * run over their union bit for bit.  0 for a whole run. */
   unsigned long long photon_offset;
   /* 1: voxel-boundary stepping: the optical depth -ln(u) of a pass is spent
-   * voxel by voxel with each voxel's mu_t, the hitting density and the
+   * voxel by voxel with each voxel's mu_t (mua + mus at excitation, muaf +
+   * mus at emission: the fluorophore's absorption included), the hitting
+   * density and the
    * weight drop use the voxel where the interaction happens, Fresnel acts at
    * every face between different refractive indices with that face's
    * normal, and scattering-free voxels are crossed without interaction.

@@ -47,6 +47,7 @@ typedef struct oracle_result {
 #define ORACLE_MAX_BULKS 100
 typedef struct oracle_bulk {
   float mutr, mua, g, n, flc, muaf, eY, albedof;
+  float mus; /* scattering coefficient: mu_t of voxel-boundary stepping */
 } oracle_bulk;
 
 #define ORACLE_MAX_LAYERS 100

@@ -845,9 +845,15 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
     const oracle_bulk &b = sim->bulks[i];
     ph.prop[i] = Prop{b.mutr, emission ? b.muaf : b.mua, b.g, b.n};
   }
-  ph.labels = sim->bulk_info;
   ph.method = sim->bulk_method == 1 ? 1 : 2;
   ph.exact = ph.method == 2 ? sim->exact_stepping : 0;
+  if (ph.exact) /* mu_t of the phase's wavelength, fluorophore absorption included */
+    for (unsigned i = 0; i < sim->n_bulks + 2; ++i) {
+      const oracle_bulk &b = sim->bulks[i];
+      const float mut = (emission ? b.muaf : b.mua) + b.mus;
+      ph.prop[i].mutr = mut == 0.0f ? FLT_MAX : 1.0f / mut;
+    }
+  ph.labels = sim->bulk_info;
   if (ph.method == 1) {
     ph.n_layers = (unsigned)sim->n_layers;
     for (unsigned i = 0; i < ph.n_layers + 2 && i < ORACLE_MAX_LAYERS + 2; ++i) ph.layers[i] = sim->layers[i];

@@ -55,7 +55,7 @@ MAX_BULKS = 100
 
 
 class CBulk(ctypes.Structure):
-    _fields_ = [(n, ctypes.c_float) for n in ("mutr", "mua", "g", "n", "flc", "muaf", "eY", "albedof")]
+    _fields_ = [(n, ctypes.c_float) for n in ("mutr", "mua", "g", "n", "flc", "muaf", "eY", "albedof", "mus")]
 
 
 MAX_LAYERS = 100
@@ -308,7 +308,7 @@ def sim_from_fields(labels: np.ndarray, bulks: list[dict], *, esp: float, grid_s
         ax, am = f32(b["absc_exi"]), f32(b["absc_emi"])
         mutr = f32(np.finfo(np.float32).max) if mus == 0 else f32(f32(1.0) / f32(mua + mus))
         s.bulks[i] = CBulk(mutr, f32(mua + flc * ax), f32(b["g"]), f32(b["n"]), flc, f32(mua + flc * am),
-                           f32(b["eY"]), f32(mus / f32(flc * ax + mus)))
+                           f32(b["eY"]), f32(mus / f32(flc * ax + mus)), mus)
     r = (np.float64(n_out) - np.float64(f32(bulks[0]["n"]))) / (np.float64(n_out) + np.float64(f32(bulks[0]["n"])))
     s.start_weight = int(np.float64(0xFFFFFFFF) * (1 - r * r))
     lab = np.ascontiguousarray(labels, dtype=np.int16)
@@ -336,7 +336,7 @@ def sim_from_arrays(labels: np.ndarray, bulks, *, half_x: float, half_y: float, 
     s.dir = 1.0
     s.n_bulks = len(bulks) - 2
     for i, b in enumerate(bulks):
-        s.bulks[i] = CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof)
+        s.bulks[i] = CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof, b.mus)
     if start_weight == 0:
         n1, n2 = np.float64(np.float32(bulks[0].n)), np.float64(np.float32(bulks[1].n))
         r = (n1 - n2) / (n1 + n2)

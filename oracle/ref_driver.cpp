@@ -341,7 +341,7 @@ extern "C" int ref_parse_mci(const char *mci_path, oracle_sim *out) {
     if (sim->n_bulks > ORACLE_MAX_BULKS) return -3;
     for (unsigned i = 0; i < sim->n_bulks + 2; ++i) {
       const BulkStruct &b = sim->bulks[i];
-      out->bulks[i] = oracle_bulk{b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof};
+      out->bulks[i] = oracle_bulk{b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof, 0.0f};
     }
     const int num_x = (int)(4 * sim->esp * sim->grid_size);
     const int num_y = (int)(4 * sim->esp * sim->grid_size);

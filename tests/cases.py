@@ -62,7 +62,7 @@ class Case:
         bl = self.bulks()
         s.n_bulks = len(bl) - 2
         for i, b in enumerate(bl):
-            s.bulks[i] = pyoracle.CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof)
+            s.bulks[i] = pyoracle.CBulk(b.mutr, b.mua, b.g, b.n, b.flc, b.muaf, b.eY, b.albedof, b.mus)
         s.start_weight = self.start_weight()
         lab = np.ascontiguousarray(self.labels.astype(np.int16))
         s.bulk_info = lab.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_short))

@@ -66,7 +66,9 @@ def test_port_reproduces_reference_build_live(name, oracle, ref_oracle, safeprim
 
 def _sim_fields(s):
     out = {k: getattr(s, k) for k, _ in s._fields_ if k not in ("bulks", "bulk_info", "vox_per_cm", "fluor_map")}
-    out["bulks"] = [tuple(np.float32(getattr(s.bulks[i], f)).tobytes() for f, _ in s.bulks[i]._fields_)
+    # mus is not a BulkStruct field (the reference's parser keeps only mutr):
+    # only voxel-boundary stepping reads it
+    out["bulks"] = [tuple(np.float32(getattr(s.bulks[i], f)).tobytes() for f, _ in s.bulks[i]._fields_ if f != "mus")
                     for i in range(s.n_bulks + 2)]
     return out
 
@@ -140,8 +142,10 @@ def _ref_sample(path):
                                  "lay:layered_timed_exit", "ref:sample2.mci"])
 def test_product_parser_matches_reference_parser(src, mcfl_lib, ref_oracle, tmp_path):
     import cudamcfl_gb300 as mc
+    case = None
     if src.startswith("case:"):
-        mci = cases.ALL[src[5:]]().write_mci(str(tmp_path))
+        case = cases.ALL[src[5:]]()
+        mci = case.write_mci(str(tmp_path))
     elif src.startswith("lay:"):
         mci = cases.LAYERED[src[4:]]().write_mci(str(tmp_path))
     else:
@@ -178,6 +182,12 @@ def test_product_parser_matches_reference_parser(src, mcfl_lib, ref_oracle, tmp_
             return
         for i in range(s.n_bulks + 2):
             for f, _ in mc.Bulk._fields_:
+                if f == "mus":  # not a BulkStruct field: the .mci column itself, 0 outside the slab
+                    if i in (0, s.n_bulks + 1):
+                        assert s.bulks[i].mus == 0.0, i
+                    elif case is not None:
+                        assert np.float32(s.bulks[i].mus) == np.float32(case.columns[i - 1][2]), i
+                    continue
                 assert np.float32(getattr(s.bulks[i], f)).tobytes() == \
                     np.float32(getattr(ref.bulks[i], f)).tobytes(), (i, f)
         nv = s.num_x * s.num_y * s.num_z

@@ -15,7 +15,9 @@ emission photons).
               run, every image and the fluence copied back, each step
   plain       the same simulation with the emission phase as one launch per
               emitting voxel (the reference's schedule), timed on a sample
-  batching    256 Gaussian beams on a 16 x 16 raster over the 4 x 4 x 2 cm
+  exact_stepping  voxel-boundary stepping against the reference's stepping on
+              the same medium at a tenth of the budgets
+  batching   256 Gaussian beams on a 16 x 16 raster over the 4 x 4 x 2 cm
               sphere medium, log-uniform budgets, one persistent launch vs
               one launch per beam
   serving     Poisson stream of requests with their own media (64^3 ..
@@ -188,12 +190,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
-    ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,batching,serving,cpu,e2e")
+    ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,exact_stepping,batching,serving,cpu,e2e")
     ap.add_argument("--profile", action="store_true",
-                    help="small case for ncu: the benchmark medium, --photons excitation photons and 20 emission "
-                         "photons per voxel, --warmup runs then one run (2 transport launches per run)")
+                    help="small case for ncu: the benchmark medium, --photons excitation photons and --per-voxel "
+                         "emission photons per voxel, --warmup runs then one run (2 transport launches per run)")
     ap.add_argument("--photons", type=int, default=2_000_000)
     ap.add_argument("--variant", type=int, default=0, help="--profile: kernel variant (0..2)")
+    ap.add_argument("--per-voxel", type=int, default=20, help="--profile: emission photons per emitting voxel")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -383,6 +386,23 @@ def main():
                                      f"one launch + host wait per voxel; {per_voxel_ms:.3f} ms per voxel",
                            "batched_over_plain": value / plain_value}
 
+    # --- voxel-boundary stepping against the reference's stepping, same medium and budgets ---
+    if "exact_stepping" not in skip:
+        sub = {}
+        for label, ex in (("reference_stepping", 0), ("voxel_boundary_stepping", 1)):
+            rx = mc.run_desc(EXC_PHOTONS // 10, det=m.det, photons_per_voxel=PHOTONS_PER_VOXEL // 10, fluence=1,
+                             seed_exc=5 + 1000 * rank, seed_fl=6 + 1000 * rank, exact_stepping=ex)
+            ox = mc.RunOut()
+            mc.check(lib.mcfl_run(ctx.handle, med.handle, mc.ctypes.byref(rx), mc.ctypes.byref(ox)))  # warm-up
+            mc.check(lib.mcfl_run(ctx.handle, med.handle, mc.ctypes.byref(rx), mc.ctypes.byref(ox)))
+            sx, sfx = dict(zip(mc.STAT_NAMES, ox.stats_exc)), dict(zip(mc.STAT_NAMES, ox.stats_fl))
+            sub[label] = {"photons_per_s": (rx.photons + ox.photons_fl) / ((ox.ms_exc + ox.ms_fl) / 1e3),
+                          "excitation_photons": rx.photons, "emission_photons": ox.photons_fl,
+                          "emitting_voxels": ox.fl_voxels, "passes_per_photon_exc": sx["steps"] / rx.photons,
+                          "passes_per_photon_fl": sfx["steps"] / max(1, ox.photons_fl)}
+        sub["workload"] = "the headline medium at a tenth of its budgets, fast math, two phases"
+        result["exact_stepping"] = sub
+
     # --- batched sweep: 256 beams on the sphere medium ---
     if "batching" not in skip:
         c1 = media.config1()
@@ -453,7 +473,7 @@ def profile_case(args):
     ctx.set_option("variant", args.variant)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
-    rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=20, fluence=1, seed_exc=1, seed_fl=2)
+    rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2)
     for _ in range(args.warmup + 1):
         r = ctx.run(med, rd, images=False, raw=False)
     print(json.dumps({"profile_case": "config2", "math": args.math, "photons": args.photons,

@@ -18,6 +18,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+#include <utility>
+
 #include "engine_types.h"
 
 namespace {
@@ -199,5 +202,78 @@ extern "C" cudaError_t mcfl_launch_normalize_phd(const unsigned long long *raw, 
 extern "C" cudaError_t mcfl_launch_normalize_128(const unsigned long long *raw, double *out, size_t n, double norm,
                                                  cudaStream_t s) {
   normalize_128<<<grid_for(n), 256, 0, s>>>(raw, out, n, norm);
+  return cudaGetLastError();
+}
+
+/* ------------------------------------------------ free-radius map
+ * For voxel-boundary stepping: the free radius of a voxel is the largest
+ * r <= MCFL_FREE_MAX such that every voxel of the grid within Chebyshev
+ * distance r of it carries its label (the transport kernel clips the cube
+ * to the grid).  It is 0 next to a different label (26 neighbours inside the
+ * grid); elsewhere it is the Chebyshev distance to the nearest such voxel,
+ * capped.  Built by Jacobi
+ * relaxation: after k sweeps of r = min(r, 1 + min over the 26 neighbours)
+ * every radius up to k is exact, so MCFL_FREE_MAX - 1 sweeps give the capped
+ * map.  Packed with the label as label | r << 8, one 2-byte load per voxel
+ * crossing. */
+
+namespace {
+
+constexpr int kFreeThreads = 256;
+
+__global__ void free_init(const uint8_t *__restrict__ labels, int nx, int ny, int nz, uint8_t *__restrict__ r) {
+  const size_t n = (size_t)nx * ny * nz;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+    bool edge = false;
+    const uint8_t l = labels[i];
+    for (int c = 0; c < 27 && !edge; ++c) {
+      const int u = x + c % 3 - 1, v = y + (c / 3) % 3 - 1, w = z + c / 9 - 1;
+      if (u < 0 || v < 0 || w < 0 || u >= nx || v >= ny || w >= nz) continue;
+      edge = labels[(size_t)u + (size_t)nx * ((size_t)v + (size_t)ny * w)] != l;
+    }
+    r[i] = edge ? 0 : MCFL_FREE_MAX;
+  }
+}
+
+__global__ void free_relax(const uint8_t *__restrict__ in, int nx, int ny, int nz, uint8_t *__restrict__ out) {
+  const size_t n = (size_t)nx * ny * nz;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    int r = in[i];
+    if (r != 0) {
+      const int x = (int)(i % nx), y = (int)((i / nx) % ny), z = (int)(i / ((size_t)nx * ny));
+      for (int c = 0; c < 27; ++c) {
+        const int u = x + c % 3 - 1, v = y + (c / 3) % 3 - 1, w = z + c / 9 - 1;
+        if (u < 0 || v < 0 || w < 0 || u >= nx || v >= ny || w >= nz) continue;
+        r = min(r, 1 + (int)in[(size_t)u + (size_t)nx * ((size_t)v + (size_t)ny * w)]);
+      }
+    }
+    out[i] = (uint8_t)r;
+  }
+}
+
+__global__ void free_pack(const uint8_t *__restrict__ labels, const uint8_t *__restrict__ r, size_t n,
+                          uint16_t *__restrict__ lab16) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    lab16[i] = (uint16_t)(labels[i] | (r[i] << 8));
+}
+
+} // namespace
+
+extern "C" cudaError_t mcfl_launch_free_map(const uint8_t *labels, int nx, int ny, int nz, uint8_t *tmp,
+                                           uint16_t *lab16, cudaStream_t s) {
+  const size_t n = (size_t)nx * ny * nz;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t want = (n + kFreeThreads - 1) / kFreeThreads;
+  const int blocks = (int)std::min<size_t>(want, (size_t)(sms > 0 ? sms : 1) * 8);
+  uint8_t *a = tmp, *b = tmp + n;
+  free_init<<<blocks, kFreeThreads, 0, s>>>(labels, nx, ny, nz, a);
+  for (int k = 1; k < MCFL_FREE_MAX; ++k) {
+    free_relax<<<blocks, kFreeThreads, 0, s>>>(a, nx, ny, nz, b);
+    std::swap(a, b);
+  }
+  free_pack<<<blocks, kFreeThreads, 0, s>>>(labels, a, n, lab16);
   return cudaGetLastError();
 }

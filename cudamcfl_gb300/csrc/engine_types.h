@@ -127,7 +127,13 @@ typedef struct McflMedium {
    * grid's. */
   const float *layer_tab;
   uint32_t layered, n_layers;
+  /* voxel-boundary stepping: per voxel its label | free radius << 8, the
+   * free radius being the largest r <= MCFL_FREE_MAX such that every voxel
+   * of the grid within Chebyshev distance r carries the same label */
+  const uint16_t *lab16;
 } McflMedium;
+
+#define MCFL_FREE_MAX 31
 
 typedef struct McflLaunch {
   const McflJob *jobs;   /* job slots */

@@ -50,6 +50,9 @@ extern "C" cudaError_t mcfl_launch_emission_prep(const uint8_t *labels, const fl
                                                  uint64_t *q, unsigned long long *list_len,
                                                  McflJob *job, unsigned long long *ticket_end, cudaStream_t s);
 size_t emission_prep_blocks(uint32_t total);
+/* label | free radius << 8 per voxel (McflMedium::lab16); tmp: 2 * nx*ny*nz bytes */
+extern "C" cudaError_t mcfl_launch_free_map(const uint8_t *labels, int nx, int ny, int nz, uint8_t *tmp,
+                                           uint16_t *lab16, cudaStream_t s);
 extern "C" cudaError_t mcfl_launch_normalize_u64(const unsigned long long *raw, double *out, size_t n, double scale,
                                                  cudaStream_t s);
 extern "C" cudaError_t mcfl_launch_normalize_phd(const unsigned long long *raw, double *out, size_t n,
@@ -107,6 +110,9 @@ struct mcfl_medium {
   /* voxel-boundary stepping: 1/mu_t with mu_t = mua + mus at excitation and
    * muaf + mus at emission (the fluorophore's absorption included) */
   mcfl::DevBuf prop_exc_x, prop_emi_x, lab_exc_x, lab_emi_x;
+  /* voxel-boundary stepping: label | free radius << 8 per voxel, built on
+   * the first such run (mcfl::ensure_free_map) */
+  mutable mcfl::DevBuf lab16;
   const float *prop_of(bool emission, bool exact) const {
     return (exact ? (emission ? prop_emi_x : prop_exc_x) : (emission ? prop_emi : prop_exc)).as<float>();
   }

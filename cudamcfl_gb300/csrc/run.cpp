@@ -82,6 +82,24 @@ void fill_source(McflJob &j, const mcfl_run_desc &r, const mcfl_medium *m) {
       }
 }
 
+/* The free-radius map of voxel-boundary stepping, built on the medium's
+ * first such run (synchronously, before any recorded graph uses it). */
+int ensure_free_map(mcfl_ctx *c, const mcfl_medium *m) {
+  if (m->lab16.p) return MCFL_OK;
+  const size_t n = (size_t)m->total;
+  mcfl::DevBuf tmp;
+  MCFL_CUDA_TRY(tmp.reserve(2 * n));
+  MCFL_CUDA_TRY(m->lab16.reserve(2 * n));
+  cudaError_t e = mcfl_launch_free_map(m->labels.as<uint8_t>(), m->nx, m->ny, m->nz, tmp.as<uint8_t>(),
+                                       m->lab16.as<uint16_t>(), c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    m->lab16.release();
+    return cuda_fail(e, "free-radius map");
+  }
+  return MCFL_OK;
+}
+
 int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run) {
   if (!c || !m || !run) return fail(MCFL_E_ARG, "null argument");
   if (m->ctx != c) return fail(MCFL_E_ARG, "medium of another context");
@@ -236,6 +254,7 @@ void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool em
   u.labels = m->labels.as<uint8_t>();
   u.prop = m->prop_of(emission, exact);
   u.lab = m->lab_of(emission, exact);
+  u.lab16 = exact ? m->lab16.as<uint16_t>() : nullptr;
   u.n_labels = (uint32_t)m->n_bulks + 2u;
   u.fhd = fhd;
   u.hx = m->hx;
@@ -269,6 +288,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   const bool fluence = emission || run->fluence;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   cudaGetLastError();
+  if (run->exact_stepping && (rc = ensure_free_map(c, m)) != MCFL_OK) return rc;
   cudaStream_t s = c->stream;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   const size_t nv = m->total;
@@ -501,6 +521,11 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
     const mcfl_detector &d = runs[i].det;
     if (d.nx != det.nx || d.ny != det.ny) return fail(MCFL_E_ARG, "mcfl_batch_run: detectors must share a size");
   }
+  if (exact) {
+    MCFL_CUDA_TRY(cudaSetDevice(c->device));
+    const int rcm = ensure_free_map(c, m);
+    if (rcm != MCFL_OK) return rcm;
+  }
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   cudaGetLastError();
   cudaStream_t s = c->stream;
@@ -644,6 +669,7 @@ extern "C" int mcfl_run_plain(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_
   const mcfl_detector &det = run->det;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   cudaGetLastError();
+  if (run->exact_stepping && (rc = ensure_free_map(c, m)) != MCFL_OK) return rc;
   cudaStream_t s = c->stream;
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
   const size_t nv = m->total;
@@ -745,6 +771,10 @@ int mcfl::run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcf
   cudaStream_t s = c->stream;
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   cudaGetLastError();
+  if (run->exact_stepping) {
+    const int rcm = ensure_free_map(c, m);
+    if (rcm != MCFL_OK) return rcm;
+  }
   MCFL_CUDA_TRY(c->R128.reserve(xy * 16));
   MCFL_CUDA_TRY(c->T128.reserve(xy * 16));
   MCFL_CUDA_TRY(c->vox.reserve(64));

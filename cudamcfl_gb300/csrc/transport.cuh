@@ -165,7 +165,8 @@ struct Med {
   unsigned long long *fhd;
   real hx, hy, esp, gx, gy, gz;
   uint32_t nx, ny, total, last;
-  uint32_t nz; /* voxel-boundary stepping only */
+  uint32_t nz;            /* voxel-boundary stepping only */
+  const uint16_t *lab16;  /* voxel-boundary stepping only: label | free radius << 8 */
 };
 
 __device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
@@ -712,7 +713,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     m.ny = L.med.ny;
     m.total = L.med.total;
     m.last = L.med.last_label;
-    if (kExactStep) m.nz = m.total / (m.nx * m.ny);
+    if (kExactStep) {
+      m.nz = m.total / (m.nx * m.ny);
+      m.lab16 = L.med.lab16;
+    }
   }
   Rec rc = {}; /* general kernel: the record of the photon's label, in registers */
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
@@ -817,44 +821,203 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
        * different indices with that face's normal, scattering-free voxels
        * are crossed without interaction.  The pass ends at the interaction
        * (PHD tally, weight drop, spin, as the reference's pass) or at an
-       * exit. ---- */
+       * exit.  Inside the grid the walk is a 3D DDA: distances along the ray
+       * from the origin (ox, oy, oz) — the pass start or the face where the
+       * direction last changed — with tx, ty, tz the distances to the next
+       * face along each axis, recomputed from the face index for the axis
+       * crossed only; a run of voxels of one label is charged its optical
+       * depth once, where the label changes (s0: where the run began).
+       * Outside the grid's lateral extent each region is one straight
+       * segment to a slab face or back into the grid. ---- */
       real tau = -MCFL_LOGF(r.oc());
       const int cap = 16 + 4 * (int)(m.nx + m.ny + m.nz);
-      bool interact = false;
-      for (int itv = 0;; ++itv) {
-        const Rec c = Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]};
-        const bool glass = c.a.x == FLT_MAX;
-        real db = FLT_MAX;
-        int axis = -1;
-        real t;
-        if (itv >= cap) break; /* cannot reach an interaction: lost below */
+      int itv = 0;
+      bool interact = false, lost = false;
+      auto face_x = [&](int k) { return (real)k / m.gx - m.hx; };
+      auto face_y = [&](int k) { return (real)k / m.gy - m.hy; };
+      auto face_z = [&](int k) {
+        return k == 0 ? MCFL_C(0.0) : (k == (int)m.nz ? m.esp : (real)k / m.gz);
+      };
+      for (;;) {
         if (p.ingrid) {
-          const real bx = (real)(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix) / m.gx - m.hx;
-          t = plane_dist(bx, p.x, p.dx);
-          if (t < db) { db = t; axis = 0; }
-          const real by = (real)(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy) / m.gy - m.hy;
-          t = plane_dist(by, p.y, p.dy);
-          if (t < db) { db = t; axis = 1; }
-          const int kz = p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz;
-          const real bz = kz == 0 ? MCFL_C(0.0) : (kz == (int)m.nz ? m.esp : (real)kz / m.gz);
-          t = plane_dist(bz, p.z, p.dz);
-          if (t < db) { db = t; axis = 2; }
-        } else {
-          t = plane_dist(p.dz > MCFL_C(0.0) ? m.esp : MCFL_C(0.0), p.z, p.dz);
-          if (t < db) { db = t; axis = 2; }
-          if ((p.x <= -m.hx && p.dx > MCFL_C(0.0)) || (p.x >= m.hx && p.dx < MCFL_C(0.0))) {
-            t = plane_dist(p.dx > MCFL_C(0.0) ? -m.hx : m.hx, p.x, p.dx);
-            const real yc = p.y + p.dy * t;
-            if (t < db && MCFL_FABS(yc) < m.hy) { db = t; axis = 0; }
+          const real ox = p.x, oy = p.y, oz = p.z;
+          /* tx, ty, tz: the next faces of the photon's voxel, computed when a
+           * step needs them (tv), never behind the distance a free cube took
+           * it to (floor_s); after a free cube the photon crosses its face
+           * next (jumped) */
+          real tx = MCFL_C(0.0), ty = MCFL_C(0.0), tz = MCFL_C(0.0), floor_s = MCFL_C(0.0);
+          bool tv = false, jumped = false;
+          real s0 = MCFL_C(0.0);
+          int cr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
+          bool restart = false, done_pass = false;
+          while (!restart) {
+            if (++itv > cap) {
+              lost = true;
+              done_pass = true;
+              break;
+            }
+            const real4 ca = s_lab[2 * p.label];
+            if (cr > 0 && !jumped) {
+              /* every voxel within cr of this one carries its label: straight
+               * to the face of that cube (clipped to the grid), or to the
+               * interaction inside it */
+              const int lx = max(p.ix - cr, 0), ux = min(p.ix + cr, (int)m.nx - 1);
+              const int ly = max(p.iy - cr, 0), uy = min(p.iy + cr, (int)m.ny - 1);
+              const int lz = max(p.iz - cr, 0), uz = min(p.iz + cr, (int)m.nz - 1);
+              const real cx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? ux + 1 : lx), ox, p.dx);
+              const real cy = plane_dist(face_y(p.dy > MCFL_C(0.0) ? uy + 1 : ly), oy, p.dy);
+              const real cz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? uz + 1 : lz), oz, p.dz);
+              real db = cx;
+              int axis = 0;
+              if (cy < db) { db = cy; axis = 1; }
+              if (cz < db) { db = cz; axis = 2; }
+              real sj = db;
+              bool hit = false;
+              if (ca.x != FLT_MAX) {
+                const real s_int = s0 + tau * ca.x;
+                if (s_int <= db) {
+                  sj = s_int;
+                  hit = true;
+                }
+              }
+              const real x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
+              /* the voxel there, kept inside the cube (on its face along the exit axis) */
+              const int jx = (!hit && axis == 0) ? (p.dx > MCFL_C(0.0) ? ux : lx)
+                                                 : min(max((int)MCFL_R2U_RZ((x + m.hx) * m.gx), lx), ux);
+              const int jy = (!hit && axis == 1) ? (p.dy > MCFL_C(0.0) ? uy : ly)
+                                                 : min(max((int)MCFL_R2U_RZ((y + m.hy) * m.gy), ly), uy);
+              const int jz = (!hit && axis == 2) ? (p.dz > MCFL_C(0.0) ? uz : lz)
+                                                 : min(max((int)MCFL_R2U_RZ(z * m.gz), lz), uz);
+              p.ix = jx;
+              p.iy = jy;
+              p.iz = jz;
+              if (hit) {
+                p.x = x;
+                p.y = y;
+                p.z = z;
+                interact = true;
+                done_pass = true;
+                break;
+              }
+              cr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
+              floor_s = db;
+              tv = false;
+              jumped = true;
+              continue;
+            }
+            jumped = false;
+            if (!tv) {
+              tx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix), ox, p.dx);
+              ty = plane_dist(face_y(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy), oy, p.dy);
+              tz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz), oz, p.dz);
+              /* never behind the cube's face */
+              if (tx < floor_s) tx = floor_s;
+              if (ty < floor_s) ty = floor_s;
+              if (tz < floor_s) tz = floor_s;
+              tv = true;
+            }
+            real db = tx;
+            int axis = 0;
+            if (ty < db) { db = ty; axis = 1; }
+            if (tz < db) { db = tz; axis = 2; }
+            if (ca.x != FLT_MAX) {
+              const real s_int = s0 + tau * ca.x;
+              if (s_int <= db) { /* the interaction happens in this voxel */
+                p.x = ox + p.dx * s_int;
+                p.y = oy + p.dy * s_int;
+                p.z = oz + p.dz * s_int;
+                interact = true;
+                done_pass = true;
+                break;
+              }
+            }
+            /* the region across the face */
+            int nix = p.ix, niy = p.iy, niz = p.iz, nin = 1;
+            if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
+            else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
+            else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
+            uint32_t next;
+            int nr = 0; /* the free radius there */
+            if (niz < 0) next = 0u;
+            else if (niz >= (int)m.nz) next = m.last;
+            else if (nix < 0 || nix >= (int)m.nx || niy < 0 || niy >= (int)m.ny) {
+              next = 1u;
+              nin = 0;
+            } else {
+              const uint32_t q = m.lab16[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
+              next = q & 0xffu;
+              nr = (int)(q >> 8);
+            }
+            if (next != p.label || !nin) {
+              /* the run of this label ends at the face */
+              if (ca.x != FLT_MAX) {
+                tau -= (db - s0) / ca.x;
+                if (tau < MCFL_C(0.0)) tau = MCFL_C(0.0);
+              }
+              s0 = db;
+              p.x = ox + p.dx * db;
+              p.y = oy + p.dy * db;
+              p.z = oz + p.dz * db;
+              if (next != p.label) {
+                const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
+                const bool bent = n_here != n_next;
+                if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: same voxel, new direction */
+                  restart = true;
+                  continue;
+                }
+                restart = bent;
+              }
+              p.label = next;
+              p.ix = nix;
+              p.iy = niy;
+              p.iz = niz;
+              p.ingrid = nin;
+              if (next == 0u || next == m.last) {
+                const bool top = next == 0u;
+                tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+                ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+                p.weight = 0u;
+                done_pass = true;
+                break;
+              }
+              if (!nin) restart = true;
+              if (restart) continue;
+            } else {
+              p.ix = nix;
+              p.iy = niy;
+              p.iz = niz;
+            }
+            cr = nr;
+            /* the next face along the axis crossed */
+            if (axis == 0) tx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix), ox, p.dx);
+            else if (axis == 1) ty = plane_dist(face_y(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy), oy, p.dy);
+            else tz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz), oz, p.dz);
           }
-          if ((p.y <= -m.hy && p.dy > MCFL_C(0.0)) || (p.y >= m.hy && p.dy < MCFL_C(0.0))) {
-            t = plane_dist(p.dy > MCFL_C(0.0) ? -m.hy : m.hy, p.y, p.dy);
-            const real xc = p.x + p.dx * t;
-            if (t < db && MCFL_FABS(xc) < m.hx) { db = t; axis = 1; }
-          }
+          if (done_pass) break;
+          continue;
         }
-        if (!glass) {
-          const real s_int = tau * c.a.x;
+        /* outside the grid's lateral extent: one straight segment */
+        if (++itv > cap) {
+          lost = true;
+          break;
+        }
+        const real4 ca = s_lab[2 * p.label];
+        real db = plane_dist(p.dz > MCFL_C(0.0) ? m.esp : MCFL_C(0.0), p.z, p.dz);
+        int axis = 2;
+        real t;
+        /* re-entry through a lateral face of the grid */
+        if ((p.x <= -m.hx && p.dx > MCFL_C(0.0)) || (p.x >= m.hx && p.dx < MCFL_C(0.0))) {
+          t = plane_dist(p.dx > MCFL_C(0.0) ? -m.hx : m.hx, p.x, p.dx);
+          const real yc = p.y + p.dy * t;
+          if (t < db && MCFL_FABS(yc) < m.hy) { db = t; axis = 0; }
+        }
+        if ((p.y <= -m.hy && p.dy > MCFL_C(0.0)) || (p.y >= m.hy && p.dy < MCFL_C(0.0))) {
+          t = plane_dist(p.dy > MCFL_C(0.0) ? -m.hy : m.hy, p.y, p.dy);
+          const real xc = p.x + p.dx * t;
+          if (t < db && MCFL_FABS(xc) < m.hx) { db = t; axis = 1; }
+        }
+        if (ca.x != FLT_MAX) {
+          const real s_int = tau * ca.x;
           if (s_int <= db) {
             p.x += p.dx * s_int;
             p.y += p.dy * s_int;
@@ -863,32 +1026,22 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             break;
           }
         }
-        if (axis < 0) break; /* scattering-free with no face ahead: lost below */
+        if (db == FLT_MAX) { /* scattering-free with no face ahead */
+          lost = true;
+          break;
+        }
         p.x += p.dx * db;
         p.y += p.dy * db;
         p.z += p.dz * db;
-        if (!glass) {
-          tau -= db / c.a.x;
+        if (ca.x != FLT_MAX) {
+          tau -= db / ca.x;
           if (tau < MCFL_C(0.0)) tau = MCFL_C(0.0);
         }
-        int nix = p.ix, niy = p.iy, niz = p.iz, nin = p.ingrid;
+        int nix = p.ix, niy = p.iy, niz = p.iz;
         uint32_t next;
-        if (p.ingrid) {
-          if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
-          else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
-          else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
-          if (niz < 0) next = 0u;
-          else if (niz >= (int)m.nz) next = m.last;
-          else if (nix < 0 || nix >= (int)m.nx || niy < 0 || niy >= (int)m.ny) {
-            next = 1u;
-            nin = 0;
-          } else {
-            next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
-          }
-        } else if (axis == 2) {
+        if (axis == 2) {
           next = p.dz > MCFL_C(0.0) ? m.last : 0u;
         } else {
-          nin = 1;
           nix = axis == 0 ? (p.dx > MCFL_C(0.0) ? 0 : (int)m.nx - 1)
                           : (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
           niy = axis == 1 ? (p.dy > MCFL_C(0.0) ? 0 : (int)m.ny - 1)
@@ -896,12 +1049,14 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           niz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
           next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
         }
-        if (next != p.label && !refract_axis(p, axis, c.b.w, s_lab[2 * next + 1].w, r)) continue;
+        if (next != p.label && !refract_axis(p, axis, s_lab[2 * p.label + 1].w, s_lab[2 * next + 1].w, r)) continue;
         p.label = next;
-        p.ix = nix;
-        p.iy = niy;
-        p.iz = niz;
-        p.ingrid = nin;
+        if (axis != 2) {
+          p.ix = nix;
+          p.iy = niy;
+          p.iz = niz;
+          p.ingrid = 1;
+        }
         if (next == 0u || next == m.last) {
           const bool top = next == 0u;
           tally_exit(J, p.x, p.y, p.weight, top, src_idx);
@@ -924,7 +1079,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.weight = 0u;
         }
         spin(p, c2, r);
-      } else if (p.weight) { /* lost without interaction (cap or no face ahead) */
+      } else if (lost && p.weight) { /* cannot reach an interaction (cap or no face ahead) */
         ev_add(MCFL_ST_W0_LOSS, p.weight);
         p.weight = 0u;
       }

@@ -131,6 +131,8 @@ struct Phase {
   unsigned last_bulk;
   Prop prop[ORACLE_MAX_BULKS + 2];
   const short *labels;
+  /* voxel-boundary stepping: each voxel's free radius (see free_radius) */
+  const unsigned char *free_r;
   int fhd_on;
   float xi, yi, zi, dir;
   uint32_t start_weight;
@@ -670,65 +672,233 @@ inline float plane_dist(float b, float c, float d) {
   return t > 0.0f ? t : 0.0f;
 }
 
+/* Coordinate of face k of the grid along axis a (0, 1, 2 = x, y, z); the
+ * z faces 0 and num_z are the slab faces themselves. */
+inline float face_coord(const Phase &ph, int a, int k) {
+  if (a == 0) return (float)k / ph.gx - ph.hx;
+  if (a == 1) return (float)k / ph.gy - ph.hy;
+  return k == 0 ? 0.0f : (k == (int)ph.num_z ? ph.esp : (float)k / ph.gz);
+}
+
+/* The region across a face crossed along axis from the photon's voxel (the
+ * grid, the slab's outer media or, laterally, the medium of label 1). */
+inline uint32_t region_across(const Photon &p, const Phase &ph, int axis, int &nix, int &niy, int &niz, int &nin) {
+  nix = p.ix;
+  niy = p.iy;
+  niz = p.iz;
+  nin = 1;
+  if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
+  else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
+  else niz += p.dz > 0.0f ? 1 : -1;
+  if (niz < 0) return 0;
+  if (niz >= (int)ph.num_z) return ph.last_bulk;
+  if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
+    nin = 0;
+    return 1;
+  }
+  return (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
+}
+
+/* An exit through a slab face: the image tally. */
+inline void exact_exit(Photon &p, const Phase &ph, Sink &sk, bool top) {
+  if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
+    const unsigned idx = pixel_index(ph, p.x, p.y);
+    if (top) {
+      if (sk.R128) add128(&sk.R128[2 * (size_t)idx], p.weight, sk.voxel_q);
+      else add_guarded(&sk.Rd[idx], p.weight, ph.guard);
+    } else {
+      if (sk.T128) add128(&sk.T128[2 * (size_t)idx], p.weight, sk.voxel_q);
+      else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
+    }
+  }
+  (top ? sk.exit_top : sk.exit_bottom) += p.weight;
+  p.weight = 0u;
+}
+
 /* One pass with voxel-boundary stepping: an optical depth -ln(u) is spent
  * voxel by voxel with each voxel's mu_t, the label is taken where the photon
  * is, Fresnel acts at every face between different indices with that face's
  * normal, scattering-free voxels are crossed without interaction.  The pass
  * ends at the interaction (PHD tally, weight drop and spin as the reference's
- * pass) or at an exit. */
+ * pass) or at an exit.
+ *
+ * Inside the grid the walk is a 3D DDA (Amanatides & Woo): distances are
+ * measured along the ray from an origin o (the pass start, or the face where
+ * the direction last changed); t[a] is the distance to the next face along
+ * axis a, recomputed from the face index for the axis crossed only.  Within a
+ * run of voxels of one label only the voxel index and t change; the optical
+ * depth of the run is charged when the label changes (s0: where the run
+ * began).  Outside the grid's lateral extent (the medium of label 1) each
+ * region is one straight segment to a slab face or back into the grid. */
 template <class M>
 unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   const uint32_t last = ph.last_bulk;
   sk.steps++;
   float tau = -M::log(r.oc());
   const int cap = 16 + 4 * (int)(ph.num_x + ph.num_y + ph.num_z);
-  for (int it = 0;; ++it) {
-    if (it >= cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
+  int it = 0;
+  for (;;) {
+    if (p.ingrid) {
+      const float ox = p.x, oy = p.y, oz = p.z;
+      /* t: the next faces of the photon's voxel, computed when a step needs
+       * them (tv), never behind the distance a free cube took it to (floor) */
+      float t[3] = {0.0f, 0.0f, 0.0f}, floor_s = 0.0f;
+      bool tv = false;
+      bool jumped = false; /* a free cube took the photon to its face: cross that face next */
+      float s0 = 0.0f;
+      int cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
+      bool restart = false;
+      while (!restart) {
+        if (++it > cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
+          sk.w0_loss += p.weight;
+          p.weight = 0u;
+          return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+        }
+        const Prop &pr = ph.prop[p.bulkpos];
+        if (cr > 0 && !jumped) {
+          /* every voxel within cr of this one carries its label: straight to
+           * the face of that cube (clipped to the grid), or to the
+           * interaction inside it */
+          const int lx = std::max(p.ix - cr, 0), ux = std::min(p.ix + cr, (int)ph.num_x - 1);
+          const int ly = std::max(p.iy - cr, 0), uy = std::min(p.iy + cr, (int)ph.num_y - 1);
+          const int lz = std::max(p.iz - cr, 0), uz = std::min(p.iz + cr, (int)ph.num_z - 1);
+          const float cx = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? ux + 1 : lx), ox, p.dx);
+          const float cy = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? uy + 1 : ly), oy, p.dy);
+          const float cz = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? uz + 1 : lz), oz, p.dz);
+          float db = cx;
+          int axis = 0;
+          if (cy < db) { db = cy; axis = 1; }
+          if (cz < db) { db = cz; axis = 2; }
+          float sj = db;
+          bool hit = false;
+          if (pr.mutr != FLT_MAX) {
+            const float s_int = s0 + tau * pr.mutr;
+            if (s_int <= db) {
+              sj = s_int;
+              hit = true;
+            }
+          }
+          const float x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
+          /* the voxel there, kept inside the cube (on its face along the exit axis) */
+          const int jx = (!hit && axis == 0) ? (p.dx > 0.0f ? ux : lx)
+                                             : std::min(std::max((int)mcfl_f2u_rz((x + ph.hx) * ph.gx), lx), ux);
+          const int jy = (!hit && axis == 1) ? (p.dy > 0.0f ? uy : ly)
+                                             : std::min(std::max((int)mcfl_f2u_rz((y + ph.hy) * ph.gy), ly), uy);
+          const int jz = (!hit && axis == 2) ? (p.dz > 0.0f ? uz : lz)
+                                             : std::min(std::max((int)mcfl_f2u_rz(z * ph.gz), lz), uz);
+          p.ix = jx;
+          p.iy = jy;
+          p.iz = jz;
+          if (hit) {
+            p.x = x;
+            p.y = y;
+            p.z = z;
+            goto interaction;
+          }
+          cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
+          floor_s = db;
+          tv = false;
+          jumped = true;
+          continue;
+        }
+        jumped = false;
+        if (!tv) {
+          t[0] = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? p.ix + 1 : p.ix), ox, p.dx);
+          t[1] = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? p.iy + 1 : p.iy), oy, p.dy);
+          t[2] = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? p.iz + 1 : p.iz), oz, p.dz);
+          for (int a = 0; a < 3; ++a) /* never behind the cube's face */
+            if (t[a] < floor_s) t[a] = floor_s;
+          tv = true;
+        }
+        float db = t[0];
+        int axis = 0;
+        if (t[1] < db) { db = t[1]; axis = 1; }
+        if (t[2] < db) { db = t[2]; axis = 2; }
+        if (pr.mutr != FLT_MAX) {
+          const float s_int = s0 + tau * pr.mutr;
+          if (s_int <= db) { /* the interaction happens in this voxel */
+            p.x = ox + p.dx * s_int;
+            p.y = oy + p.dy * s_int;
+            p.z = oz + p.dz * s_int;
+            goto interaction;
+          }
+        }
+        int nix, niy, niz, nin;
+        const uint32_t next = region_across(p, ph, axis, nix, niy, niz, nin);
+        if (next != p.bulkpos || !nin) {
+          /* the run of this label ends at the face */
+          if (pr.mutr != FLT_MAX) {
+            tau -= (db - s0) / pr.mutr;
+            if (tau < 0.0f) tau = 0.0f;
+          }
+          s0 = db;
+          p.x = ox + p.dx * db;
+          p.y = oy + p.dy * db;
+          p.z = oz + p.dz * db;
+          const float n_next = ph.prop[next].n;
+          if (next != p.bulkpos) {
+            const bool bent = pr.n != n_next;
+            if (!refract_axis(p, axis, pr.n, n_next, r)) { /* reflected: same voxel, new direction */
+              restart = true;
+              continue;
+            }
+            restart = bent;
+          }
+          p.bulkpos = next;
+          p.ix = nix;
+          p.iy = niy;
+          p.iz = niz;
+          p.ingrid = nin;
+          if (next == 0 || next == last) {
+            exact_exit(p, ph, sk, next == 0);
+            return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+          }
+          if (!nin) restart = true;
+          if (restart) continue;
+        } else {
+          p.ix = nix;
+          p.iy = niy;
+          p.iz = niz;
+        }
+        cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
+        /* the next face along the axis crossed */
+        if (axis == 0) t[0] = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? p.ix + 1 : p.ix), ox, p.dx);
+        else if (axis == 1) t[1] = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? p.iy + 1 : p.iy), oy, p.dy);
+        else t[2] = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? p.iz + 1 : p.iz), oz, p.dz);
+      }
+      continue;
+    }
+    /* outside the grid's lateral extent: one straight segment */
+    if (++it > cap) {
       sk.w0_loss += p.weight;
       p.weight = 0u;
       return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
     }
     const Prop &pr = ph.prop[p.bulkpos];
-    const bool glass = pr.mutr == FLT_MAX;
-    float db = FLT_MAX;
-    int axis = -1;
-    float t;
-    if (p.ingrid) {
-      const float bx = (float)(p.dx > 0.0f ? p.ix + 1 : p.ix) / ph.gx - ph.hx;
-      t = plane_dist(bx, p.x, p.dx);
-      if (t < db) { db = t; axis = 0; }
-      const float by = (float)(p.dy > 0.0f ? p.iy + 1 : p.iy) / ph.gy - ph.hy;
-      t = plane_dist(by, p.y, p.dy);
-      if (t < db) { db = t; axis = 1; }
-      const int kz = p.dz > 0.0f ? p.iz + 1 : p.iz;
-      const float bz = kz == 0 ? 0.0f : (kz == (int)ph.num_z ? ph.esp : (float)kz / ph.gz);
-      t = plane_dist(bz, p.z, p.dz);
-      if (t < db) { db = t; axis = 2; }
-    } else {
-      t = plane_dist(p.dz > 0.0f ? ph.esp : 0.0f, p.z, p.dz);
-      if (t < db) { db = t; axis = 2; }
-      /* re-entry through a lateral face of the grid */
-      if ((p.x <= -ph.hx && p.dx > 0.0f) || (p.x >= ph.hx && p.dx < 0.0f)) {
-        t = plane_dist(p.dx > 0.0f ? -ph.hx : ph.hx, p.x, p.dx);
-        const float yc = p.y + p.dy * t;
-        if (t < db && fabsf(yc) < ph.hy) { db = t; axis = 0; }
-      }
-      if ((p.y <= -ph.hy && p.dy > 0.0f) || (p.y >= ph.hy && p.dy < 0.0f)) {
-        t = plane_dist(p.dy > 0.0f ? -ph.hy : ph.hy, p.y, p.dy);
-        const float xc = p.x + p.dx * t;
-        if (t < db && fabsf(xc) < ph.hx) { db = t; axis = 1; }
-      }
+    float db = plane_dist(p.dz > 0.0f ? ph.esp : 0.0f, p.z, p.dz);
+    int axis = 2;
+    float tt;
+    /* re-entry through a lateral face of the grid */
+    if ((p.x <= -ph.hx && p.dx > 0.0f) || (p.x >= ph.hx && p.dx < 0.0f)) {
+      tt = plane_dist(p.dx > 0.0f ? -ph.hx : ph.hx, p.x, p.dx);
+      const float yc = p.y + p.dy * tt;
+      if (tt < db && fabsf(yc) < ph.hy) { db = tt; axis = 0; }
     }
-    if (!glass) {
+    if ((p.y <= -ph.hy && p.dy > 0.0f) || (p.y >= ph.hy && p.dy < 0.0f)) {
+      tt = plane_dist(p.dy > 0.0f ? -ph.hy : ph.hy, p.y, p.dy);
+      const float xc = p.x + p.dx * tt;
+      if (tt < db && fabsf(xc) < ph.hx) { db = tt; axis = 1; }
+    }
+    if (pr.mutr != FLT_MAX) {
       const float s_int = tau * pr.mutr;
-      if (s_int <= db) { /* the interaction happens in this voxel */
+      if (s_int <= db) {
         p.x += p.dx * s_int;
         p.y += p.dy * s_int;
         p.z += p.dz * s_int;
-        break;
+        goto interaction;
       }
     }
-    if (axis < 0) { /* a scattering-free region with no face ahead */
+    if (db == FLT_MAX) { /* a scattering-free region with no face ahead */
       sk.w0_loss += p.weight;
       p.weight = 0u;
       return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
@@ -736,64 +906,42 @@ unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
     p.x += p.dx * db;
     p.y += p.dy * db;
     p.z += p.dz * db;
-    if (!glass) {
+    if (pr.mutr != FLT_MAX) {
       tau -= db / pr.mutr;
       if (tau < 0.0f) tau = 0.0f;
     }
-    /* the region across the face */
-    int nix = p.ix, niy = p.iy, niz = p.iz, nin = p.ingrid;
-    uint32_t next;
-    if (p.ingrid) {
-      if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
-      else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
-      else niz += p.dz > 0.0f ? 1 : -1;
-      if (niz < 0) next = 0;
-      else if (niz >= (int)ph.num_z) next = last;
-      else if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
-        next = 1;
-        nin = 0;
+    {
+      int nix = p.ix, niy = p.iy, niz = p.iz;
+      uint32_t next;
+      if (axis == 2) {
+        next = p.dz > 0.0f ? last : 0;
       } else {
+        nix = axis == 0 ? (p.dx > 0.0f ? 0 : (int)ph.num_x - 1)
+                        : (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
+        niy = axis == 1 ? (p.dy > 0.0f ? 0 : (int)ph.num_y - 1)
+                        : (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
+        niz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
         next = (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
       }
-    } else if (axis == 2) {
-      next = p.dz > 0.0f ? last : 0;
-    } else {
-      nin = 1;
-      nix = axis == 0 ? (p.dx > 0.0f ? 0 : (int)ph.num_x - 1)
-                      : (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
-      niy = axis == 1 ? (p.dy > 0.0f ? 0 : (int)ph.num_y - 1)
-                      : (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
-      niz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
-      next = (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
-    }
-    if (next != p.bulkpos && !refract_axis(p, axis, pr.n, ph.prop[next].n, r)) continue; /* reflected */
-    p.bulkpos = next;
-    p.ix = nix;
-    p.iy = niy;
-    p.iz = niz;
-    p.ingrid = nin;
-    if (next == 0 || next == last) {
-      const bool top = next == 0;
-      if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
-        const unsigned idx = pixel_index(ph, p.x, p.y);
-        if (top) {
-          if (sk.R128) add128(&sk.R128[2 * (size_t)idx], p.weight, sk.voxel_q);
-          else add_guarded(&sk.Rd[idx], p.weight, ph.guard);
-        } else {
-          if (sk.T128) add128(&sk.T128[2 * (size_t)idx], p.weight, sk.voxel_q);
-          else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
-        }
+      if (next != p.bulkpos && !refract_axis(p, axis, pr.n, ph.prop[next].n, r)) continue; /* reflected */
+      p.bulkpos = next;
+      if (axis != 2) {
+        p.ix = nix;
+        p.iy = niy;
+        p.iz = niz;
+        p.ingrid = 1;
       }
-      (top ? sk.exit_top : sk.exit_bottom) += p.weight;
-      p.weight = 0u;
-      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+      if (next == 0 || next == last) {
+        exact_exit(p, ph, sk, next == 0);
+        return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+      }
     }
   }
-  /* the interaction */
+interaction:
   if (ph.fhd_on == 1 && p.ingrid)
     add_guarded(&sk.fhd[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)], p.weight, ph.guard);
-  const Prop &pr = ph.prop[p.bulkpos];
-  uint32_t w = mcfl_f2u_ru(pr.mua * pr.mutr * mcfl_u2f_rn(p.weight));
+  const Prop &pi = ph.prop[p.bulkpos];
+  uint32_t w = mcfl_f2u_ru(pi.mua * pi.mutr * mcfl_u2f_rn(p.weight));
   if (w > 0) {
     p.weight -= w;
     sk.absorbed += w;
@@ -801,7 +949,7 @@ unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
     sk.w0_loss += p.weight;
     p.weight = 0u;
   }
-  spin<M>(p, pr.g, r);
+  spin<M>(p, pi.g, r);
   return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
 }
 
@@ -812,6 +960,57 @@ inline unsigned step_any(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
 }
 
 /* ------------------------------------------------------------------------ */
+
+/* Largest free radius kept (the engine keeps the same). */
+#define ORACLE_FREE_MAX 31
+
+/* Free radius of every voxel, for voxel-boundary stepping: the largest
+ * r <= ORACLE_FREE_MAX such that every voxel of the grid within Chebyshev
+ * distance r of it carries its label.  It is 0 next to a different label
+ * (26 neighbours inside the grid), and otherwise the Chebyshev distance to
+ * the nearest such voxel, capped: a chamfer transform, one forward and one
+ * backward raster pass over the 13 neighbours already visited, which is
+ * exact for the Chebyshev metric.  A free cube is clipped to the grid where
+ * it is used. */
+static void free_radius(const short *labels, unsigned nx, unsigned ny, unsigned nz, std::vector<unsigned char> &out) {
+  const size_t n = (size_t)nx * ny * nz;
+  out.assign(n, 0);
+  std::vector<int> d(n);
+  auto at = [&](long x, long y, long z) { return (size_t)x + nx * ((size_t)y + ny * (size_t)z); };
+  for (long z = 0; z < (long)nz; ++z)
+    for (long y = 0; y < (long)ny; ++y)
+      for (long x = 0; x < (long)nx; ++x) {
+        const size_t i = at(x, y, z);
+        bool edge = false;
+        for (int c = 0; c < 27 && !edge; ++c) {
+          const long u = x + c % 3 - 1, v = y + (c / 3) % 3 - 1, w = z + c / 9 - 1;
+          if (u < 0 || v < 0 || w < 0 || u >= (long)nx || v >= (long)ny || w >= (long)nz) continue;
+          edge = labels[at(u, v, w)] != labels[i];
+        }
+        d[i] = edge ? 0 : INT_MAX / 2;
+      }
+  for (int pass = 0; pass < 2; ++pass) {
+    const long s = pass == 0 ? 1 : -1;
+    for (long zz = 0; zz < (long)nz; ++zz)
+      for (long yy = 0; yy < (long)ny; ++yy)
+        for (long xx = 0; xx < (long)nx; ++xx) {
+          const long x = pass == 0 ? xx : (long)nx - 1 - xx, y = pass == 0 ? yy : (long)ny - 1 - yy,
+                     z = pass == 0 ? zz : (long)nz - 1 - zz;
+          const size_t i = at(x, y, z);
+          if (d[i] == 0) continue;
+          for (int c = 0; c < 13; ++c) { /* the neighbours before this voxel in the pass's order */
+            const long dx = c % 3 - 1, dy = (c / 3) % 3 - 1, dz = c / 9 - 1;
+            const long u = x + s * dx, v = y + s * dy, w = z + s * dz;
+            if (u < 0 || v < 0 || w < 0 || u >= (long)nx || v >= (long)ny || w >= (long)nz) continue;
+            d[i] = std::min(d[i], d[at(u, v, w)] + 1);
+          }
+        }
+  }
+  for (size_t i = 0; i < n; ++i) out[i] = (unsigned char)std::min(d[i], ORACLE_FREE_MAX);
+}
+
+/* one free-radius map per phase kind, rebuilt by make_phase */
+static std::vector<unsigned char> g_free_r[2];
 
 void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
   memset(&ph, 0, sizeof(ph));
@@ -854,6 +1053,10 @@ void make_phase(const oracle_sim *sim, Phase &ph, int emission) {
       ph.prop[i].mutr = mut == 0.0f ? FLT_MAX : 1.0f / mut;
     }
   ph.labels = sim->bulk_info;
+  if (ph.exact) {
+    free_radius(ph.labels, ph.num_x, ph.num_y, ph.num_z, g_free_r[emission ? 1 : 0]);
+    ph.free_r = g_free_r[emission ? 1 : 0].data();
+  }
   if (ph.method == 1) {
     ph.n_layers = (unsigned)sim->n_layers;
     for (unsigned i = 0; i < ph.n_layers + 2 && i < ORACLE_MAX_LAYERS + 2; ++i) ph.layers[i] = sim->layers[i];

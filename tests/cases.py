@@ -181,6 +181,27 @@ def deep(photons=40000, per_voxel=40000) -> Case:
                 1.0, photons, per_voxel, (0.1, 0.1, 20, 20, 0.0, 0.0))
 
 
+def blocks(photons=40000, per_voxel=2000) -> Case:
+    """A larger grid (80 x 80 x 20 voxels of 0.05 cm) with long homogeneous
+    runs: a block of another refractive index and a fluorescent sphere in a
+    weakly scattering background (mean free path about one voxel), so that
+    voxel-boundary stepping crosses many faces and free cubes of radius up to
+    9 voxels."""
+    esp, grid = 1.0, 20
+    lab = _labels(esp, grid)
+    nz, ny, nx = lab.shape
+    lab[4:12, 30:44, 20:36] = 3
+    z = (np.arange(nz) + 0.5) / grid
+    y = (np.arange(ny) + 0.5) / grid - 2 * esp
+    x = (np.arange(nx) + 0.5) / grid - 2 * esp
+    m = ((x[None, None, :] - 0.4) ** 2 + (y[None, :, None] + 0.3) ** 2 + (z[:, None, None] - 0.45) ** 2) <= 0.3 ** 2
+    lab[m] = 2
+    return Case("blocks", esp, grid, lab,
+                [(1.4, 0.1, 20.0, 0.0, 0.0, 0.0, 0.0, 0.8), (1.4, 0.1, 20.0, 1.0, 0.5, 0.2, 0.1, 0.8),
+                 (1.6, 0.3, 40.0, 0.0, 0.0, 0.0, 0.0, 0.7)],
+                1.0, photons, per_voxel, (0.05, 0.05, 60, 60, 0.0, 0.0))
+
+
 def timed(photons=40000, per_voxel=40000, face=0, base=None) -> Case:
     """mismatch (or another case) with a 3 x 2 array of time-resolved
     detectors, discs of 0.15 cm 0.25 cm apart, on the entry (face 0) or exit
@@ -324,4 +345,4 @@ LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}
 
 # voxel-boundary stepping (no time-resolved detectors on this path)
 EXACT = {n + "_exact": exact(f) for n, f in {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere,
-                                              "deep": deep}.items()}
+                                              "deep": deep, "blocks": blocks}.items()}

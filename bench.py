@@ -197,6 +197,7 @@ def main():
     ap.add_argument("--photons", type=int, default=2_000_000)
     ap.add_argument("--variant", type=int, default=0, help="--profile: kernel variant (0..2)")
     ap.add_argument("--per-voxel", type=int, default=20, help="--profile: emission photons per emitting voxel")
+    ap.add_argument("--exact-stepping", action="store_true", help="--profile: voxel-boundary stepping")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -473,10 +474,12 @@ def profile_case(args):
     ctx.set_option("variant", args.variant)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
-    rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2)
+    rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2,
+                     exact_stepping=1 if args.exact_stepping else 0)
     for _ in range(args.warmup + 1):
         r = ctx.run(med, rd, images=False, raw=False)
     print(json.dumps({"profile_case": "config2", "math": args.math, "photons": args.photons,
+                      "exact_stepping": bool(args.exact_stepping),
                       "emission_photons": r.photons_fl, "steps_exc": r.stats_exc["steps"],
                       "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
                       "variant": args.variant, "regs": ctx.get_option("regs"), "grid": ctx.get_option("grid"),

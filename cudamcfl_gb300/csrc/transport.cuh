@@ -455,6 +455,14 @@ __device__ __forceinline__ real plane_dist(real b, real c, real d) {
   return t > MCFL_C(0.0) ? t : MCFL_C(0.0);
 }
 
+/* Voxel-boundary stepping: coordinate of grid face k along x, y, z (the z
+ * faces 0 and nz are the slab faces themselves). */
+__device__ __forceinline__ real face_x(const Med &m, int k) { return (real)k / m.gx - m.hx; }
+__device__ __forceinline__ real face_y(const Med &m, int k) { return (real)k / m.gy - m.hy; }
+__device__ __forceinline__ real face_z(const Med &m, int k) {
+  return k == 0 ? MCFL_C(0.0) : (k == (int)m.nz ? m.esp : (real)k / m.gz);
+}
+
 /* Fresnel reflection / refraction at a voxel face whose normal is axis a
  * (0, 1, 2 = x, y, z): reflect() with that axis in place of z.  Returns true
  * when the photon crosses. */
@@ -719,6 +727,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
   }
   Rec rc = {}; /* general kernel: the record of the photon's label, in registers */
+  /* voxel-boundary stepping: the state of the photon's pass between
+   * segments (remaining optical depth, ray origin, start of the label run,
+   * free radius, segments so far; xbegin: the origin is to be set) */
+  real xtau = MCFL_C(0.0), xox = MCFL_C(0.0), xoy = MCFL_C(0.0), xoz = MCFL_C(0.0), xs0 = MCFL_C(0.0);
+  int xcr = 0, xit = 0;
+  bool xmid = false, xbegin = false;
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
   const McflJob *J = nullptr;
@@ -813,131 +827,93 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (!alive) continue;
     }
 
-    ++pst;
+    if constexpr (!kExactStep) ++pst;
     if constexpr (kExactStep) {
-      /* ---- one pass with voxel-boundary stepping: the optical depth
-       * -ln(u) is spent voxel by voxel with each voxel's mu_t, the label is
-       * the one where the photon is, Fresnel acts at every face between
-       * different indices with that face's normal, scattering-free voxels
-       * are crossed without interaction.  The pass ends at the interaction
-       * (PHD tally, weight drop, spin, as the reference's pass) or at an
-       * exit.  Inside the grid the walk is a 3D DDA: distances along the ray
-       * from the origin (ox, oy, oz) — the pass start or the face where the
-       * direction last changed — with tx, ty, tz the distances to the next
-       * face along each axis, recomputed from the face index for the axis
-       * crossed only; a run of voxels of one label is charged its optical
-       * depth once, where the label changes (s0: where the run began).
-       * Outside the grid's lateral extent each region is one straight
-       * segment to a slab face or back into the grid. ---- */
-      real tau = -MCFL_LOGF(r.oc());
+      /* ---- voxel-boundary stepping, one segment per loop iteration: the
+       * optical depth -ln(u) of a pass is spent voxel by voxel with each
+       * voxel's mu_t, the label is the one where the photon is, Fresnel acts
+       * at every face between different indices with that face's normal,
+       * scattering-free voxels are crossed without interaction.  A pass ends
+       * at the interaction (PHD tally, weight drop, spin, as the reference's
+       * pass) or at an exit.  Inside the grid a segment goes from the
+       * photon's voxel straight to the face of its free cube (radius xcr of
+       * the label + free-radius map, clipped to the grid; the voxel itself
+       * when 0), or to the interaction inside it, and then across that face;
+       * distances run along the ray from an origin (xo*) — the pass start or
+       * the face where the direction last changed — and a run of voxels of
+       * one label is charged its optical depth once, where the label changes
+       * (xs0: where the run began).  Outside the grid's lateral extent a
+       * segment is one straight line to a slab face or back into the grid.
+       * The pass state (xtau, xo*, xs0, xcr, xit) lives across iterations,
+       * so every lane of a warp runs one segment per iteration, whatever
+       * number of segments its pass needs. ---- */
+      if (!xmid) { /* a new pass */
+        ++pst;
+        xtau = -MCFL_LOGF(r.oc());
+        xit = 0;
+        xmid = true;
+        xbegin = true;
+      }
       const int cap = 16 + 4 * (int)(m.nx + m.ny + m.nz);
-      int itv = 0;
-      bool interact = false, lost = false;
-      auto face_x = [&](int k) { return (real)k / m.gx - m.hx; };
-      auto face_y = [&](int k) { return (real)k / m.gy - m.hy; };
-      auto face_z = [&](int k) {
-        return k == 0 ? MCFL_C(0.0) : (k == (int)m.nz ? m.esp : (real)k / m.gz);
-      };
-      for (;;) {
-        if (p.ingrid) {
-          const real ox = p.x, oy = p.y, oz = p.z;
-          /* tx, ty, tz: the next faces of the photon's voxel, computed when a
-           * step needs them (tv), never behind the distance a free cube took
-           * it to (floor_s); after a free cube the photon crosses its face
-           * next (jumped) */
-          real tx = MCFL_C(0.0), ty = MCFL_C(0.0), tz = MCFL_C(0.0), floor_s = MCFL_C(0.0);
-          bool tv = false, jumped = false;
-          real s0 = MCFL_C(0.0);
-          int cr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
-          bool restart = false, done_pass = false;
-          while (!restart) {
-            if (++itv > cap) {
-              lost = true;
-              done_pass = true;
-              break;
+      /* 0: the pass goes on, 1: interaction, 2: exit (tallied), 3: lost */
+      int outcome = 0;
+      if (p.ingrid) {
+        if (xbegin) {
+          xox = p.x;
+          xoy = p.y;
+          xoz = p.z;
+          xs0 = MCFL_C(0.0);
+          xcr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
+          xbegin = false;
+        }
+        if (++xit > cap) {
+          outcome = 3;
+        } else {
+          const real4 ca = s_lab[2 * p.label];
+          const int cr = xcr;
+          const int lx = max(p.ix - cr, 0), ux = min(p.ix + cr, (int)m.nx - 1);
+          const int ly = max(p.iy - cr, 0), uy = min(p.iy + cr, (int)m.ny - 1);
+          const int lz = max(p.iz - cr, 0), uz = min(p.iz + cr, (int)m.nz - 1);
+          const real cx = plane_dist(face_x(m, p.dx > MCFL_C(0.0) ? ux + 1 : lx), xox, p.dx);
+          const real cy = plane_dist(face_y(m, p.dy > MCFL_C(0.0) ? uy + 1 : ly), xoy, p.dy);
+          const real cz = plane_dist(face_z(m, p.dz > MCFL_C(0.0) ? uz + 1 : lz), xoz, p.dz);
+          real db = cx;
+          int axis = 0;
+          if (cy < db) { db = cy; axis = 1; }
+          if (cz < db) { db = cz; axis = 2; }
+          real sj = db;
+          bool hit = false;
+          if (ca.x != FLT_MAX) {
+            const real s_int = xs0 + xtau * ca.x;
+            if (s_int <= db) {
+              sj = s_int;
+              hit = true;
             }
-            const real4 ca = s_lab[2 * p.label];
-            if (cr > 0 && !jumped) {
-              /* every voxel within cr of this one carries its label: straight
-               * to the face of that cube (clipped to the grid), or to the
-               * interaction inside it */
-              const int lx = max(p.ix - cr, 0), ux = min(p.ix + cr, (int)m.nx - 1);
-              const int ly = max(p.iy - cr, 0), uy = min(p.iy + cr, (int)m.ny - 1);
-              const int lz = max(p.iz - cr, 0), uz = min(p.iz + cr, (int)m.nz - 1);
-              const real cx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? ux + 1 : lx), ox, p.dx);
-              const real cy = plane_dist(face_y(p.dy > MCFL_C(0.0) ? uy + 1 : ly), oy, p.dy);
-              const real cz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? uz + 1 : lz), oz, p.dz);
-              real db = cx;
-              int axis = 0;
-              if (cy < db) { db = cy; axis = 1; }
-              if (cz < db) { db = cz; axis = 2; }
-              real sj = db;
-              bool hit = false;
-              if (ca.x != FLT_MAX) {
-                const real s_int = s0 + tau * ca.x;
-                if (s_int <= db) {
-                  sj = s_int;
-                  hit = true;
-                }
-              }
-              const real x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
-              /* the voxel there, kept inside the cube (on its face along the exit axis) */
-              const int jx = (!hit && axis == 0) ? (p.dx > MCFL_C(0.0) ? ux : lx)
-                                                 : min(max((int)MCFL_R2U_RZ((x + m.hx) * m.gx), lx), ux);
-              const int jy = (!hit && axis == 1) ? (p.dy > MCFL_C(0.0) ? uy : ly)
-                                                 : min(max((int)MCFL_R2U_RZ((y + m.hy) * m.gy), ly), uy);
-              const int jz = (!hit && axis == 2) ? (p.dz > MCFL_C(0.0) ? uz : lz)
-                                                 : min(max((int)MCFL_R2U_RZ(z * m.gz), lz), uz);
-              p.ix = jx;
-              p.iy = jy;
-              p.iz = jz;
-              if (hit) {
-                p.x = x;
-                p.y = y;
-                p.z = z;
-                interact = true;
-                done_pass = true;
-                break;
-              }
-              cr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
-              floor_s = db;
-              tv = false;
-              jumped = true;
-              continue;
-            }
-            jumped = false;
-            if (!tv) {
-              tx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix), ox, p.dx);
-              ty = plane_dist(face_y(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy), oy, p.dy);
-              tz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz), oz, p.dz);
-              /* never behind the cube's face */
-              if (tx < floor_s) tx = floor_s;
-              if (ty < floor_s) ty = floor_s;
-              if (tz < floor_s) tz = floor_s;
-              tv = true;
-            }
-            real db = tx;
-            int axis = 0;
-            if (ty < db) { db = ty; axis = 1; }
-            if (tz < db) { db = tz; axis = 2; }
-            if (ca.x != FLT_MAX) {
-              const real s_int = s0 + tau * ca.x;
-              if (s_int <= db) { /* the interaction happens in this voxel */
-                p.x = ox + p.dx * s_int;
-                p.y = oy + p.dy * s_int;
-                p.z = oz + p.dz * s_int;
-                interact = true;
-                done_pass = true;
-                break;
-              }
-            }
+          }
+          const real x = xox + p.dx * sj, y = xoy + p.dy * sj, z = xoz + p.dz * sj;
+          /* the voxel there, inside the cube (its last layer along the exit axis) */
+          const int fx = (!hit && axis == 0) ? (p.dx > MCFL_C(0.0) ? ux : lx)
+                                             : min(max((int)MCFL_R2U_RZ((x + m.hx) * m.gx), lx), ux);
+          const int fy = (!hit && axis == 1) ? (p.dy > MCFL_C(0.0) ? uy : ly)
+                                             : min(max((int)MCFL_R2U_RZ((y + m.hy) * m.gy), ly), uy);
+          const int fz = (!hit && axis == 2) ? (p.dz > MCFL_C(0.0) ? uz : lz)
+                                             : min(max((int)MCFL_R2U_RZ(z * m.gz), lz), uz);
+          if (hit) {
+            p.ix = fx;
+            p.iy = fy;
+            p.iz = fz;
+            p.x = x;
+            p.y = y;
+            p.z = z;
+            outcome = 1;
+          } else {
             /* the region across the face */
-            int nix = p.ix, niy = p.iy, niz = p.iz, nin = 1;
+            int nix = fx, niy = fy, niz = fz, nin = 1;
             if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
             else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
             else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
             uint32_t next;
-            int nr = 0; /* the free radius there */
+            int nr = 0;
             if (niz < 0) next = 0u;
             else if (niz >= (int)m.nz) next = m.last;
             else if (nix < 0 || nix >= (int)m.nx || niy < 0 || niy >= (int)m.ny) {
@@ -948,59 +924,59 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               next = q & 0xffu;
               nr = (int)(q >> 8);
             }
-            if (next != p.label || !nin) {
+            if (next == p.label && nin) { /* the same label: on, without a stop */
+              p.ix = nix;
+              p.iy = niy;
+              p.iz = niz;
+              xcr = nr;
+            } else {
               /* the run of this label ends at the face */
               if (ca.x != FLT_MAX) {
-                tau -= (db - s0) / ca.x;
-                if (tau < MCFL_C(0.0)) tau = MCFL_C(0.0);
+                xtau -= (db - xs0) / ca.x;
+                if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
               }
-              s0 = db;
-              p.x = ox + p.dx * db;
-              p.y = oy + p.dy * db;
-              p.z = oz + p.dz * db;
+              xs0 = db;
+              p.x = x;
+              p.y = y;
+              p.z = z;
+              bool restart = !nin, reflected = false;
               if (next != p.label) {
                 const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
-                const bool bent = n_here != n_next;
-                if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: same voxel, new direction */
-                  restart = true;
-                  continue;
+                if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: the face voxel, a new direction */
+                  p.ix = fx;
+                  p.iy = fy;
+                  p.iz = fz;
+                  reflected = true;
+                  xbegin = true;
+                } else if (n_here != n_next) {
+                  restart = true; /* refracted: a new direction */
                 }
-                restart = bent;
               }
-              p.label = next;
-              p.ix = nix;
-              p.iy = niy;
-              p.iz = niz;
-              p.ingrid = nin;
-              if (next == 0u || next == m.last) {
-                const bool top = next == 0u;
-                tally_exit(J, p.x, p.y, p.weight, top, src_idx);
-                ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
-                p.weight = 0u;
-                done_pass = true;
-                break;
+              if (!reflected) {
+                p.label = next;
+                p.ix = nix;
+                p.iy = niy;
+                p.iz = niz;
+                p.ingrid = nin;
+                if (next == 0u || next == m.last) {
+                  const bool top = next == 0u;
+                  tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+                  ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+                  p.weight = 0u;
+                  outcome = 2;
+                } else if (restart) {
+                  xbegin = true;
+                } else {
+                  xcr = nr;
+                }
               }
-              if (!nin) restart = true;
-              if (restart) continue;
-            } else {
-              p.ix = nix;
-              p.iy = niy;
-              p.iz = niz;
             }
-            cr = nr;
-            /* the next face along the axis crossed */
-            if (axis == 0) tx = plane_dist(face_x(p.dx > MCFL_C(0.0) ? p.ix + 1 : p.ix), ox, p.dx);
-            else if (axis == 1) ty = plane_dist(face_y(p.dy > MCFL_C(0.0) ? p.iy + 1 : p.iy), oy, p.dy);
-            else tz = plane_dist(face_z(p.dz > MCFL_C(0.0) ? p.iz + 1 : p.iz), oz, p.dz);
           }
-          if (done_pass) break;
-          continue;
         }
+      } else if (++xit > cap) {
+        outcome = 3;
+      } else {
         /* outside the grid's lateral extent: one straight segment */
-        if (++itv > cap) {
-          lost = true;
-          break;
-        }
         const real4 ca = s_lab[2 * p.label];
         real db = plane_dist(p.dz > MCFL_C(0.0) ? m.esp : MCFL_C(0.0), p.z, p.dz);
         int axis = 2;
@@ -1016,56 +992,61 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           const real xc = p.x + p.dx * t;
           if (t < db && MCFL_FABS(xc) < m.hx) { db = t; axis = 1; }
         }
+        bool hit = false;
         if (ca.x != FLT_MAX) {
-          const real s_int = tau * ca.x;
+          const real s_int = xtau * ca.x;
           if (s_int <= db) {
             p.x += p.dx * s_int;
             p.y += p.dy * s_int;
             p.z += p.dz * s_int;
-            interact = true;
-            break;
+            hit = true;
+            outcome = 1;
           }
         }
-        if (db == FLT_MAX) { /* scattering-free with no face ahead */
-          lost = true;
-          break;
-        }
-        p.x += p.dx * db;
-        p.y += p.dy * db;
-        p.z += p.dz * db;
-        if (ca.x != FLT_MAX) {
-          tau -= db / ca.x;
-          if (tau < MCFL_C(0.0)) tau = MCFL_C(0.0);
-        }
-        int nix = p.ix, niy = p.iy, niz = p.iz;
-        uint32_t next;
-        if (axis == 2) {
-          next = p.dz > MCFL_C(0.0) ? m.last : 0u;
-        } else {
-          nix = axis == 0 ? (p.dx > MCFL_C(0.0) ? 0 : (int)m.nx - 1)
-                          : (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
-          niy = axis == 1 ? (p.dy > MCFL_C(0.0) ? 0 : (int)m.ny - 1)
-                          : (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
-          niz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
-          next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
-        }
-        if (next != p.label && !refract_axis(p, axis, s_lab[2 * p.label + 1].w, s_lab[2 * next + 1].w, r)) continue;
-        p.label = next;
-        if (axis != 2) {
-          p.ix = nix;
-          p.iy = niy;
-          p.iz = niz;
-          p.ingrid = 1;
-        }
-        if (next == 0u || next == m.last) {
-          const bool top = next == 0u;
-          tally_exit(J, p.x, p.y, p.weight, top, src_idx);
-          ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
-          p.weight = 0u;
-          break;
+        if (!hit && db == FLT_MAX) { /* scattering-free with no face ahead */
+          outcome = 3;
+        } else if (!hit) {
+          p.x += p.dx * db;
+          p.y += p.dy * db;
+          p.z += p.dz * db;
+          if (ca.x != FLT_MAX) {
+            xtau -= db / ca.x;
+            if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
+          }
+          xbegin = true;
+          int nix = p.ix, niy = p.iy, niz = p.iz;
+          uint32_t next;
+          if (axis == 2) {
+            next = p.dz > MCFL_C(0.0) ? m.last : 0u;
+          } else {
+            nix = axis == 0 ? (p.dx > MCFL_C(0.0) ? 0 : (int)m.nx - 1)
+                            : (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
+            niy = axis == 1 ? (p.dy > MCFL_C(0.0) ? 0 : (int)m.ny - 1)
+                            : (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
+            niz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
+            next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
+          }
+          if (next == p.label || refract_axis(p, axis, s_lab[2 * p.label + 1].w, s_lab[2 * next + 1].w, r)) {
+            p.label = next;
+            if (axis != 2) {
+              p.ix = nix;
+              p.iy = niy;
+              p.iz = niz;
+              p.ingrid = 1;
+            }
+            if (next == 0u || next == m.last) {
+              const bool top = next == 0u;
+              tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+              ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+              p.weight = 0u;
+              outcome = 2;
+            }
+          }
         }
       }
-      if (interact) {
+      if (outcome == 0) continue; /* the pass goes on in the next iteration */
+      xmid = false;
+      if (outcome == 1) {
         if (m.fhd && p.ingrid)
           atomicAdd(&m.fhd[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)],
                     (unsigned long long)p.weight);
@@ -1079,7 +1060,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.weight = 0u;
         }
         spin(p, c2, r);
-      } else if (lost && p.weight) { /* cannot reach an interaction (cap or no face ahead) */
+      } else if (outcome == 3 && p.weight) { /* cannot reach an interaction (cap or no face ahead) */
         ev_add(MCFL_ST_W0_LOSS, p.weight);
         p.weight = 0u;
       }

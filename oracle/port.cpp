@@ -680,25 +680,6 @@ inline float face_coord(const Phase &ph, int a, int k) {
   return k == 0 ? 0.0f : (k == (int)ph.num_z ? ph.esp : (float)k / ph.gz);
 }
 
-/* The region across a face crossed along axis from the photon's voxel (the
- * grid, the slab's outer media or, laterally, the medium of label 1). */
-inline uint32_t region_across(const Photon &p, const Phase &ph, int axis, int &nix, int &niy, int &niz, int &nin) {
-  nix = p.ix;
-  niy = p.iy;
-  niz = p.iz;
-  nin = 1;
-  if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
-  else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
-  else niz += p.dz > 0.0f ? 1 : -1;
-  if (niz < 0) return 0;
-  if (niz >= (int)ph.num_z) return ph.last_bulk;
-  if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
-    nin = 0;
-    return 1;
-  }
-  return (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
-}
-
 /* An exit through a slab face: the image tally. */
 inline void exact_exit(Photon &p, const Phase &ph, Sink &sk, bool top) {
   if (fabsf(p.x - ph.det_x0) < ph.size_x && fabsf(p.y - ph.det_y0) < ph.size_y) {
@@ -722,14 +703,15 @@ inline void exact_exit(Photon &p, const Phase &ph, Sink &sk, bool top) {
  * ends at the interaction (PHD tally, weight drop and spin as the reference's
  * pass) or at an exit.
  *
- * Inside the grid the walk is a 3D DDA (Amanatides & Woo): distances are
- * measured along the ray from an origin o (the pass start, or the face where
- * the direction last changed); t[a] is the distance to the next face along
- * axis a, recomputed from the face index for the axis crossed only.  Within a
- * run of voxels of one label only the voxel index and t change; the optical
- * depth of the run is charged when the label changes (s0: where the run
- * began).  Outside the grid's lateral extent (the medium of label 1) each
- * region is one straight segment to a slab face or back into the grid. */
+ * Inside the grid distances run along the ray from an origin o (the pass
+ * start, or the face where the direction last changed).  Each step goes from
+ * the photon's voxel straight to the face of its free cube (every voxel of
+ * the grid within the free radius carries the same label; the voxel itself
+ * when the radius is 0), or to the interaction inside it, and then across
+ * that face; a run of voxels of one label is charged its optical depth once,
+ * where the label changes (s0: where the run began).  Outside the grid's
+ * lateral extent (the medium of label 1) each region is one straight
+ * segment to a slab face or back into the grid. */
 template <class M>
 unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   const uint32_t last = ph.last_bulk;
@@ -739,132 +721,111 @@ unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   int it = 0;
   for (;;) {
     if (p.ingrid) {
+      /* one segment per iteration: from the photon's voxel straight to the
+       * face of its free cube (radius cr, clipped to the grid; the voxel
+       * itself when cr = 0), or to the interaction inside it; then across
+       * that face */
       const float ox = p.x, oy = p.y, oz = p.z;
-      /* t: the next faces of the photon's voxel, computed when a step needs
-       * them (tv), never behind the distance a free cube took it to (floor) */
-      float t[3] = {0.0f, 0.0f, 0.0f}, floor_s = 0.0f;
-      bool tv = false;
-      bool jumped = false; /* a free cube took the photon to its face: cross that face next */
       float s0 = 0.0f;
       int cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
-      bool restart = false;
-      while (!restart) {
+      for (;;) {
         if (++it > cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
           sk.w0_loss += p.weight;
           p.weight = 0u;
           return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
         }
         const Prop &pr = ph.prop[p.bulkpos];
-        if (cr > 0 && !jumped) {
-          /* every voxel within cr of this one carries its label: straight to
-           * the face of that cube (clipped to the grid), or to the
-           * interaction inside it */
-          const int lx = std::max(p.ix - cr, 0), ux = std::min(p.ix + cr, (int)ph.num_x - 1);
-          const int ly = std::max(p.iy - cr, 0), uy = std::min(p.iy + cr, (int)ph.num_y - 1);
-          const int lz = std::max(p.iz - cr, 0), uz = std::min(p.iz + cr, (int)ph.num_z - 1);
-          const float cx = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? ux + 1 : lx), ox, p.dx);
-          const float cy = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? uy + 1 : ly), oy, p.dy);
-          const float cz = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? uz + 1 : lz), oz, p.dz);
-          float db = cx;
-          int axis = 0;
-          if (cy < db) { db = cy; axis = 1; }
-          if (cz < db) { db = cz; axis = 2; }
-          float sj = db;
-          bool hit = false;
-          if (pr.mutr != FLT_MAX) {
-            const float s_int = s0 + tau * pr.mutr;
-            if (s_int <= db) {
-              sj = s_int;
-              hit = true;
-            }
-          }
-          const float x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
-          /* the voxel there, kept inside the cube (on its face along the exit axis) */
-          const int jx = (!hit && axis == 0) ? (p.dx > 0.0f ? ux : lx)
-                                             : std::min(std::max((int)mcfl_f2u_rz((x + ph.hx) * ph.gx), lx), ux);
-          const int jy = (!hit && axis == 1) ? (p.dy > 0.0f ? uy : ly)
-                                             : std::min(std::max((int)mcfl_f2u_rz((y + ph.hy) * ph.gy), ly), uy);
-          const int jz = (!hit && axis == 2) ? (p.dz > 0.0f ? uz : lz)
-                                             : std::min(std::max((int)mcfl_f2u_rz(z * ph.gz), lz), uz);
-          p.ix = jx;
-          p.iy = jy;
-          p.iz = jz;
-          if (hit) {
-            p.x = x;
-            p.y = y;
-            p.z = z;
-            goto interaction;
-          }
-          cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
-          floor_s = db;
-          tv = false;
-          jumped = true;
-          continue;
-        }
-        jumped = false;
-        if (!tv) {
-          t[0] = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? p.ix + 1 : p.ix), ox, p.dx);
-          t[1] = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? p.iy + 1 : p.iy), oy, p.dy);
-          t[2] = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? p.iz + 1 : p.iz), oz, p.dz);
-          for (int a = 0; a < 3; ++a) /* never behind the cube's face */
-            if (t[a] < floor_s) t[a] = floor_s;
-          tv = true;
-        }
-        float db = t[0];
+        const int lx = std::max(p.ix - cr, 0), ux = std::min(p.ix + cr, (int)ph.num_x - 1);
+        const int ly = std::max(p.iy - cr, 0), uy = std::min(p.iy + cr, (int)ph.num_y - 1);
+        const int lz = std::max(p.iz - cr, 0), uz = std::min(p.iz + cr, (int)ph.num_z - 1);
+        const float cx = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? ux + 1 : lx), ox, p.dx);
+        const float cy = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? uy + 1 : ly), oy, p.dy);
+        const float cz = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? uz + 1 : lz), oz, p.dz);
+        float db = cx;
         int axis = 0;
-        if (t[1] < db) { db = t[1]; axis = 1; }
-        if (t[2] < db) { db = t[2]; axis = 2; }
+        if (cy < db) { db = cy; axis = 1; }
+        if (cz < db) { db = cz; axis = 2; }
+        float sj = db;
+        bool hit = false;
         if (pr.mutr != FLT_MAX) {
           const float s_int = s0 + tau * pr.mutr;
-          if (s_int <= db) { /* the interaction happens in this voxel */
-            p.x = ox + p.dx * s_int;
-            p.y = oy + p.dy * s_int;
-            p.z = oz + p.dz * s_int;
-            goto interaction;
+          if (s_int <= db) {
+            sj = s_int;
+            hit = true;
           }
         }
-        int nix, niy, niz, nin;
-        const uint32_t next = region_across(p, ph, axis, nix, niy, niz, nin);
-        if (next != p.bulkpos || !nin) {
-          /* the run of this label ends at the face */
-          if (pr.mutr != FLT_MAX) {
-            tau -= (db - s0) / pr.mutr;
-            if (tau < 0.0f) tau = 0.0f;
-          }
-          s0 = db;
-          p.x = ox + p.dx * db;
-          p.y = oy + p.dy * db;
-          p.z = oz + p.dz * db;
-          const float n_next = ph.prop[next].n;
-          if (next != p.bulkpos) {
-            const bool bent = pr.n != n_next;
-            if (!refract_axis(p, axis, pr.n, n_next, r)) { /* reflected: same voxel, new direction */
-              restart = true;
-              continue;
-            }
-            restart = bent;
-          }
-          p.bulkpos = next;
-          p.ix = nix;
-          p.iy = niy;
-          p.iz = niz;
-          p.ingrid = nin;
-          if (next == 0 || next == last) {
-            exact_exit(p, ph, sk, next == 0);
-            return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
-          }
-          if (!nin) restart = true;
-          if (restart) continue;
+        const float x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
+        /* the voxel there, inside the cube (its last layer along the exit axis) */
+        const int fx = (!hit && axis == 0) ? (p.dx > 0.0f ? ux : lx)
+                                           : std::min(std::max((int)mcfl_f2u_rz((x + ph.hx) * ph.gx), lx), ux);
+        const int fy = (!hit && axis == 1) ? (p.dy > 0.0f ? uy : ly)
+                                           : std::min(std::max((int)mcfl_f2u_rz((y + ph.hy) * ph.gy), ly), uy);
+        const int fz = (!hit && axis == 2) ? (p.dz > 0.0f ? uz : lz)
+                                           : std::min(std::max((int)mcfl_f2u_rz(z * ph.gz), lz), uz);
+        if (hit) {
+          p.ix = fx;
+          p.iy = fy;
+          p.iz = fz;
+          p.x = x;
+          p.y = y;
+          p.z = z;
+          goto interaction;
+        }
+        /* the region across the face */
+        int nix = fx, niy = fy, niz = fz, nin = 1;
+        if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
+        else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
+        else niz += p.dz > 0.0f ? 1 : -1;
+        uint32_t next;
+        int nr = 0;
+        if (niz < 0) next = 0;
+        else if (niz >= (int)ph.num_z) next = last;
+        else if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
+          next = 1;
+          nin = 0;
         } else {
+          const size_t q = (size_t)nix + ph.num_x * ((size_t)niy + ph.num_y * (size_t)niz);
+          next = (uint32_t)(unsigned short)ph.labels[q];
+          nr = ph.free_r[q];
+        }
+        if (next == p.bulkpos && nin) { /* the same label: on, without a stop */
           p.ix = nix;
           p.iy = niy;
           p.iz = niz;
+          cr = nr;
+          continue;
         }
-        cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
-        /* the next face along the axis crossed */
-        if (axis == 0) t[0] = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? p.ix + 1 : p.ix), ox, p.dx);
-        else if (axis == 1) t[1] = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? p.iy + 1 : p.iy), oy, p.dy);
-        else t[2] = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? p.iz + 1 : p.iz), oz, p.dz);
+        /* the run of this label ends at the face */
+        if (pr.mutr != FLT_MAX) {
+          tau -= (db - s0) / pr.mutr;
+          if (tau < 0.0f) tau = 0.0f;
+        }
+        s0 = db;
+        p.x = x;
+        p.y = y;
+        p.z = z;
+        bool restart = !nin;
+        if (next != p.bulkpos) {
+          const float n_next = ph.prop[next].n;
+          if (!refract_axis(p, axis, pr.n, n_next, r)) { /* reflected: the face voxel, a new direction */
+            p.ix = fx;
+            p.iy = fy;
+            p.iz = fz;
+            break;
+          }
+          if (pr.n != n_next) restart = true; /* refracted: a new direction */
+        }
+        p.bulkpos = next;
+        p.ix = nix;
+        p.iy = niy;
+        p.iz = niz;
+        p.ingrid = nin;
+        if (next == 0 || next == last) {
+          exact_exit(p, ph, sk, next == 0);
+          return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+        }
+        if (restart) break;
+        cr = nr;
       }
       continue;
     }

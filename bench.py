@@ -124,7 +124,7 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ CPU arm
 
-def cpu_reference_sample(nthreads: int, exc_photons: int = 2_000_000, fl_voxels: int = 8, per_voxel: int = 40_000):
+def cpu_reference_sample(nthreads: int, exc_photons: int = 4_000_000, fl_voxels: int = 16, per_voxel: int = 40_000):
     """The reference's transport algorithm on host threads over the benchmark
     medium (reference RNG streams and relaunch schedule, C-library math).
     Returns (photons/s, photons, seconds, description)."""

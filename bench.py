@@ -284,6 +284,7 @@ def main():
                    "schedule": "batched: one persistent launch per phase, CUDA-graph replay",
                    "variant": variant, "block": ctx.get_option("launch_block"), "grid": ctx.get_option("grid"),
                    "regs": ctx.get_option("regs"), "l2_window": ctx.get_option("l2_window"),
+                   "phd_agg": ctx.get_option("phd_agg"),
                    "autotune_sample_photons_per_s": tune_rate},
         "phases": {"excitation_ms": statistics.mean(exc_ms), "emission_ms": statistics.mean(fl_ms),
                    "excitation_photons_per_s": EXC_PHOTONS / (statistics.mean(exc_ms) / 1e3),

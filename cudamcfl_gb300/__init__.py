@@ -360,8 +360,9 @@ class Context:
         check(load().mcfl_set_stream(self.handle, stream_handle))
 
     def autotune(self, medium: "Medium", rd: RunDesc, sample_photons: int = 2_000_000) -> tuple[int, float]:
-        """Times every kernel variant (with and without the L2 window) on a
-        sample of `rd` and keeps the fastest; returns (variant, photons/s)."""
+        """Times every kernel variant (with and without the L2 window, with
+        each form of the photon-hitting-density tally when `rd` tallies it) on
+        a sample of `rd` and keeps the fastest; returns (variant, photons/s)."""
         v = ctypes.c_int(0)
         rate = ctypes.c_double(0.0)
         check(load().mcfl_autotune(self.handle, medium.handle, ctypes.byref(rd), int(sample_photons),

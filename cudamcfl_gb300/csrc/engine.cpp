@@ -75,7 +75,7 @@ int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool 
   *bps = 0;
   *regs = 0;
   const int mixed = mixed_variant == 1 ? -3 : mixed_variant == 2 ? -4 : -1;
-  const int v = exact ? 6 : uniform ? (time ? 3 : variant) : (time ? -2 : mixed);
+  const int v = exact ? 6 : uniform ? (time ? 3 : variant_code()) : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
@@ -168,6 +168,8 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
   } else if (k == "variant") {
     if (v < 0 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant: 0..2");
     c->variant = (int)v;
+  } else if (k == "phd_agg") {
+    c->phd_agg = v ? 1 : 0;
   } else if (k == "mixed_variant") {
     if (v < 0 || v > 2) return fail(MCFL_E_ARG, "mixed_variant: 0..2");
     c->mixed_variant = (int)v;
@@ -204,6 +206,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "block") return c->block;
   if (k == "blocks_per_sm") return c->blocks_per_sm;
   if (k == "variant") return c->variant;
+  if (k == "phd_agg") return c->phd_agg;
   if (k == "mixed_variant") return c->mixed_variant;
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;

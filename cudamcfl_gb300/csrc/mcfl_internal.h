@@ -160,6 +160,9 @@ struct mcfl_ctx {
   int math = MCFL_MATH_EXACT;
   int block = 256;   /* threads per block, clamped to the variant's bound */
   int variant = 0;   /* occupancy variant of the single-medium kernel */
+  int phd_agg = 0;   /* 1: photon-hitting-density sums held in a register (kernel variants 7..9) */
+  /* the single-medium kernel variant the launches use */
+  int variant_code() const { return variant + (phd_agg ? 7 : 0); }
   int mixed_variant = 2; /* occupancy variant of the mixed-media kernel (128 x 7 measured fastest) */
   int blocks_per_sm = 0;
   uint32_t step_cap = 1u << 24;

@@ -235,7 +235,7 @@ McflLaunch base_launch(mcfl_ctx *c) {
   std::memset(&L, 0, sizeof(L));
   L.mult = c->mult.as<uint32_t>();
   L.step_cap = c->step_cap;
-  L.variant = (uint32_t)c->variant;
+  L.variant = (uint32_t)c->variant_code();
   return L;
 }
 
@@ -424,7 +424,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                    timed ? c->tarr.p : nullptr},
                                   {xy, nv, (unsigned long long)emission, (unsigned long long)fluence, photons,
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
-                                   (unsigned long long)block, c->step_cap, (unsigned long long)c->variant,
+                                   (unsigned long long)block, c->step_cap, (unsigned long long)c->variant_code(),
                                    (unsigned long long)c->l2_window, tsize, (unsigned long long)grid_exc,
                                    (unsigned long long)block_exc, (unsigned long long)exact, m->serial});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
@@ -585,7 +585,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
     std::string key =
         ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
-                 c->step_cap, (unsigned long long)c->variant, (unsigned long long)c->l2_window,
+                 c->step_cap, (unsigned long long)c->variant_code(), (unsigned long long)c->l2_window,
                  (unsigned long long)uniform, (unsigned long long)exact, m->serial});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;

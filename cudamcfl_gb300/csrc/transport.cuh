@@ -657,7 +657,11 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
  * instead of per-lane registers loaded from the job. */
 /* kMode: 0 = the reference's voxelized transport (MCd3D), 1 = layered media
  * (MCd), 2 = voxel-boundary ("exact") stepping. */
-template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks>
+/* kPhdAgg (single medium, reference stepping): the photon-hitting-density
+ * tally sums the weights of a thread's successive passes in one voxel in a
+ * register and adds them to HBM when the voxel changes (and at the end),
+ * instead of one atomic add per pass; the autotuner picks the form. */
+template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks, bool kPhdAgg = false>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   constexpr bool kLayered = kMode == 1;
   constexpr bool kExactStep = kMode == 2;
@@ -733,6 +737,9 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   real xtau = MCFL_C(0.0), xox = MCFL_C(0.0), xoy = MCFL_C(0.0), xoz = MCFL_C(0.0), xs0 = MCFL_C(0.0);
   int xcr = 0, xit = 0;
   bool xmid = false, xbegin = false;
+  /* kPhdAgg: the voxel and the weight summed there so far */
+  uint32_t f_idx = 0;
+  unsigned long long f_acc = 0ull;
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
   const McflJob *J = nullptr;
@@ -1170,7 +1177,16 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
      * looked up unless the pass was clipped to a face */
     if (m.fhd && (vi != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp))) {
       const uint32_t fi = vi != 0xffffffffu ? vi : voxel_index(m, p.x, p.y, p.z);
-      atomicAdd(&m.fhd[fi], (unsigned long long)p.weight);
+      if constexpr (kPhdAgg) {
+        if (fi != f_idx) {
+          if (f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
+          f_idx = fi;
+          f_acc = 0ull;
+        }
+        f_acc += p.weight;
+      } else {
+        atomicAdd(&m.fhd[fi], (unsigned long long)p.weight);
+      }
     }
     if (p.label == 0u || p.label == m.last) {
       const bool top = p.label == 0u;
@@ -1216,6 +1232,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
   }
   if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
+  if (kPhdAgg && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 
   if (!kUniform && L.max_iters && L.saved) {
     McflSaved sv;
@@ -1245,7 +1262,8 @@ static size_t smem_bytes(int block, bool uniform) {
 
 /* Kernel variants.  Single medium (occupancy variants: threads per block x
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
- * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner; 3 = 256 x 3 carrying
+ * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner, and 7, 8, 9 the same
+ * with the photon-hitting-density sums held in a register; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
  * of flight; voxel-boundary stepping 6 = 256 x 4.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
  * -2 = 256 x 2 with the time of flight. */
@@ -1267,6 +1285,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case 4: *threads = 256; return MCFL_KERNEL_NAME<true, false, 1, 256, 4>;
   case 5: *threads = 256; return MCFL_KERNEL_NAME<true, true, 1, 256, 3>;
   case 6: *threads = 256; return MCFL_KERNEL_NAME<true, false, 2, 256, 4>;
+  case 7: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, true>;
+  case 8: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, true>;
+  case 9: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, true>;
   default: *threads = 0; return nullptr;
   }
 }

@@ -247,16 +247,36 @@ __device__ __forceinline__ uint32_t find_job(const McflJob *jobs, const uint32_t
   return (t >= b && t - b < n) ? slot : 0xffffffffu;
 }
 
-/* The photon's voxel from its position (voxel-boundary stepping). */
+/* Voxel-boundary stepping: voxel (x, y) lies in the grid's lateral extent. */
+__device__ __forceinline__ bool in_grid(const Med &m, int x, int y) {
+  return x >= 0 && x < (int)m.nx && y >= 0 && y < (int)m.ny;
+}
+
+__device__ __forceinline__ int vfloor(real v) { return (int)floor(v); }
+
+/* The photon's voxel from its position, for voxel-boundary stepping: beyond
+ * the grid's lateral extent the slab continues as virtual voxels of label 1
+ * (the reference's medium there), so the lateral indices are any integers. */
 __device__ __forceinline__ void locate(Photon &p, const Med &m) {
-  if (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy) {
-    p.ix = (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
-    p.iy = (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
-    p.iz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
-    p.ingrid = 1;
+  p.ix = vfloor((p.x + m.hx) * m.gx);
+  p.iy = vfloor((p.y + m.hy) * m.gy);
+  p.iz = min(max(vfloor(p.z * m.gz), 0), (int)m.nz - 1);
+  p.ingrid = in_grid(m, p.ix, p.iy) ? 1 : 0;
+}
+
+/* Label and free radius of voxel (x, y, z), z inside the slab: the grid's
+ * label + free-radius map, or beyond the grid's lateral extent label 1 with
+ * the radius that keeps its cube outside the grid. */
+__device__ __forceinline__ void region_of(const Med &m, int x, int y, int z, uint32_t &label, int &r) {
+  if (in_grid(m, x, y)) {
+    const uint32_t q = m.lab16[(uint32_t)x + m.nx * ((uint32_t)y + m.ny * (uint32_t)z)];
+    label = q & 0xffu;
+    r = (int)(q >> 8);
   } else {
-    p.ix = p.iy = p.iz = 0;
-    p.ingrid = 0;
+    const int dx = x < 0 ? -x : x - ((int)m.nx - 1);
+    const int dy = y < 0 ? -y : y - ((int)m.ny - 1);
+    label = 1u;
+    r = min(MCFL_FREE_MAX, max(dx, dy) - 1);
   }
 }
 
@@ -842,18 +862,19 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
        * at every face between different indices with that face's normal,
        * scattering-free voxels are crossed without interaction.  A pass ends
        * at the interaction (PHD tally, weight drop, spin, as the reference's
-       * pass) or at an exit.  Inside the grid a segment goes from the
-       * photon's voxel straight to the face of its free cube (radius xcr of
-       * the label + free-radius map, clipped to the grid; the voxel itself
-       * when 0), or to the interaction inside it, and then across that face;
-       * distances run along the ray from an origin (xo*) — the pass start or
-       * the face where the direction last changed — and a run of voxels of
-       * one label is charged its optical depth once, where the label changes
-       * (xs0: where the run began).  Outside the grid's lateral extent a
-       * segment is one straight line to a slab face or back into the grid.
-       * The pass state (xtau, xo*, xs0, xcr, xit) lives across iterations,
-       * so every lane of a warp runs one segment per iteration, whatever
-       * number of segments its pass needs. ---- */
+       * pass) or at an exit.  A segment goes from the photon's voxel
+       * straight to the face of its free cube (radius xcr of the label +
+       * free-radius map, clipped to the grid; the voxel itself when 0), or
+       * to the interaction inside it, and then across that face; beyond the
+       * grid's lateral extent the slab continues as virtual voxels of label 1
+       * (the reference's medium there), walked by the same code.  Distances
+       * run along the ray from an origin (xo*) — the pass start or the face
+       * where the direction last changed — and a run of voxels of one label
+       * is charged its optical depth once, where the label changes (xs0:
+       * where the run began).  The pass state (xtau, xo*, xs0, xcr, xit)
+       * lives across iterations, so every lane of a warp runs the same
+       * segment code once per iteration, whatever number of segments its
+       * pass needs. ---- */
       if (!xmid) { /* a new pass */
         ++pst;
         xtau = -MCFL_LOGF(r.oc());
@@ -864,189 +885,104 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       const int cap = 16 + 4 * (int)(m.nx + m.ny + m.nz);
       /* 0: the pass goes on, 1: interaction, 2: exit (tallied), 3: lost */
       int outcome = 0;
-      if (p.ingrid) {
-        if (xbegin) {
-          xox = p.x;
-          xoy = p.y;
-          xoz = p.z;
-          xs0 = MCFL_C(0.0);
-          xcr = (int)(m.lab16[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)] >> 8);
-          xbegin = false;
-        }
-        if (++xit > cap) {
-          outcome = 3;
-        } else {
-          const real4 ca = s_lab[2 * p.label];
-          const int cr = xcr;
-          const int lx = max(p.ix - cr, 0), ux = min(p.ix + cr, (int)m.nx - 1);
-          const int ly = max(p.iy - cr, 0), uy = min(p.iy + cr, (int)m.ny - 1);
-          const int lz = max(p.iz - cr, 0), uz = min(p.iz + cr, (int)m.nz - 1);
-          const real cx = plane_dist(face_x(m, p.dx > MCFL_C(0.0) ? ux + 1 : lx), xox, p.dx);
-          const real cy = plane_dist(face_y(m, p.dy > MCFL_C(0.0) ? uy + 1 : ly), xoy, p.dy);
-          const real cz = plane_dist(face_z(m, p.dz > MCFL_C(0.0) ? uz + 1 : lz), xoz, p.dz);
-          real db = cx;
-          int axis = 0;
-          if (cy < db) { db = cy; axis = 1; }
-          if (cz < db) { db = cz; axis = 2; }
-          real sj = db;
-          bool hit = false;
-          if (ca.x != FLT_MAX) {
-            const real s_int = xs0 + xtau * ca.x;
-            if (s_int <= db) {
-              sj = s_int;
-              hit = true;
-            }
+      if (xbegin) {
+        xox = p.x;
+        xoy = p.y;
+        xoz = p.z;
+        xs0 = MCFL_C(0.0);
+        uint32_t here;
+        region_of(m, p.ix, p.iy, p.iz, here, xcr);
+        xbegin = false;
+      }
+      if (++xit > cap) {
+        outcome = 3;
+      } else {
+        const real4 ca = s_lab[2 * p.label];
+        const int cr = xcr;
+        const bool in = in_grid(m, p.ix, p.iy);
+        const int lx = in ? max(p.ix - cr, 0) : p.ix - cr, ux = in ? min(p.ix + cr, (int)m.nx - 1) : p.ix + cr;
+        const int ly = in ? max(p.iy - cr, 0) : p.iy - cr, uy = in ? min(p.iy + cr, (int)m.ny - 1) : p.iy + cr;
+        const int lz = max(p.iz - cr, 0), uz = min(p.iz + cr, (int)m.nz - 1);
+        const real cx = plane_dist(face_x(m, p.dx > MCFL_C(0.0) ? ux + 1 : lx), xox, p.dx);
+        const real cy = plane_dist(face_y(m, p.dy > MCFL_C(0.0) ? uy + 1 : ly), xoy, p.dy);
+        const real cz = plane_dist(face_z(m, p.dz > MCFL_C(0.0) ? uz + 1 : lz), xoz, p.dz);
+        real db = cx;
+        int axis = 0;
+        if (cy < db) { db = cy; axis = 1; }
+        if (cz < db) { db = cz; axis = 2; }
+        real sj = db;
+        bool hit = false;
+        if (ca.x != FLT_MAX) {
+          const real s_int = xs0 + xtau * ca.x;
+          if (s_int <= db) {
+            sj = s_int;
+            hit = true;
           }
-          const real x = xox + p.dx * sj, y = xoy + p.dy * sj, z = xoz + p.dz * sj;
-          /* the voxel there, inside the cube (its last layer along the exit axis) */
-          const int fx = (!hit && axis == 0) ? (p.dx > MCFL_C(0.0) ? ux : lx)
-                                             : min(max((int)MCFL_R2U_RZ((x + m.hx) * m.gx), lx), ux);
-          const int fy = (!hit && axis == 1) ? (p.dy > MCFL_C(0.0) ? uy : ly)
-                                             : min(max((int)MCFL_R2U_RZ((y + m.hy) * m.gy), ly), uy);
-          const int fz = (!hit && axis == 2) ? (p.dz > MCFL_C(0.0) ? uz : lz)
-                                             : min(max((int)MCFL_R2U_RZ(z * m.gz), lz), uz);
-          if (hit) {
-            p.ix = fx;
-            p.iy = fy;
-            p.iz = fz;
+        }
+        const real x = xox + p.dx * sj, y = xoy + p.dy * sj, z = xoz + p.dz * sj;
+        /* the voxel there, inside the cube (its last layer along the exit axis) */
+        const int fx = (!hit && axis == 0) ? (p.dx > MCFL_C(0.0) ? ux : lx)
+                                           : min(max(vfloor((x + m.hx) * m.gx), lx), ux);
+        const int fy = (!hit && axis == 1) ? (p.dy > MCFL_C(0.0) ? uy : ly)
+                                           : min(max(vfloor((y + m.hy) * m.gy), ly), uy);
+        const int fz = (!hit && axis == 2) ? (p.dz > MCFL_C(0.0) ? uz : lz)
+                                           : min(max(vfloor(z * m.gz), lz), uz);
+        if (hit) {
+          p.ix = fx;
+          p.iy = fy;
+          p.iz = fz;
+          p.x = x;
+          p.y = y;
+          p.z = z;
+          outcome = 1;
+        } else {
+          /* the region across the face */
+          int nix = fx, niy = fy, niz = fz;
+          if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
+          else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
+          else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
+          uint32_t next;
+          int nr = 0;
+          if (niz < 0) next = 0u;
+          else if (niz >= (int)m.nz) next = m.last;
+          else region_of(m, nix, niy, niz, next, nr);
+          if (next == p.label) { /* the same label: on, without a stop */
+            p.ix = nix;
+            p.iy = niy;
+            p.iz = niz;
+            xcr = nr;
+          } else {
+            /* the run of this label ends at the face */
+            if (ca.x != FLT_MAX) {
+              xtau -= (db - xs0) / ca.x;
+              if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
+            }
+            xs0 = db;
             p.x = x;
             p.y = y;
             p.z = z;
-            outcome = 1;
-          } else {
-            /* the region across the face */
-            int nix = fx, niy = fy, niz = fz, nin = 1;
-            if (axis == 0) nix += p.dx > MCFL_C(0.0) ? 1 : -1;
-            else if (axis == 1) niy += p.dy > MCFL_C(0.0) ? 1 : -1;
-            else niz += p.dz > MCFL_C(0.0) ? 1 : -1;
-            uint32_t next;
-            int nr = 0;
-            if (niz < 0) next = 0u;
-            else if (niz >= (int)m.nz) next = m.last;
-            else if (nix < 0 || nix >= (int)m.nx || niy < 0 || niy >= (int)m.ny) {
-              next = 1u;
-              nin = 0;
+            const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
+            if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: the face voxel, a new direction */
+              p.ix = fx;
+              p.iy = fy;
+              p.iz = fz;
+              xbegin = true;
             } else {
-              const uint32_t q = m.lab16[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
-              next = q & 0xffu;
-              nr = (int)(q >> 8);
-            }
-            if (next == p.label && nin) { /* the same label: on, without a stop */
+              p.label = next;
               p.ix = nix;
               p.iy = niy;
               p.iz = niz;
-              xcr = nr;
-            } else {
-              /* the run of this label ends at the face */
-              if (ca.x != FLT_MAX) {
-                xtau -= (db - xs0) / ca.x;
-                if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
+              if (next == 0u || next == m.last) {
+                const bool top = next == 0u;
+                tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+                ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+                p.weight = 0u;
+                outcome = 2;
+              } else if (n_here != n_next) {
+                xbegin = true; /* refracted: a new direction */
+              } else {
+                xcr = nr;
               }
-              xs0 = db;
-              p.x = x;
-              p.y = y;
-              p.z = z;
-              bool restart = !nin, reflected = false;
-              if (next != p.label) {
-                const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
-                if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: the face voxel, a new direction */
-                  p.ix = fx;
-                  p.iy = fy;
-                  p.iz = fz;
-                  reflected = true;
-                  xbegin = true;
-                } else if (n_here != n_next) {
-                  restart = true; /* refracted: a new direction */
-                }
-              }
-              if (!reflected) {
-                p.label = next;
-                p.ix = nix;
-                p.iy = niy;
-                p.iz = niz;
-                p.ingrid = nin;
-                if (next == 0u || next == m.last) {
-                  const bool top = next == 0u;
-                  tally_exit(J, p.x, p.y, p.weight, top, src_idx);
-                  ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
-                  p.weight = 0u;
-                  outcome = 2;
-                } else if (restart) {
-                  xbegin = true;
-                } else {
-                  xcr = nr;
-                }
-              }
-            }
-          }
-        }
-      } else if (++xit > cap) {
-        outcome = 3;
-      } else {
-        /* outside the grid's lateral extent: one straight segment */
-        const real4 ca = s_lab[2 * p.label];
-        real db = plane_dist(p.dz > MCFL_C(0.0) ? m.esp : MCFL_C(0.0), p.z, p.dz);
-        int axis = 2;
-        real t;
-        /* re-entry through a lateral face of the grid */
-        if ((p.x <= -m.hx && p.dx > MCFL_C(0.0)) || (p.x >= m.hx && p.dx < MCFL_C(0.0))) {
-          t = plane_dist(p.dx > MCFL_C(0.0) ? -m.hx : m.hx, p.x, p.dx);
-          const real yc = p.y + p.dy * t;
-          if (t < db && MCFL_FABS(yc) < m.hy) { db = t; axis = 0; }
-        }
-        if ((p.y <= -m.hy && p.dy > MCFL_C(0.0)) || (p.y >= m.hy && p.dy < MCFL_C(0.0))) {
-          t = plane_dist(p.dy > MCFL_C(0.0) ? -m.hy : m.hy, p.y, p.dy);
-          const real xc = p.x + p.dx * t;
-          if (t < db && MCFL_FABS(xc) < m.hx) { db = t; axis = 1; }
-        }
-        bool hit = false;
-        if (ca.x != FLT_MAX) {
-          const real s_int = xtau * ca.x;
-          if (s_int <= db) {
-            p.x += p.dx * s_int;
-            p.y += p.dy * s_int;
-            p.z += p.dz * s_int;
-            hit = true;
-            outcome = 1;
-          }
-        }
-        if (!hit && db == FLT_MAX) { /* scattering-free with no face ahead */
-          outcome = 3;
-        } else if (!hit) {
-          p.x += p.dx * db;
-          p.y += p.dy * db;
-          p.z += p.dz * db;
-          if (ca.x != FLT_MAX) {
-            xtau -= db / ca.x;
-            if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
-          }
-          xbegin = true;
-          int nix = p.ix, niy = p.iy, niz = p.iz;
-          uint32_t next;
-          if (axis == 2) {
-            next = p.dz > MCFL_C(0.0) ? m.last : 0u;
-          } else {
-            nix = axis == 0 ? (p.dx > MCFL_C(0.0) ? 0 : (int)m.nx - 1)
-                            : (int)min(MCFL_R2U_RZ((p.x + m.hx) * m.gx), m.nx - 1u);
-            niy = axis == 1 ? (p.dy > MCFL_C(0.0) ? 0 : (int)m.ny - 1)
-                            : (int)min(MCFL_R2U_RZ((p.y + m.hy) * m.gy), m.ny - 1u);
-            niz = (int)min(MCFL_R2U_RZ(p.z * m.gz), m.nz - 1u);
-            next = (uint32_t)m.labels[(uint32_t)nix + m.nx * ((uint32_t)niy + m.ny * (uint32_t)niz)];
-          }
-          if (next == p.label || refract_axis(p, axis, s_lab[2 * p.label + 1].w, s_lab[2 * next + 1].w, r)) {
-            p.label = next;
-            if (axis != 2) {
-              p.ix = nix;
-              p.iy = niy;
-              p.iz = niz;
-              p.ingrid = 1;
-            }
-            if (next == 0u || next == m.last) {
-              const bool top = next == 0u;
-              tally_exit(J, p.x, p.y, p.weight, top, src_idx);
-              ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
-              p.weight = 0u;
-              outcome = 2;
             }
           }
         }
@@ -1054,7 +990,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       if (outcome == 0) continue; /* the pass goes on in the next iteration */
       xmid = false;
       if (outcome == 1) {
-        if (m.fhd && p.ingrid)
+        if (m.fhd && in_grid(m, p.ix, p.iy))
           atomicAdd(&m.fhd[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)],
                     (unsigned long long)p.weight);
         const Rec c2 = Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]};

@@ -614,16 +614,37 @@ unsigned step_layers(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
 
 /* ------------------------- voxel-boundary stepping ------------------------ */
 
-/* The photon's voxel from its position (voxel-boundary stepping). */
+/* Largest free radius kept (the engine keeps the same). */
+#define ORACLE_FREE_MAX 31
+
+/* Voxel-boundary stepping: voxel (x, y) lies in the grid's lateral extent. */
+inline bool in_grid(const Phase &ph, int x, int y) {
+  return x >= 0 && x < (int)ph.num_x && y >= 0 && y < (int)ph.num_y;
+}
+
+/* The photon's voxel from its position, for voxel-boundary stepping: beyond
+ * the grid's lateral extent the slab continues as virtual voxels of label 1
+ * (the reference's medium there), so the lateral indices are any integers. */
 inline void locate(Photon &p, const Phase &ph) {
-  if (fabsf(p.x) < ph.hx && fabsf(p.y) < ph.hy) {
-    p.ix = (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
-    p.iy = (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
-    p.iz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
-    p.ingrid = 1;
+  p.ix = (int)floorf((p.x + ph.hx) * ph.gx);
+  p.iy = (int)floorf((p.y + ph.hy) * ph.gy);
+  p.iz = std::min(std::max((int)floorf(p.z * ph.gz), 0), (int)ph.num_z - 1);
+  p.ingrid = in_grid(ph, p.ix, p.iy) ? 1 : 0;
+}
+
+/* Label and free radius of voxel (x, y, z), z inside the slab: the grid's
+ * map, or beyond the grid's lateral extent label 1 with the radius that keeps
+ * its cube outside the grid. */
+inline void region_of(const Phase &ph, int x, int y, int z, uint32_t &label, int &r) {
+  if (in_grid(ph, x, y)) {
+    const size_t q = (size_t)x + ph.num_x * ((size_t)y + ph.num_y * (size_t)z);
+    label = (uint32_t)(unsigned short)ph.labels[q];
+    r = ph.free_r[q];
   } else {
-    p.ix = p.iy = p.iz = 0;
-    p.ingrid = 0;
+    const int dx = x < 0 ? -x : x - ((int)ph.num_x - 1);
+    const int dy = y < 0 ? -y : y - ((int)ph.num_y - 1);
+    label = 1;
+    r = std::min(ORACLE_FREE_MAX, std::max(dx, dy) - 1);
   }
 }
 
@@ -709,197 +730,120 @@ inline void exact_exit(Photon &p, const Phase &ph, Sink &sk, bool top) {
  * the grid within the free radius carries the same label; the voxel itself
  * when the radius is 0), or to the interaction inside it, and then across
  * that face; a run of voxels of one label is charged its optical depth once,
- * where the label changes (s0: where the run began).  Outside the grid's
- * lateral extent (the medium of label 1) each region is one straight
- * segment to a slab face or back into the grid. */
+ * where the label changes (s0: where the run began).  Beyond the grid's
+ * lateral extent the slab continues as virtual voxels of label 1 (the
+ * reference's medium there, CUDAMCFLtransport.cu:331), walked the same way. */
 template <class M>
 unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
   const uint32_t last = ph.last_bulk;
   sk.steps++;
   float tau = -M::log(r.oc());
   const int cap = 16 + 4 * (int)(ph.num_x + ph.num_y + ph.num_z);
+  const int nx = (int)ph.num_x, ny = (int)ph.num_y, nz = (int)ph.num_z;
   int it = 0;
   for (;;) {
-    if (p.ingrid) {
-      /* one segment per iteration: from the photon's voxel straight to the
-       * face of its free cube (radius cr, clipped to the grid; the voxel
-       * itself when cr = 0), or to the interaction inside it; then across
-       * that face */
-      const float ox = p.x, oy = p.y, oz = p.z;
-      float s0 = 0.0f;
-      int cr = ph.free_r[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)];
-      for (;;) {
-        if (++it > cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
-          sk.w0_loss += p.weight;
-          p.weight = 0u;
-          return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+    /* one segment per iteration: from the photon's voxel straight to the
+     * face of its free cube (radius cr, clipped to the grid for a voxel of
+     * the grid; the voxel itself when cr = 0), or to the interaction inside
+     * it; then across that face */
+    const float ox = p.x, oy = p.y, oz = p.z;
+    float s0 = 0.0f;
+    uint32_t here; /* the photon's label, p.bulkpos */
+    int cr;
+    region_of(ph, p.ix, p.iy, p.iz, here, cr);
+    (void)here;
+    for (;;) {
+      if (++it > cap) { /* a photon that cannot reach an interaction (e.g. glass all around) */
+        sk.w0_loss += p.weight;
+        p.weight = 0u;
+        return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
+      }
+      const Prop &pr = ph.prop[p.bulkpos];
+      const bool in = in_grid(ph, p.ix, p.iy);
+      const int lx = in ? std::max(p.ix - cr, 0) : p.ix - cr, ux = in ? std::min(p.ix + cr, nx - 1) : p.ix + cr;
+      const int ly = in ? std::max(p.iy - cr, 0) : p.iy - cr, uy = in ? std::min(p.iy + cr, ny - 1) : p.iy + cr;
+      const int lz = std::max(p.iz - cr, 0), uz = std::min(p.iz + cr, nz - 1);
+      const float cx = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? ux + 1 : lx), ox, p.dx);
+      const float cy = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? uy + 1 : ly), oy, p.dy);
+      const float cz = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? uz + 1 : lz), oz, p.dz);
+      float db = cx;
+      int axis = 0;
+      if (cy < db) { db = cy; axis = 1; }
+      if (cz < db) { db = cz; axis = 2; }
+      float sj = db;
+      bool hit = false;
+      if (pr.mutr != FLT_MAX) {
+        const float s_int = s0 + tau * pr.mutr;
+        if (s_int <= db) {
+          sj = s_int;
+          hit = true;
         }
-        const Prop &pr = ph.prop[p.bulkpos];
-        const int lx = std::max(p.ix - cr, 0), ux = std::min(p.ix + cr, (int)ph.num_x - 1);
-        const int ly = std::max(p.iy - cr, 0), uy = std::min(p.iy + cr, (int)ph.num_y - 1);
-        const int lz = std::max(p.iz - cr, 0), uz = std::min(p.iz + cr, (int)ph.num_z - 1);
-        const float cx = plane_dist(face_coord(ph, 0, p.dx > 0.0f ? ux + 1 : lx), ox, p.dx);
-        const float cy = plane_dist(face_coord(ph, 1, p.dy > 0.0f ? uy + 1 : ly), oy, p.dy);
-        const float cz = plane_dist(face_coord(ph, 2, p.dz > 0.0f ? uz + 1 : lz), oz, p.dz);
-        float db = cx;
-        int axis = 0;
-        if (cy < db) { db = cy; axis = 1; }
-        if (cz < db) { db = cz; axis = 2; }
-        float sj = db;
-        bool hit = false;
-        if (pr.mutr != FLT_MAX) {
-          const float s_int = s0 + tau * pr.mutr;
-          if (s_int <= db) {
-            sj = s_int;
-            hit = true;
-          }
-        }
-        const float x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
-        /* the voxel there, inside the cube (its last layer along the exit axis) */
-        const int fx = (!hit && axis == 0) ? (p.dx > 0.0f ? ux : lx)
-                                           : std::min(std::max((int)mcfl_f2u_rz((x + ph.hx) * ph.gx), lx), ux);
-        const int fy = (!hit && axis == 1) ? (p.dy > 0.0f ? uy : ly)
-                                           : std::min(std::max((int)mcfl_f2u_rz((y + ph.hy) * ph.gy), ly), uy);
-        const int fz = (!hit && axis == 2) ? (p.dz > 0.0f ? uz : lz)
-                                           : std::min(std::max((int)mcfl_f2u_rz(z * ph.gz), lz), uz);
-        if (hit) {
-          p.ix = fx;
-          p.iy = fy;
-          p.iz = fz;
-          p.x = x;
-          p.y = y;
-          p.z = z;
-          goto interaction;
-        }
-        /* the region across the face */
-        int nix = fx, niy = fy, niz = fz, nin = 1;
-        if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
-        else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
-        else niz += p.dz > 0.0f ? 1 : -1;
-        uint32_t next;
-        int nr = 0;
-        if (niz < 0) next = 0;
-        else if (niz >= (int)ph.num_z) next = last;
-        else if (nix < 0 || nix >= (int)ph.num_x || niy < 0 || niy >= (int)ph.num_y) {
-          next = 1;
-          nin = 0;
-        } else {
-          const size_t q = (size_t)nix + ph.num_x * ((size_t)niy + ph.num_y * (size_t)niz);
-          next = (uint32_t)(unsigned short)ph.labels[q];
-          nr = ph.free_r[q];
-        }
-        if (next == p.bulkpos && nin) { /* the same label: on, without a stop */
-          p.ix = nix;
-          p.iy = niy;
-          p.iz = niz;
-          cr = nr;
-          continue;
-        }
-        /* the run of this label ends at the face */
-        if (pr.mutr != FLT_MAX) {
-          tau -= (db - s0) / pr.mutr;
-          if (tau < 0.0f) tau = 0.0f;
-        }
-        s0 = db;
+      }
+      const float x = ox + p.dx * sj, y = oy + p.dy * sj, z = oz + p.dz * sj;
+      /* the voxel there, inside the cube (its last layer along the exit axis) */
+      const int fx = (!hit && axis == 0) ? (p.dx > 0.0f ? ux : lx)
+                                         : std::min(std::max((int)floorf((x + ph.hx) * ph.gx), lx), ux);
+      const int fy = (!hit && axis == 1) ? (p.dy > 0.0f ? uy : ly)
+                                         : std::min(std::max((int)floorf((y + ph.hy) * ph.gy), ly), uy);
+      const int fz = (!hit && axis == 2) ? (p.dz > 0.0f ? uz : lz)
+                                         : std::min(std::max((int)floorf(z * ph.gz), lz), uz);
+      if (hit) {
+        p.ix = fx;
+        p.iy = fy;
+        p.iz = fz;
         p.x = x;
         p.y = y;
         p.z = z;
-        bool restart = !nin;
-        if (next != p.bulkpos) {
-          const float n_next = ph.prop[next].n;
-          if (!refract_axis(p, axis, pr.n, n_next, r)) { /* reflected: the face voxel, a new direction */
-            p.ix = fx;
-            p.iy = fy;
-            p.iz = fz;
-            break;
-          }
-          if (pr.n != n_next) restart = true; /* refracted: a new direction */
-        }
-        p.bulkpos = next;
-        p.ix = nix;
-        p.iy = niy;
-        p.iz = niz;
-        p.ingrid = nin;
-        if (next == 0 || next == last) {
-          exact_exit(p, ph, sk, next == 0);
-          return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
-        }
-        if (restart) break;
-        cr = nr;
-      }
-      continue;
-    }
-    /* outside the grid's lateral extent: one straight segment */
-    if (++it > cap) {
-      sk.w0_loss += p.weight;
-      p.weight = 0u;
-      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
-    }
-    const Prop &pr = ph.prop[p.bulkpos];
-    float db = plane_dist(p.dz > 0.0f ? ph.esp : 0.0f, p.z, p.dz);
-    int axis = 2;
-    float tt;
-    /* re-entry through a lateral face of the grid */
-    if ((p.x <= -ph.hx && p.dx > 0.0f) || (p.x >= ph.hx && p.dx < 0.0f)) {
-      tt = plane_dist(p.dx > 0.0f ? -ph.hx : ph.hx, p.x, p.dx);
-      const float yc = p.y + p.dy * tt;
-      if (tt < db && fabsf(yc) < ph.hy) { db = tt; axis = 0; }
-    }
-    if ((p.y <= -ph.hy && p.dy > 0.0f) || (p.y >= ph.hy && p.dy < 0.0f)) {
-      tt = plane_dist(p.dy > 0.0f ? -ph.hy : ph.hy, p.y, p.dy);
-      const float xc = p.x + p.dx * tt;
-      if (tt < db && fabsf(xc) < ph.hx) { db = tt; axis = 1; }
-    }
-    if (pr.mutr != FLT_MAX) {
-      const float s_int = tau * pr.mutr;
-      if (s_int <= db) {
-        p.x += p.dx * s_int;
-        p.y += p.dy * s_int;
-        p.z += p.dz * s_int;
         goto interaction;
       }
-    }
-    if (db == FLT_MAX) { /* a scattering-free region with no face ahead */
-      sk.w0_loss += p.weight;
-      p.weight = 0u;
-      return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
-    }
-    p.x += p.dx * db;
-    p.y += p.dy * db;
-    p.z += p.dz * db;
-    if (pr.mutr != FLT_MAX) {
-      tau -= db / pr.mutr;
-      if (tau < 0.0f) tau = 0.0f;
-    }
-    {
-      int nix = p.ix, niy = p.iy, niz = p.iz;
+      /* the region across the face */
+      int nix = fx, niy = fy, niz = fz;
+      if (axis == 0) nix += p.dx > 0.0f ? 1 : -1;
+      else if (axis == 1) niy += p.dy > 0.0f ? 1 : -1;
+      else niz += p.dz > 0.0f ? 1 : -1;
       uint32_t next;
-      if (axis == 2) {
-        next = p.dz > 0.0f ? last : 0;
-      } else {
-        nix = axis == 0 ? (p.dx > 0.0f ? 0 : (int)ph.num_x - 1)
-                        : (int)std::min<unsigned>(mcfl_f2u_rz((p.x + ph.hx) * ph.gx), ph.num_x - 1);
-        niy = axis == 1 ? (p.dy > 0.0f ? 0 : (int)ph.num_y - 1)
-                        : (int)std::min<unsigned>(mcfl_f2u_rz((p.y + ph.hy) * ph.gy), ph.num_y - 1);
-        niz = (int)std::min<unsigned>(mcfl_f2u_rz(p.z * ph.gz), ph.num_z - 1);
-        next = (uint32_t)(unsigned short)ph.labels[nix + ph.num_x * (niy + ph.num_y * niz)];
-      }
-      if (next != p.bulkpos && !refract_axis(p, axis, pr.n, ph.prop[next].n, r)) continue; /* reflected */
-      p.bulkpos = next;
-      if (axis != 2) {
+      int nr = 0;
+      if (niz < 0) next = 0;
+      else if (niz >= nz) next = last;
+      else region_of(ph, nix, niy, niz, next, nr);
+      if (next == p.bulkpos) { /* the same label: on, without a stop */
         p.ix = nix;
         p.iy = niy;
         p.iz = niz;
-        p.ingrid = 1;
+        cr = nr;
+        continue;
       }
+      /* the run of this label ends at the face */
+      if (pr.mutr != FLT_MAX) {
+        tau -= (db - s0) / pr.mutr;
+        if (tau < 0.0f) tau = 0.0f;
+      }
+      s0 = db;
+      p.x = x;
+      p.y = y;
+      p.z = z;
+      const float n_next = ph.prop[next].n;
+      if (!refract_axis(p, axis, pr.n, n_next, r)) { /* reflected: the face voxel, a new direction */
+        p.ix = fx;
+        p.iy = fy;
+        p.iz = fz;
+        break;
+      }
+      const bool bent = pr.n != n_next; /* refracted: a new direction */
+      p.bulkpos = next;
+      p.ix = nix;
+      p.iy = niy;
+      p.iz = niz;
       if (next == 0 || next == last) {
         exact_exit(p, ph, sk, next == 0);
         return photon_survive(p, r, &sk.r_gain, &sk.r_loss);
       }
+      if (bent) break;
+      cr = nr;
     }
   }
 interaction:
-  if (ph.fhd_on == 1 && p.ingrid)
+  if (ph.fhd_on == 1 && in_grid(ph, p.ix, p.iy))
     add_guarded(&sk.fhd[p.ix + ph.num_x * (p.iy + ph.num_y * p.iz)], p.weight, ph.guard);
   const Prop &pi = ph.prop[p.bulkpos];
   uint32_t w = mcfl_f2u_ru(pi.mua * pi.mutr * mcfl_u2f_rn(p.weight));
@@ -922,8 +866,6 @@ inline unsigned step_any(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
 
 /* ------------------------------------------------------------------------ */
 
-/* Largest free radius kept (the engine keeps the same). */
-#define ORACLE_FREE_MAX 31
 
 /* Free radius of every voxel, for voxel-boundary stepping: the largest
  * r <= ORACLE_FREE_MAX such that every voxel of the grid within Chebyshev

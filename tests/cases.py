@@ -202,6 +202,20 @@ def blocks(photons=40000, per_voxel=2000) -> Case:
                 1.0, photons, per_voxel, (0.05, 0.05, 60, 60, 0.0, 0.0))
 
 
+def sparse(photons=40000, per_voxel=2000) -> Case:
+    """A weakly scattering slab (mean free path 2 mm, 0.5 cm thick) on a grid
+    of 8 x 8 x 2 voxels of 0.25 cm: photons leave the grid's lateral extent
+    often, so voxel-boundary stepping walks the medium of label 1 beyond it,
+    and come back through its lateral faces into a block of another index."""
+    lab = _labels(0.5, 4)
+    lab[1, 2:6, 2:6] = 2
+    lab[0, 3:5, 0:2] = 3
+    return Case("sparse", 0.5, 4, lab,
+                [(1.4, 0.2, 5.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.5, 0.2, 5.0, 1.0, 0.5, 0.2, 0.1, 0.8),
+                 (1.3, 0.5, 8.0, 0.0, 0.0, 0.0, 0.0, 0.7)],
+                1.0, photons, per_voxel, (0.1, 0.1, 30, 30, 0.0, 0.0))
+
+
 def timed(photons=40000, per_voxel=40000, face=0, base=None) -> Case:
     """mismatch (or another case) with a 3 x 2 array of time-resolved
     detectors, discs of 0.15 cm 0.25 cm apart, on the entry (face 0) or exit
@@ -345,4 +359,4 @@ LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}
 
 # voxel-boundary stepping (no time-resolved detectors on this path)
 EXACT = {n + "_exact": exact(f) for n, f in {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere,
-                                              "deep": deep, "blocks": blocks}.items()}
+                                              "deep": deep, "blocks": blocks, "sparse": sparse}.items()}

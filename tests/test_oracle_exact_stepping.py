@@ -21,18 +21,20 @@ B = 16
 N = 20000
 
 
-def _slab_sim(layers, n_out, photons, exact):
+def _slab_sim(layers, n_out, photons, exact, lateral=(8, 0.1, 40.0)):
+    """lateral: voxels across, voxels per cm and half extent of the grid."""
     from oracle import pyoracle
     nz = [int(round(l[0] * 100)) for l in layers]
-    lab = np.ones((sum(nz), 8, 8), np.uint8)
+    nl, gl, half = lateral
+    lab = np.ones((sum(nz), nl, nl), np.uint8)
     z0 = 0
     for i, k in enumerate(nz):
         lab[z0:z0 + k] = i + 1
         z0 += k
     bulks = [mc.outer_bulk(n_out)] + [mc.bulk_from_mci_columns(l[4], l[1], l[2], g=l[3]) for l in layers] + \
         [mc.outer_bulk(n_out)]
-    sim = pyoracle.sim_from_arrays(lab, bulks, half_x=40.0, half_y=40.0, thickness=sum(nz) / 100.0,
-                                   vox_per_cm=[0.1, 0.1, 100.0], photons=photons, per_voxel=0,
+    sim = pyoracle.sim_from_arrays(lab, bulks, half_x=half, half_y=half, thickness=sum(nz) / 100.0,
+                                   vox_per_cm=[gl, gl, 100.0], photons=photons, per_voxel=0,
                                    det=(0.1, 0.1, 10, 10, 0.0, 0.0), do_fl=0)
     sim.exact_stepping = exact
     return sim
@@ -71,3 +73,15 @@ def test_reference_stepping_is_biased_on_index_steps_and_agrees_without_them(ora
     rc1 = np.array([_fractions(oracle, table32768, _slab_sim(one, 1.0, N, 0), 600 + b) for b in range(B)])
     for i in range(3):
         stats.scalar_gate(ex1[:, i], rc1[:, i])
+
+
+def test_exact_stepping_beyond_a_narrow_grid_matches_independent_slab_mc(oracle, table32768):
+    """A one-label slab whose voxel grid covers only 0.2 x 0.2 cm: photons
+    spend most passes beyond the grid's lateral extent, where the medium of
+    label 1 continues, so the slab is still homogeneous and infinite."""
+    layers = [(0.1, 0.5, 20.0, 0.8, 1.4)]
+    sim = lambda: _slab_sim(layers, 1.0, N, 1, lateral=(4, 20.0, 0.1))
+    port = np.array([_fractions(oracle, table32768, sim(), 800 + 13 * b) for b in range(B)])
+    ref = np.array([slab_mc.run(layers, 1.0, 1.0, N, 9500 + b) for b in range(B)])
+    for i in range(3):
+        stats.scalar_gate(port[:, i], ref[:, i])

@@ -138,9 +138,9 @@ struct Photon {
   real x, y, z, dx, dy, dz;
   uint32_t weight, label;
   uint64_t tof; /* time of flight [fs], time-of-flight kernels only */
-  /* voxel-boundary stepping only: the photon's voxel, or ingrid = 0 outside
-   * the grid's lateral extent (the medium of label 1) */
-  int ix, iy, iz, ingrid;
+  /* voxel-boundary stepping only: the photon's voxel (lateral indices beyond
+   * the grid name virtual voxels of label 1) */
+  int ix, iy, iz;
 };
 
 /* Time-of-flight increment (unsigned long)(v / c) of a path of optical
@@ -261,7 +261,6 @@ __device__ __forceinline__ void locate(Photon &p, const Med &m) {
   p.ix = vfloor((p.x + m.hx) * m.gx);
   p.iy = vfloor((p.y + m.hy) * m.gy);
   p.iz = min(max(vfloor(p.z * m.gz), 0), (int)m.nz - 1);
-  p.ingrid = in_grid(m, p.ix, p.iy) ? 1 : 0;
 }
 
 /* Label and free radius of voxel (x, y, z), z inside the slab: the grid's
@@ -345,7 +344,6 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
       p.ix = (int)(v % m.nx);
       p.iy = (int)((v / m.nx) % m.ny);
       p.iz = (int)(v / (m.nx * m.ny));
-      p.ingrid = 1;
     } else {
       locate(p, m);
     }

@@ -112,9 +112,9 @@ struct Photon {
   uint32_t weight;
   uint32_t bulkpos;
   uint64_t tof; /* time of flight [fs] */
-  /* voxel-boundary stepping: the photon's voxel, or ingrid = 0 outside the
-   * grid's lateral extent (the medium of label 1) */
-  int ix, iy, iz, ingrid;
+  /* voxel-boundary stepping: the photon's voxel (lateral indices beyond the
+   * grid name virtual voxels of label 1) */
+  int ix, iy, iz;
 };
 
 /* Everything one transport phase reads (the reference's __constant__ set). */
@@ -629,7 +629,6 @@ inline void locate(Photon &p, const Phase &ph) {
   p.ix = (int)floorf((p.x + ph.hx) * ph.gx);
   p.iy = (int)floorf((p.y + ph.hy) * ph.gy);
   p.iz = std::min(std::max((int)floorf(p.z * ph.gz), 0), (int)ph.num_z - 1);
-  p.ingrid = in_grid(ph, p.ix, p.iy) ? 1 : 0;
 }
 
 /* Label and free radius of voxel (x, y, z), z inside the slab: the grid's
@@ -1207,7 +1206,6 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
       p.ix = (int)ix;
       p.iy = (int)iy;
       p.iz = (int)iz;
-      p.ingrid = 1;
     } else {
       launch_photon<M, true>(p, r, ph, ph.xi, ph.yi, ph.zi);
       locate(p, ph);

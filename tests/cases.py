@@ -216,6 +216,15 @@ def sparse(photons=40000, per_voxel=2000) -> Case:
                 1.0, photons, per_voxel, (0.1, 0.1, 30, 30, 0.0, 0.0))
 
 
+def sparse_offset(photons=40000, per_voxel=2000) -> Case:
+    """sparse with the beam 0.5 cm beyond the grid's lateral extent: every
+    photon starts in the medium of label 1 outside the grid."""
+    c = sparse(photons, per_voxel)
+    c.name = "sparse_offset"
+    c.source = (1.5, 0.25, 0.0)
+    return c
+
+
 def timed(photons=40000, per_voxel=40000, face=0, base=None) -> Case:
     """mismatch (or another case) with a 3 x 2 array of time-resolved
     detectors, discs of 0.15 cm 0.25 cm apart, on the entry (face 0) or exit
@@ -359,4 +368,5 @@ LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}
 
 # voxel-boundary stepping (no time-resolved detectors on this path)
 EXACT = {n + "_exact": exact(f) for n, f in {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere,
-                                              "deep": deep, "blocks": blocks, "sparse": sparse}.items()}
+                                              "deep": deep, "blocks": blocks, "sparse": sparse,
+                                              "sparse_offset": sparse_offset}.items()}

@@ -75,7 +75,7 @@ int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool 
   *bps = 0;
   *regs = 0;
   const int mixed = mixed_variant == 1 ? -3 : mixed_variant == 2 ? -4 : -1;
-  const int v = exact ? 6 : uniform ? (time ? 3 : variant_code()) : (time ? -2 : mixed);
+  const int v = exact ? (time ? 10 : 6) : uniform ? (time ? 3 : variant_code()) : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 

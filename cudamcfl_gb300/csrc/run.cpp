@@ -120,7 +120,6 @@ int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run)
   }
   if (run->exact_stepping) {
     if (m->layered) return fail(MCFL_E_ARG, "exact stepping: voxelized media only");
-    if (td.nx != 0) return fail(MCFL_E_ARG, "exact stepping: no time-resolved detectors");
   }
   if (m->layered) {
     if (run->photons_per_voxel) return fail(MCFL_E_ARG, "layered medium: excitation runs only");
@@ -365,7 +364,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   const bool exact = run->exact_stepping != 0;
   int block = 0, block_exc = 0;
   const int grid = c->grid_for(true, &block, nullptr, false, exact);
-  const int grid_exc = timed ? c->grid_for(true, &block_exc, nullptr, true) : grid;
+  const int grid_exc = timed ? c->grid_for(true, &block_exc, nullptr, true, exact) : grid;
   if (!timed) block_exc = block;
   const unsigned long long photons = run->photons;
   const unsigned per_voxel = run->photons_per_voxel;

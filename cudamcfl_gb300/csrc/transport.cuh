@@ -932,6 +932,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.x = x;
           p.y = y;
           p.z = z;
+          if (kTime) p.tof += tof_fs((sj - xs0) * s_lab[2 * p.label + 1].w); /* the run's optical path */
           outcome = 1;
         } else {
           /* the region across the face */
@@ -951,15 +952,16 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             xcr = nr;
           } else {
             /* the run of this label ends at the face */
+            const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
             if (ca.x != FLT_MAX) {
               xtau -= (db - xs0) / ca.x;
               if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
             }
+            if (kTime) p.tof += tof_fs((db - xs0) * n_here);
             xs0 = db;
             p.x = x;
             p.y = y;
             p.z = z;
-            const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
             if (!refract_axis(p, axis, n_here, n_next, r)) { /* reflected: the face voxel, a new direction */
               p.ix = fx;
               p.iy = fy;
@@ -973,6 +975,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               if (next == 0u || next == m.last) {
                 const bool top = next == 0u;
                 tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+                if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
                 ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
                 p.weight = 0u;
                 outcome = 2;
@@ -1199,7 +1202,8 @@ static size_t smem_bytes(int block, bool uniform) {
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner, and 7, 8, 9 the same
  * with the photon-hitting-density sums held in a register; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
- * of flight; voxel-boundary stepping 6 = 256 x 4.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
+ * of flight; voxel-boundary stepping 6 = 256 x 4, 10 = 256 x 3 with the time
+ * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
  * -2 = 256 x 2 with the time of flight. */
 typedef void (*TransportKernel)(McflLaunch);
 
@@ -1222,6 +1226,7 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case 7: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, true>;
   case 8: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, true>;
   case 9: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, true>;
+  case 10: *threads = 256; return MCFL_KERNEL_NAME<true, true, 2, 256, 3>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -1239,7 +1244,7 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
   if (L->max_iters && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
   if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
     return cudaErrorInvalidValue;
-  const int v = L->exact_step ? 6
+  const int v = L->exact_step ? (L->time_on ? 10 : 6)
                 : L->med.layered ? (L->time_on ? 5 : 4)
                 : L->uniform_medium ? (L->time_on ? 3 : (int)L->variant)
                 : L->time_on        ? -2

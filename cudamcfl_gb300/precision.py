@@ -20,7 +20,8 @@ with signal and the share of them beyond 3 paired standard errors.
 
 runs the large precision-study medium (media.config5: 512 x 512 x 256
 voxels, mu_s' = 20/cm, wide-field source); --small uses its quarter
-resolution variant.
+resolution variant, --exact-stepping runs every build with voxel-boundary
+stepping.
 """
 from __future__ import annotations
 
@@ -151,6 +152,7 @@ def main(argv=None) -> int:
     ap.add_argument("--small", action="store_true", help="the 128 x 128 x 64 variant at 0.04 cm")
     ap.add_argument("--modes", default="fast,exact,f64")
     ap.add_argument("--no-fluence", action="store_true")
+    ap.add_argument("--exact-stepping", action="store_true", help="voxel-boundary stepping in every build")
     args = ap.parse_args(argv)
     m = media_mod.config5(shape=(64, 128, 128), voxel=0.04) if args.small else media_mod.config5()
     ctx = Context(device=0)
@@ -160,7 +162,7 @@ def main(argv=None) -> int:
 
     def rd_for_seed(seed):
         return run_desc(per_batch, det=m.det, fluence=0 if args.no_fluence else 1, seed_exc=seed, seed_fl=seed + 1,
-                        kind=SOURCE_WIDEFIELD, width=w, height=h)
+                        kind=SOURCE_WIDEFIELD, width=w, height=h, exact_stepping=1 if args.exact_stepping else 0)
 
     # full size: the fluence compared on 4^3-voxel cells (128 x 128 x 64)
     res = study(ctx, med, rd_for_seed, args.batches, tuple(args.modes.split(",")), fluence=not args.no_fluence,
@@ -169,7 +171,8 @@ def main(argv=None) -> int:
     s["workload"] = {"medium": "config5" + (" quarter resolution" if args.small else ""),
                      "shape_zyx": list(m.labels.shape), "voxel_cm": m.voxel_cm[0], "photons_per_build": per_batch *
                      args.batches, "batches": args.batches, "source": f"wide-field {w:.2f} x {h:.2f} cm",
-                     "fluence_cells": "voxels" if args.small else "4x4x4-voxel cells"}
+                     "fluence_cells": "voxels" if args.small else "4x4x4-voxel cells",
+                     "stepping": "voxel boundary" if args.exact_stepping else "the reference's"}
     print(json.dumps(s), flush=True)
     med.free()
     ctx.close()

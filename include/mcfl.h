@@ -285,8 +285,8 @@ typedef struct mcfl_run_desc {
    * 0: the reference's stepping (the whole pass with the start voxel's mu_t,
    * the label looked up at the end point, z as the Fresnel normal;
    * CUDAMCFLtransport.cu:280-352).  Voxelized media; mcfl_run (excitation
-   * and emission) and mcfl_batch_run over one medium; not with time-resolved
-   * detectors, and not through the server or the allocation-free entry. */
+   * and emission, time-resolved detectors included) and mcfl_batch_run over
+   * one medium; not through the server or the allocation-free entry. */
   int exact_stepping;
 } mcfl_run_desc;
 

@@ -712,6 +712,7 @@ inline void exact_exit(Photon &p, const Phase &ph, Sink &sk, bool top) {
       else add_guarded(&sk.Tt[idx], p.weight, ph.guard);
     }
   }
+  if (ph.time_on && ph.tdet_face == (top ? 0 : 1)) tally_time(ph, p, sk);
   (top ? sk.exit_top : sk.exit_bottom) += p.weight;
   p.weight = 0u;
 }
@@ -793,6 +794,7 @@ unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
         p.x = x;
         p.y = y;
         p.z = z;
+        p.tof += tof_u64((double)((sj - s0) * pr.n) / kCcmfs, ph.tof_wrap); /* the run's optical path */
         goto interaction;
       }
       /* the region across the face */
@@ -817,6 +819,7 @@ unsigned step_exact(Photon &p, Rng &r, const Phase &ph, Sink &sk) {
         tau -= (db - s0) / pr.mutr;
         if (tau < 0.0f) tau = 0.0f;
       }
+      p.tof += tof_u64((double)((db - s0) * pr.n) / kCcmfs, ph.tof_wrap);
       s0 = db;
       p.x = x;
       p.y = y;

@@ -366,7 +366,8 @@ def layered_timed_exit(photons=40000, per_voxel=40000) -> LayeredCase:
 
 LAYERED = {"layered": layered, "layered_timed_exit": layered_timed_exit}
 
-# voxel-boundary stepping (no time-resolved detectors on this path)
+# voxel-boundary stepping
 EXACT = {n + "_exact": exact(f) for n, f in {"tiny": tiny, "mismatch": mismatch, "glass": glass, "sphere": sphere,
                                               "deep": deep, "blocks": blocks, "sparse": sparse,
-                                              "sparse_offset": sparse_offset}.items()}
+                                              "sparse_offset": sparse_offset, "mismatch_timed": mismatch_timed,
+                                              "glass_timed_exit": glass_timed_exit}.items()}

@@ -114,6 +114,8 @@ typedef struct oracle_sim {
   int exact_stepping;
 } oracle_sim;
 
+/* The free-radius map of voxel-boundary stepping (port.cpp free_radius). */
+void oracle_free_radius(const short *labels, unsigned nx, unsigned ny, unsigned nz, unsigned char *out);
 void oracle_free_result(oracle_result *r);
 
 /* Reference build (oracle/_ref).  seed_fl replaces time(NULL) of the emission

@@ -1341,6 +1341,14 @@ extern "C" int oracle_run_photon(const oracle_sim *sim, const uint32_t *multipli
 
 /* ---------------------------------------------------------- test helpers */
 
+/* The free-radius map of voxel-boundary stepping for labels (nz, ny, nx),
+ * x fastest, into out (one byte per voxel). */
+extern "C" void oracle_free_radius(const short *labels, unsigned nx, unsigned ny, unsigned nz, unsigned char *out) {
+  std::vector<unsigned char> r;
+  free_radius(labels, nx, ny, nz, r);
+  memcpy(out, r.data(), r.size());
+}
+
 extern "C" float oracle_plogf(float x) { return mcfl_plogf(x); }
 extern "C" void oracle_psincosf(float x, float *s, float *c) { mcfl_psincosf(x, s, c); }
 

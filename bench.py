@@ -127,7 +127,8 @@ class ClockSampler:
 def cpu_reference_sample(nthreads: int, exc_photons: int = 4_000_000, fl_voxels: int = 16, per_voxel: int = 40_000):
     """The reference's transport algorithm on host threads over the benchmark
     medium (reference RNG streams and relaunch schedule, C-library math).
-    Returns (photons/s, photons, seconds, description)."""
+    Returns (photons/s, photons, seconds, description, excitation passes per
+    photon)."""
     from cudamcfl_gb300 import media
     from oracle import pyoracle
     pyoracle.build()
@@ -151,7 +152,7 @@ def cpu_reference_sample(nthreads: int, exc_photons: int = 4_000_000, fl_voxels:
     photons = r.photons_exc + r.photons_fl
     desc = (f"config-2 medium, {r.photons_exc} excitation photons + {r.fl_voxels} emitting voxels x {per_voxel} "
             f"emission photons; reference RNG streams (32768 MWC) and relaunch schedule, libm math")
-    return photons / dt, photons, dt, desc
+    return photons / dt, photons, dt, desc, r.steps_exc / max(1, r.photons_exc)
 
 
 def run_reference_arm(args):
@@ -162,9 +163,9 @@ def run_reference_arm(args):
     for _ in range(args.warmup):
         cpu_reference_sample(nthreads, exc_photons=100_000, fl_voxels=1)
     vals, tot_p, tot_t = [], 0, 0.0
-    desc = ""
+    desc, ppp = "", 0.0
     for _ in range(args.steps):
-        v, p, t, desc = cpu_reference_sample(nthreads, exc_photons=600_000, fl_voxels=4)
+        v, p, t, desc, ppp = cpu_reference_sample(nthreads, exc_photons=600_000, fl_voxels=4)
         vals.append(v)
         tot_p += p
         tot_t += t
@@ -174,7 +175,8 @@ def run_reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample": desc},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc,
+                         "passes_per_photon_exc": ppp},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -456,9 +458,9 @@ def main():
     # --- CPU baseline (reference algorithm on host cores) ---
     if "cpu" not in skip:
         nthreads = os.cpu_count() or 1
-        v, p, t, desc = cpu_reference_sample(nthreads)
+        v, p, t, desc, ppp = cpu_reference_sample(nthreads)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc,
-                                  "seconds": t}
+                                  "seconds": t, "passes_per_photon_exc": ppp}
     med.free()
     ctx.close()
     print(json.dumps(result), flush=True)

@@ -2,8 +2,9 @@
  * Persistent photon-transport kernel for voxelized (bulk-descriptor) turbid
  * media, sm_103a.
  *
- * Included by two translation units that differ only in floating-point
- * semantics:
+ * Included by three translation units that differ only in floating-point
+ * semantics (transport_f64.cu, the double-precision build of the same
+ * kernel, states the single-precision error):
  *   transport_exact.cu  MCFL_EXACT_MATH=1, nvcc -fmad=false -prec-div=true
  *                       -prec-sqrt=true -ftz=false: every float operation is
  *                       rounded once, logarithm and sine/cosine come from
@@ -41,11 +42,16 @@
  *     label (reloaded on a label change) when it mixes media;
  *   - the photon-hitting-density tally is one fire-and-forget 64-bit
  *     atomic add per pass, resolved in L2 (the 32 MB tally of a 200 x 200 x
- *     100 grid stays resident); aggregating successive passes in the same
- *     voxel in a register measured 5 % slower (the flush branch costs more
- *     than the atomics it saves);
+ *     100 grid stays resident), or, in the kPhdAgg variants the autotuner
+ *     can pick, successive passes in one voxel summed in a register first
+ *     (measured 4-5 % slower: the flush branch costs more than the atomics
+ *     it saves);
  *   - per-job weight accounting (absorbed, left at each face, roulette) for
- *     an exact integer energy balance.
+ *     an exact integer energy balance;
+ *   - an optional voxel-boundary stepping (kMode 2, beyond the reference):
+ *     the optical depth spent voxel by voxel, runs of equal labels crossed
+ *     in free cubes of a label + free-radius map, one segment per loop
+ *     iteration for every lane.
  */
 #include <cuda_runtime.h>
 #include <float.h>

@@ -36,7 +36,7 @@ def test_f64_kernel_agrees_with_exact_kernel(gpu_ctx):
         for k in ("Rd", "Tt", "fhd"):
             a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in dp])
             b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ex])
-            stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+            stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=None if k == "fhd" else (case.det[3], case.det[2]))
         for k in ("flR", "flT"):
             stats.gate(np.stack([getattr(r, k)[:xy] for r in dp]), np.stack([getattr(r, k)[:xy] for r in ex]),
                        frac_max=0.02, min_rel=1e-2)

@@ -49,7 +49,7 @@ def test_fast_math_kernel_agrees_with_exact_kernel(gpu_ctx):
         for k in ("Rd", "Tt", "fhd"):
             a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in fa])
             b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ex])
-            stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+            stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=None if k == "fhd" else (case.det[3], case.det[2]))
         for k in ("flR", "flT"):
             stats.gate(np.stack([getattr(r, k)[:xy] for r in fa]), np.stack([getattr(r, k)[:xy] for r in ex]),
                        frac_max=0.02, min_rel=1e-2)
@@ -82,7 +82,7 @@ def test_engine_agrees_with_reference_streams(math, oracle, safeprimes_file):
     for k in ("Rd", "Tt", "fhd"):
         a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in eng])
         b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ref])
-        stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+        stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=None if k == "fhd" else (case.det[3], case.det[2]))
     for k in ("flR", "flT"):
         stats.gate(np.stack([getattr(r, k)[:xy] for r in eng]), np.stack([getattr(r, k)[:xy] for r in ref]),
                    frac_max=0.02, min_rel=1e-2)
@@ -139,7 +139,7 @@ def test_layered_medium_agrees_with_reference_streams(math, oracle, safeprimes_f
     for k in ("Rd", "Tt", "fhd"):
         a = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in eng])
         b = np.stack([getattr(r, k)[:xy if k != "fhd" else None].astype(float) for r in ref])
-        stats.gate(a, b, frac_max=0.02, min_rel=1e-2)
+        stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=None if k == "fhd" else (case.det[3], case.det[2]))
     stats.gate(np.stack([r.time_xyt.ravel().astype(float) for r in eng]),
                np.stack([r.time_xyt.astype(float) for r in ref]), frac_max=0.02, min_rel=1e-2)
     w0 = case.start_weight()

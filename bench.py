@@ -18,7 +18,8 @@ emission photons).
   exact_stepping  voxel-boundary stepping against the reference's stepping on
               the same medium at a tenth of the budgets
   batching   256 Gaussian beams on a 16 x 16 raster over the 4 x 4 x 2 cm
-              sphere medium, log-uniform budgets, one persistent launch vs
+              sphere medium, log-uniform budgets 1e6..5e7 times
+              --batching-scale (0.1 by default), one persistent launch vs
               one launch per beam
   serving     Poisson stream of requests with their own media (64^3 ..
               256 x 256 x 128) and 1e5..1e8 photons at ~80 % load through the
@@ -27,9 +28,9 @@ emission photons).
               reference-stream mode, bit-identical to the reference's code) on
               the host cores, on a bounded sample of the same workload
 
---impl reference times that CPU implementation alone (the reference's own
-CUDA build cannot run here: it needs its missing multiplier file and a GPU
-build of sm_35/sm_50 era; the host build is its transport).
+--impl reference times that CPU implementation alone.  The reference's own
+CUDA program is not run: this repository holds none of the reference's
+sources, so there is nothing of it to build where the benchmark runs.
 """
 from __future__ import annotations
 
@@ -192,6 +193,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
+    ap.add_argument("--batching-scale", type=float, default=0.1,
+                    help="batching section: scale of config3's per-beam budgets (1e6..5e7 at 1.0)")
     ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,exact_stepping,batching,serving,cpu,e2e")
     ap.add_argument("--profile", action="store_true",
                     help="small case for ncu: the benchmark medium, --photons excitation photons and --per-voxel "
@@ -411,7 +414,7 @@ def main():
     if "batching" not in skip:
         c1 = media.config1()
         med1 = ctx.medium(c1.labels, c1.bulks, voxel_cm=c1.voxel_cm)
-        scale = 0.1
+        scale = args.batching_scale
         pos, budgets = media.raster_sources(16, 4.0, seed=3, scale=scale)
         runs = [mc.run_desc(b, source=(x, y, 0.0), det=c1.det, seed_exc=10_000 + i) for i, ((x, y), b)
                 in enumerate(zip(pos, budgets))]

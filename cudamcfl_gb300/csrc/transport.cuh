@@ -138,6 +138,12 @@ struct Rng {
     return MCFL_U2R_RZ((uint32_t)x) * MCFL_C(0x1p-32);
   }
   __device__ __forceinline__ real oc() { return MCFL_C(1.0) - co(); }
+  /* the next draw unscaled: co() = raw() * 2^-32 exactly (a power-of-two
+   * scale), so a constant times co() equals (constant * 2^-32) times raw() */
+  __device__ __forceinline__ real raw() {
+    x = (uint64_t)(uint32_t)x * a + (x >> 32);
+    return MCFL_U2R_RZ((uint32_t)x);
+  }
 };
 
 struct Photon {
@@ -414,15 +420,19 @@ __device__ __forceinline__ void spin(Photon &p, const Rec &c, Rng &r) {
   cost = (c.b.y - temp * temp) * c.b.z;
   if (two_g == MCFL_C(0.0)) cost = MCFL_C(2.0) * r.co() - MCFL_C(1.0);
   sint = MCFL_SQRT(MCFL_C(1.0) - cost * cost);
-  __sincosf(MCFL_C(2.0) * kPi * r.co(), &cosp, &sinp);
+  /* 2*pi*co() with the 2^-32 scale folded into the constant: the same value */
+  __sincosf((MCFL_C(2.0) * kPi * MCFL_C(0x1p-32)) * r.raw(), &cosp, &sinp);
   const real q = MCFL_C(1.0) - p.dz * p.dz;
   real dx, dy, dz;
   if (q > MCFL_C(0.0)) {
+    /* with st = sin(theta)/sin(theta_old), a = st cos(psi), b = st sin(psi):
+     * dz' = -sin(theta) cos(psi) sin(theta_old) + dz cos(theta) = -a q + dz cos(theta) */
     const real rq = rsqrtf(q); /* 1/sin(theta_old) */
     const real st = sint * rq;
-    dx = st * (p.dx * p.dz * cosp - p.dy * sinp) + p.dx * cost;
-    dy = st * (p.dy * p.dz * cosp + p.dx * sinp) + p.dy * cost;
-    dz = -sint * cosp * (q * rq) + p.dz * cost;
+    const real a = st * cosp, b = st * sinp;
+    dx = a * (p.dx * p.dz) - b * p.dy + p.dx * cost;
+    dy = a * (p.dy * p.dz) + b * p.dx + p.dy * cost;
+    dz = -a * q + p.dz * cost;
   } else {
     dx = sint * cosp;
     dy = sint * sinp;

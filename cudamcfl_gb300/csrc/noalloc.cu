@@ -13,21 +13,29 @@
  * Limits and rules:
  *   - at most MCFL_NOALLOC_MAX_JOBS simulations per call (the job table's
  *     size); more is rejected with MCFL_E_RANGE;
- *   - the first call on a device, with that device current, resolves the
- *     array's device address (cudaGetSymbolAddress) and writes the multiplier
- *     table into it; make that first call before any stream capture;
+ *   - the first call in a CUDA context (the device's primary context, or any
+ *     context the caller made current), with that context current, resolves
+ *     the array's device address (cudaGetSymbolAddress) and writes the
+ *     multiplier table into it; make that first call before any stream
+ *     capture (it is refused with MCFL_E_STATE while the stream captures).
+ *     A new context on the device (after cudaDeviceReset, for instance) has
+ *     its own copy of the array, which its first call sets up again;
  *   - every call shares the array and leaves its contents behind; the ticket
  *     counter is cleared at the start of each call, so calls that run one after
  *     another are independent, but calls that overlap on the GPU (other
  *     streams, other host threads) race on the array;
+ *   - the job table travels to the GPU as a kernel parameter (by value), so
+ *     nothing on the GPU refers to host memory of the call after it returns;
  *   - the output images and stats are cleared by the call, then accumulated
  *     by the kernel; the call is asynchronous on the given stream.
  * Nothing here calls cudaMalloc, cudaFree or any allocating library routine.
  */
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstddef>
 #include <cstring>
+#include <map>
 #include <mutex>
 
 #include "mcfl_internal.h"
@@ -45,40 +53,89 @@ struct NoallocScratch {
   uint32_t mult[32768];
 };
 
-/* Label records from the caller's (mutr, mu_a, g, n) table. */
-__global__ void noalloc_label_records(const float4 *prop, uint32_t n, float *lab) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
+/* A call's job table, passed by value (19.5 KB of kernel parameters). */
+struct JobStage {
+  McflJob jobs[MCFL_NOALLOC_MAX_JOBS];
+};
+static_assert(sizeof(JobStage) + 64 < 32764, "job table beyond the kernel parameter limit");
+
+/* Writes the call's job table into the scratch, clears the ticket counter and
+ * builds the label records from the caller's (mutr, mu_a, g, n) table. */
+__global__ void noalloc_prepare(const __grid_constant__ JobStage t, uint32_t n_jobs, const float4 *prop,
+                                uint32_t n_labels, NoallocScratch *sc) {
+  const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t nthreads = gridDim.x * blockDim.x;
+  const uint4 *src = reinterpret_cast<const uint4 *>(t.jobs);
+  uint4 *dst = reinterpret_cast<uint4 *>(sc->jobs);
+  const uint32_t words = n_jobs * (uint32_t)(sizeof(McflJob) / sizeof(uint4));
+  for (uint32_t i = tid; i < words; i += nthreads) dst[i] = src[i];
+  for (uint32_t i = tid; i < n_labels; i += nthreads) {
     const float4 q = prop[i];
-    mcfl_label_record(q.x, q.y, q.z, q.w, lab + (size_t)i * MCFL_LAB_FLOATS);
+    mcfl_label_record(q.x, q.y, q.z, q.w, sc->lab + (size_t)i * MCFL_LAB_FLOATS);
   }
+  if (tid == 0) sc->counter = 0ull;
 }
+static_assert(sizeof(McflJob) % sizeof(uint4) == 0, "job records are copied as 16-byte words");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoallocScratch)];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-NoallocScratch *g_scratch[kMaxDevices] = {nullptr};
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext *);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long *);
 
-/* Device address of the scratch array on the current device, set up on the
- * first call. */
-int scratch_for_current_device(NoallocScratch **out) {
-  int dev = 0;
-  MCFL_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return mcfl::fail(MCFL_E_RANGE, "noalloc: device index beyond 63");
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch[dev]) {
-    void *p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess) return mcfl::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
-    const std::vector<uint32_t> &tab = mcfl::mwc_table();
-    if (tab.size() != mcfl::kMwcTableEntries + 1) return mcfl::fail(MCFL_E_STATE, "multiplier table incomplete");
-    e = cudaMemcpy((char *)p + offsetof(NoallocScratch, mult), tab.data() + 1, mcfl::kMwcTableEntries * 4,
-                   cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return mcfl::cuda_fail(e, "noalloc multiplier upload");
-    g_scratch[dev] = (NoallocScratch *)p;
+std::mutex g_mu;
+/* set-up done, per CUDA context (by the context's process-unique ID) */
+std::map<unsigned long long, NoallocScratch *> g_scratch;
+
+/* The process-unique ID of the calling thread's current CUDA context (driver
+ * entry points looked up through the runtime, so the library does not link
+ * the driver library). */
+int current_context_id(unsigned long long *id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = cudaDriverEntryPointSymbolNotFound;
+    void *f1 = nullptr, *f2 = nullptr;
+    MCFL_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 4000, cudaEnableDefault, &q1));
+    MCFL_CUDA_TRY(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2));
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return mcfl::fail(MCFL_E_STATE, "noalloc: driver entry points cuCtxGetCurrent/cuCtxGetId not found");
+    get_current = (PfnCtxGetCurrent)f1;
+    get_id = (PfnCtxGetId)f2;
   }
-  *out = g_scratch[dev];
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return mcfl::fail(MCFL_E_STATE, "noalloc: no current CUDA context");
+  if (get_id(ctx, id) != CUDA_SUCCESS) return mcfl::fail(MCFL_E_STATE, "noalloc: cuCtxGetId failed");
+  return MCFL_OK;
+}
+
+/* Device address of the scratch array in the current context, set up on the
+ * context's first call (refused while stream s captures: the set-up copies
+ * the multiplier table synchronously). */
+int scratch_for_current_context(cudaStream_t s, NoallocScratch **out) {
+  /* resolves (and, on a context's first use, creates) the current context */
+  void *p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return mcfl::cuda_fail(e, "cudaGetSymbolAddress(noalloc scratch)");
+  unsigned long long id = 0;
+  int rc = current_context_id(&id);
+  if (rc != MCFL_OK) return rc;
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_scratch.find(id);
+  if (it != g_scratch.end() && it->second == (NoallocScratch *)p) {
+    *out = it->second;
+    return MCFL_OK;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  MCFL_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return mcfl::fail(MCFL_E_STATE, "noalloc: the first call in a CUDA context must come before stream capture");
+  const std::vector<uint32_t> &tab = mcfl::mwc_table();
+  if (tab.size() != mcfl::kMwcTableEntries + 1) return mcfl::fail(MCFL_E_STATE, "multiplier table incomplete");
+  e = cudaMemcpy((char *)p + offsetof(NoallocScratch, mult), tab.data() + 1, mcfl::kMwcTableEntries * 4,
+                 cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return mcfl::cuda_fail(e, "noalloc multiplier upload");
+  g_scratch[id] = (NoallocScratch *)p;
+  *out = (NoallocScratch *)p;
   return MCFL_OK;
 }
 
@@ -97,10 +154,14 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
   if (nx <= 0 || ny <= 0 || nz <= 0 || (unsigned long long)nx * ny * nz >= 0xFFFFFFFFull)
     return fail(MCFL_E_ARG, "noalloc: bad grid");
   if (n_bulks < 1 || n_bulks > MCFL_MAX_BULKS) return fail(MCFL_E_RANGE, "noalloc: n_bulks out of range");
+  if ((uintptr_t)d_prop % 16 != 0) return fail(MCFL_E_ARG, "noalloc: d_prop must be 16-byte aligned");
+  if ((uintptr_t)d_R % 8 != 0 || (uintptr_t)d_T % 8 != 0 || (uintptr_t)d_stats % 8 != 0)
+    return fail(MCFL_E_ARG, "noalloc: d_R, d_T and d_stats must be 8-byte aligned");
   const mcfl_detector det = runs[0].det;
-  if (det.nx <= 0 || det.ny <= 0 || !(det.dx > 0) || !(det.dy > 0)) return fail(MCFL_E_ARG, "noalloc: bad detector");
   for (int i = 0; i < n; ++i) {
     const mcfl_run_desc &r = runs[i];
+    if (r.det.nx <= 0 || r.det.ny <= 0 || !(r.det.dx > 0) || !(r.det.dy > 0))
+      return fail(MCFL_E_ARG, "noalloc: bad detector");
     if (r.photons == 0 || r.photons_per_voxel || r.fluence) return fail(MCFL_E_ARG, "noalloc: excitation images only");
     if (r.tdet.nx || r.exact_stepping) return fail(MCFL_E_ARG, "noalloc: the reference's stepping, no time detectors");
     if (r.start_weight == 0) return fail(MCFL_E_ARG, "noalloc: start_weight must be given");
@@ -108,14 +169,15 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
     if (r.source.kind != MCFL_SOURCE_GAUSS_BEAM && r.source.kind != MCFL_SOURCE_WIDEFIELD)
       return fail(MCFL_E_ARG, "noalloc: unknown source kind");
   }
-  NoallocScratch *sc = nullptr;
-  int rc = scratch_for_current_device(&sc);
-  if (rc != MCFL_OK) return rc;
   cudaStream_t s = (cudaStream_t)stream;
+  NoallocScratch *sc = nullptr;
+  int rc = scratch_for_current_context(s, &sc);
+  if (rc != MCFL_OK) return rc;
   cudaGetLastError();
   const size_t xy = (size_t)det.nx + (size_t)det.nx * det.ny;
-  McflJob jobs[MCFL_NOALLOC_MAX_JOBS];
-  std::memset(jobs, 0, sizeof(McflJob) * (size_t)n);
+  JobStage stage;
+  std::memset(&stage, 0, sizeof(stage));
+  McflJob *jobs = stage.jobs;
   unsigned long long tickets = 0;
   for (int i = 0; i < n; ++i) {
     const mcfl_run_desc &r = runs[i];
@@ -147,13 +209,11 @@ extern "C" int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, c
     j.photons = r.photons;
     tickets += r.photons;
   }
-  MCFL_CUDA_TRY(cudaMemsetAsync(&sc->counter, 0, sizeof(unsigned long long), s));
-  MCFL_CUDA_TRY(cudaMemcpyAsync(sc->jobs, jobs, sizeof(McflJob) * (size_t)n, cudaMemcpyHostToDevice, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(d_R, 0, (size_t)n * xy * 8, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(d_T, 0, (size_t)n * xy * 8, s));
   MCFL_CUDA_TRY(cudaMemsetAsync(d_stats, 0, (size_t)n * MCFL_ST_COUNT * 8, s));
   const uint32_t n_labels = (uint32_t)n_bulks + 2u;
-  noalloc_label_records<<<(n_labels + 127) / 128, 128, 0, s>>>((const float4 *)d_prop, n_labels, sc->lab);
+  noalloc_prepare<<<8, 256, 0, s>>>(stage, (uint32_t)n, (const float4 *)d_prop, n_labels, sc);
   MCFL_CUDA_TRY(cudaGetLastError());
   McflLaunch L;
   std::memset(&L, 0, sizeof(L));

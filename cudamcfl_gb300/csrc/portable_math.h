@@ -23,7 +23,8 @@
  *        then the Taylor series of sin (to r^9) and cos (to r^10) on
  *        |r| <= pi/4, truncation below 2e-9.
  * Domain: plog for positive normal floats; psincos for |x| < 2^10.  Both are
- * within a few ulp of the true function (tests/test_portable_math.py).
+ * within a few ulp of the true function (test_portable_math_accuracy in
+ * tests/test_cpu_basics.py).
  */
 #ifndef MCFL_PORTABLE_MATH_H
 #define MCFL_PORTABLE_MATH_H

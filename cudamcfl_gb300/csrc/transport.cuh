@@ -294,11 +294,14 @@ __device__ __forceinline__ void region_of(const Med &m, int x, int y, int z, uin
 template <int kMode>
 __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,
                                               Photon &p, Rng &r, uint32_t &src_idx) {
-  mcfl_photon_stream(__ldg((const unsigned long long *)&J->key),
-                     __ldg((const unsigned long long *)&J->rng_offset) + k, mult, &r.x, &r.a);
+  const uint64_t stream = __ldg((const unsigned long long *)&J->rng_offset) + k;
+  mcfl_photon_stream(__ldg((const unsigned long long *)&J->key), stream, mult, &r.x, &r.a);
   const uint64_t x_at_launch = r.x;
   const uint32_t kind = __ldg(&J->src_kind);
-  uint64_t k_in_run = k;
+  /* the photon's index in its run: the stream index for a beam (a shard of a
+   * run starts at its photon offset), the index within the voxel's run for
+   * an emitting voxel */
+  uint64_t k_in_run = stream;
   if (kind == MCFL_SRC_VOXELS) {
     const uint32_t per = __ldg(&J->per_voxel);
     src_idx = (uint32_t)(k / per);

@@ -273,7 +273,10 @@ typedef struct mcfl_run_desc {
   /* Index of the excitation run's first photon in the stream family of
    * seed_exc: photon k of the run draws stream photon_offset + k, so runs
    * over disjoint index ranges of one seed (on one GPU or several) sum to the
-   * run over their union bit for bit.  0 for a whole run. */
+   * run over their union bit for bit.  0 for a whole run.  With
+   * launch_rng_reuse the reuse applies to the photons whose index in the
+   * whole run, photon_offset + k, is below 32768, so the shards still sum to
+   * the whole run. */
   unsigned long long photon_offset;
   /* 1: voxel-boundary stepping: the optical depth -ln(u) of a pass is spent
    * voxel by voxel with each voxel's mu_t (mua + mus at excitation, muaf +
@@ -470,17 +473,21 @@ void mcfl_server_destroy(mcfl_server *server);
  * only handed device buffers): runs n <= MCFL_NOALLOC_MAX_JOBS excitation
  * simulations on one medium in one persistent launch, like mcfl_batch_run,
  * without allocating anything.  The caller passes the medium on the device
- * (labels, nx*ny*nz bytes; d_prop, 4 floats per label: 1/(mua+mus), mua, g, n
- * for labels 0..n_bulks+1) and the outputs on the device (d_R, d_T: n images
- * of det.nx + det.nx*det.ny 64-bit sums; d_stats: n x MCFL_NSTATS), which
- * the call clears.  Every run must give start_weight.  The kernel's scratch
- * (ticket counter, job table, label records, multiplier table, about
- * 159 KB) is one static
+ * (labels, nx*ny*nz bytes, each label <= n_bulks+1: a larger label reads an
+ * unset property record; d_prop, 16-byte aligned, 4 floats per label:
+ * 1/(mua+mus), mua, g, n for labels 0..n_bulks+1) and the outputs on the
+ * device (d_R, d_T: n images of det.nx + det.nx*det.ny 64-bit sums; d_stats:
+ * n x MCFL_NSTATS; all three 8-byte aligned), which the call clears.  Every
+ * run must give start_weight.  The kernel's scratch (ticket counter, job
+ * table, label records, multiplier table, about 159 KB) is one static
  * device array that every GPU loading the library holds until exit; the
- * first call on a device sets it up (make it before any stream capture);
- * calls share it, so calls that overlap on the GPU race.  Asynchronous on
- * stream (a cudaStream_t, NULL for the default stream).  More than
- * MCFL_NOALLOC_MAX_JOBS runs: MCFL_E_RANGE. */
+ * first call in a CUDA context sets it up, copying the multiplier table
+ * synchronously (make it before any stream capture; a new context, e.g.
+ * after cudaDeviceReset, is set up again by its first call); calls share the
+ * array, so calls that overlap on the GPU race.  The job table is passed to
+ * the GPU by value.  Asynchronous on stream (a cudaStream_t, NULL for the
+ * default stream).  More than MCFL_NOALLOC_MAX_JOBS runs: MCFL_E_RANGE;
+ * misaligned buffers: MCFL_E_ARG. */
 int mcfl_batch_run_noalloc(int math, const unsigned char *d_labels, const float *d_prop, int nx, int ny, int nz,
                            float half_x, float half_y, float thickness, const float *vox_per_cm, int n_bulks,
                            const mcfl_run_desc *runs, int n, unsigned long long *d_R, unsigned long long *d_T,

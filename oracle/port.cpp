@@ -1196,7 +1196,10 @@ void run_photon_range(const Phase &ph, uint64_t key, const uint32_t *table, uint
     Rng r;
     mcfl_photon_stream(key, offset + k, table, &r.x, &r.a);
     const uint64_t x_at_launch = r.x;
-    const uint64_t k_in_run = vox ? k % nv : k;
+    /* the photon's index in its run: the stream index for the beam (a shard
+     * of a run starts at its photon offset), the index within the voxel's
+     * run for an emitting voxel */
+    const uint64_t k_in_run = vox ? k % nv : offset + k;
     Photon p;
     if (vox) {
       uint32_t v = vox[k / nv];

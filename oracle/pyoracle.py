@@ -181,6 +181,17 @@ def build(reference_dir: str | None = None, quiet: bool = True) -> None:
     subprocess.run(args, **kw)
 
 
+def reference_dir() -> str:
+    """The reference checkout the host build of the reference compiles from:
+    REFERENCE_DIR of the environment, else the Makefile's default."""
+    env = os.environ.get("REFERENCE_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "refdir"], cwd=HERE, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                       text=True)
+    return r.stdout.strip()
+
+
 def _load(path):
     if not os.path.exists(path):
         raise FileNotFoundError(path)

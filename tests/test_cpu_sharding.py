@@ -8,7 +8,9 @@ it bit for bit, tests/test_gpu_parity.py) on its range with
 photon_offset = rank x share; an all-reduce sums R, T and the photon hitting
 density; rank 0's sum must equal the single-process run.  This is the
 multi-GPU decomposition of the path (one exchange: the integer sum);
-benchmark runs use one GPU per replica.
+benchmark runs use one GPU per replica.  With the reference's first-photon
+random-number reuse on, the reuse follows the photon's index in the whole
+run (photon_offset + k < 32768), so the shards still sum to the whole run.
 """
 import os
 import socket
@@ -25,7 +27,7 @@ def _free_port() -> int:
         return s.getsockname()[1]
 
 
-def _worker(rank, world, port, total, out_path):
+def _worker(rank, world, port, total, reuse, out_path):
     import torch.distributed as dist
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
@@ -40,6 +42,7 @@ def _worker(rank, world, port, total, out_path):
         case.do_fl = 2  # photon hitting density, no emission phase
         sim = case.oracle_sim()
         sim.photon_offset = rank * share
+        sim.launch_rng_reuse = reuse
         r = o.run_photon(sim, table, 5, 6, libm=False, nthreads=2)
         parts = [r.Rd, r.Tt, r.fhd, np.array(r.balance, dtype=np.uint64), np.array([r.steps_exc], dtype=np.uint64)]
         t = torch.from_numpy(np.concatenate(parts).view(np.int64).copy())
@@ -50,15 +53,19 @@ def _worker(rank, world, port, total, out_path):
         dist.destroy_process_group()
 
 
-def test_two_rank_shards_sum_to_the_whole_run(oracle, table32768, tmp_path):
+@pytest.mark.parametrize("reuse", [0, 1])
+def test_two_rank_shards_sum_to_the_whole_run(reuse, oracle, table32768, tmp_path):
     import torch.multiprocessing as mp
-    total = 40000
+    total = 40000  # with reuse, the first 32768 photons span both shards
     out = str(tmp_path / "sum.npy")
-    mp.start_processes(_worker, args=(2, _free_port(), total, out), nprocs=2, join=True, start_method="spawn")
+    mp.start_processes(_worker, args=(2, _free_port(), total, reuse, out), nprocs=2, join=True,
+                       start_method="spawn")
     from tests import cases
     case = cases.mismatch(photons=total, per_voxel=0)
     case.do_fl = 2
-    whole = oracle.run_photon(case.oracle_sim(), table32768, 5, 6, libm=False)
+    sim = case.oracle_sim()
+    sim.launch_rng_reuse = reuse
+    whole = oracle.run_photon(sim, table32768, 5, 6, libm=False)
     expect = np.concatenate([whole.Rd, whole.Tt, whole.fhd, np.array(whole.balance, dtype=np.uint64),
                              np.array([whole.steps_exc], dtype=np.uint64)])
     got = np.load(out)

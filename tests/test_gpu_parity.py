@@ -405,18 +405,24 @@ def test_time_and_layer_inputs_fail_with_status(gpu_ctx):
 
 
 @pytest.mark.gpu
-def test_photon_offset_shards_sum_to_the_whole_run(gpu_ctx):
+@pytest.mark.parametrize("reuse", [0, 1])
+def test_photon_offset_shards_sum_to_the_whole_run(reuse, gpu_ctx):
     """Runs over disjoint photon index ranges of one seed (photon_offset) sum
     to the run over their union, bit for bit: the decomposition a multi-GPU
-    run would use."""
-    case = cases.mismatch(photons=30000, per_voxel=0)
+    run would use; with the reference's first-photon reuse on, the reuse
+    follows the index in the whole run (the first 32768 photons span both
+    shards here)."""
+    case = cases.mismatch(photons=40000, per_voxel=0)
     case.do_fl = 2
     med = case.engine_medium(gpu_ctx)
-    whole = gpu_ctx.run(med, case.run_desc(7, 8))
+    rd = case.run_desc(7, 8)
+    rd.launch_rng_reuse = reuse
+    whole = gpu_ctx.run(med, rd)
     parts = []
-    for off, n in ((0, 7000), (7000, 23000)):
+    for off, n in ((0, 17000), (17000, 23000)):
         rd = case.run_desc(7, 8, photons=n)
         rd.photon_offset = off
+        rd.launch_rng_reuse = reuse
         parts.append(gpu_ctx.run(med, rd))
     med.free()
     for k in ("Rd", "Tt", "fhd"):

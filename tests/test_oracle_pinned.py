@@ -131,8 +131,9 @@ def _product_parse(lib, mci):
 
 
 def _ref_sample(path):
-    ref_dir = "/root/reference"
-    p = os.path.join(ref_dir, path)
+    from oracle import pyoracle
+    ref_dir = pyoracle.reference_dir()
+    p = os.path.join(ref_dir, path) if ref_dir else ""
     if not os.path.exists(p):
         pytest.skip("reference checkout not present")
     return p

@@ -5,10 +5,14 @@ memory pool, or handed only device buffers) use this variant of the batched
 excitation run: its scratch is a static device array inside the library, and
 the caller provides inputs and outputs on the device.  Here the device
 buffers come from torch, and the results must equal those of the allocating
-entry point (mcfl_batch_run) bit for bit — the same tolerance as every other
-parity test of the exact kernel — on two calls in a row, since the calls
-share and reuse the static scratch.  This file is collected last so that a
-run stopping at its first failure has run every other test before it.
+entry point (mcfl_batch_run, same math, same kernel variant) bit for bit —
+the tolerance of every other parity test of the exact kernel, and the
+fast-math kernel is as deterministic — on two calls in a row, since the
+calls share and reuse the static scratch.  The second call must leave the
+device's free memory and torch's allocated memory unchanged.  Invalid
+arguments are rejected before anything touches the GPU.  This file is
+collected last so that a run stopping at its first failure has run every
+other test before it.
 """
 import ctypes
 
@@ -28,16 +32,19 @@ def _runs(case):
             for i, ((x, y), b) in enumerate(zip(srcs, budgets))]
 
 
-def _noalloc(lib, case, runs, labels, prop, R, T, st, stream):
+def _ptr(t):
+    return ctypes.c_void_p(t if isinstance(t, int) else t.data_ptr())
+
+
+def _noalloc(lib, case, runs, labels, prop, R, T, st, stream, math=mc.MATH_EXACT):
     nx, ny, nz = case.dims
     e = np.float32(case.esp)
     vox = (ctypes.c_float * 3)(*([float(case.grid)] * 3))
     arr = (mc.RunDesc * len(runs))(*runs)
     return lib.mcfl_batch_run_noalloc(
-        mc.MATH_EXACT, ctypes.c_void_p(labels.data_ptr()), ctypes.c_void_p(prop.data_ptr()), nx, ny, nz,
+        math, _ptr(labels), _ptr(prop), nx, ny, nz,
         ctypes.c_float(float(np.float32(2) * e)), ctypes.c_float(float(np.float32(2) * e)), ctypes.c_float(float(e)),
-        vox, len(case.bulks()) - 2, arr, len(runs), ctypes.c_void_p(R.data_ptr()), ctypes.c_void_p(T.data_ptr()),
-        ctypes.c_void_p(st.data_ptr()), ctypes.c_void_p(stream))
+        vox, len(case.bulks()) - 2, arr, len(runs), _ptr(R), _ptr(T), _ptr(st), ctypes.c_void_p(stream))
 
 
 def _bind(lib):
@@ -49,7 +56,8 @@ def _bind(lib):
 
 
 @pytest.mark.gpu
-def test_noalloc_equals_batch_run_on_two_calls():
+@pytest.mark.parametrize("math", [mc.MATH_EXACT, mc.MATH_FAST])
+def test_noalloc_equals_batch_run_on_two_calls(math):
     torch = pytest.importorskip("torch")
     from cudamcfl_gb300 import build
     build.build()
@@ -57,7 +65,8 @@ def test_noalloc_equals_batch_run_on_two_calls():
     _bind(lib)
     case = cases.sphere()
     runs = _runs(case)
-    ctx = mc.Context(math=mc.MATH_EXACT)
+    ctx = mc.Context(math=math)
+    ctx.set_option("variant", 0)  # the kernel variant the allocation-free call launches
     med = case.engine_medium(ctx)
     ref, _ = mc.batch_run(ctx, med, runs, mc.SCHEDULE_BATCHED)
     med.free()
@@ -73,8 +82,14 @@ def test_noalloc_equals_batch_run_on_two_calls():
     st = torch.full((n * mc.NSTATS,), -1, dtype=torch.int64, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
     for call in range(2):
-        assert _noalloc(lib, case, runs, labels, prop, R, T, st, stream) == mc.OK, mc.last_error()
         torch.cuda.synchronize(dev)
+        free0, _ = torch.cuda.mem_get_info(dev)
+        alloc0 = torch.cuda.memory_allocated(dev)
+        assert _noalloc(lib, case, runs, labels, prop, R, T, st, stream, math) == mc.OK, mc.last_error()
+        torch.cuda.synchronize(dev)
+        if call == 1:  # the first call of the process may load kernels; the second allocates nothing
+            assert torch.cuda.mem_get_info(dev)[0] == free0
+            assert torch.cuda.memory_allocated(dev) == alloc0
         Rh = R.cpu().numpy().view(np.uint64).reshape(n, xy)
         Th = T.cpu().numpy().view(np.uint64).reshape(n, xy)
         Sh = st.cpu().numpy().view(np.uint64).reshape(n, mc.NSTATS)
@@ -99,3 +114,27 @@ def test_noalloc_rejects_more_than_max_jobs():
     rc = _noalloc(lib, case, runs, labels, prop, buf, buf, buf, torch.cuda.current_stream(dev).cuda_stream)
     assert rc == mc.E_RANGE
     assert "MCFL_NOALLOC_MAX_JOBS" in mc.last_error()
+
+
+def test_noalloc_rejects_bad_arguments_before_any_gpu_work():
+    """Misaligned buffers and a bad detector on any run are refused by the
+    host checks, before the call touches the GPU (the addresses below are
+    never dereferenced)."""
+    from cudamcfl_gb300 import build
+    build.build()
+    lib = mc.load()
+    _bind(lib)
+    case = cases.tiny()
+    runs = _runs(case)
+    good = dict(labels=0x10000, prop=0x20000, R=0x30000, T=0x40000, st=0x50000)
+
+    def call(**kw):
+        a = dict(good, **kw)
+        return _noalloc(lib, case, kw.pop("runs", runs), a["labels"], a["prop"], a["R"], a["T"], a["st"], 0)
+
+    assert call(prop=0x20004) == mc.E_ARG and "16-byte" in mc.last_error()
+    assert call(R=0x30004) == mc.E_ARG and "8-byte" in mc.last_error()
+    assert call(st=0x50002) == mc.E_ARG
+    bad = _runs(case)
+    bad[2].det.dx = 0.0
+    assert call(runs=bad) == mc.E_ARG and "detector" in mc.last_error()

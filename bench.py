@@ -18,12 +18,15 @@ emission photons).
   exact_stepping  voxel-boundary stepping against the reference's stepping on
               the same medium at a tenth of the budgets
   batching   256 Gaussian beams on a 16 x 16 raster over the 4 x 4 x 2 cm
-              sphere medium, log-uniform budgets 1e6..5e7 times
-              --batching-scale (0.1 by default), one persistent launch vs
-              one launch per beam
+              sphere medium, log-uniform budgets 1e6..5e7 (3.1e9 photons;
+              --batching-scale scales them), one persistent launch vs one
+              launch per beam
   serving     Poisson stream of requests with their own media (64^3 ..
               256 x 256 x 128) and 1e5..1e8 photons at ~80 % load through the
               continuous-batching server: p50/p99 latency, photons/s
+  precision   the config-5 medium (512 x 512 x 256 voxels, 268 MB map), the
+              FP32 builds against the FP64 build of the same kernel on the
+              same seeds: integrated R/T/absorbed error and z, R image
   cpu_baseline  the reference's transport algorithm (the oracle restatement in
               reference-stream mode, bit-identical to the reference's code) on
               the host cores, on a bounded sample of the same workload
@@ -35,6 +38,8 @@ sources, so there is nothing of it to build where the benchmark runs.
 from __future__ import annotations
 
 import argparse
+import csv
+import hashlib
 import json
 import math
 import os
@@ -60,6 +65,74 @@ WORKLOAD = ("voxelized heterogeneous bulk descriptor 200x200x100 @0.02cm, 8 labe
 
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ traffic
+
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "transport_fast_traffic.json")
+KERNEL_SOURCES = ("transport.cuh", "transport_fast.cu", "engine_types.h", "portable_math.h")
+
+
+def kernel_source_sha() -> str:
+    """SHA-256 over the fast-math transport kernel's sources and nvcc flags
+    (include paths left out): the identity of the build a DRAM-traffic
+    capture belongs to."""
+    from cudamcfl_gb300 import build as b
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(b.CSRC, f), "rb") as fh:
+            h.update(fh.read())
+    flags = b.ARCH + [f for f in b.NVCC_COMMON if not f.startswith("-I")] + b.CUDA_UNITS["transport_fast.cu"]
+    h.update(" ".join(flags).encode())
+    return h.hexdigest()
+
+
+_UNITS = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "Tbyte": 1e12,
+          "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0}
+
+
+def traffic_from_csv(path: str, command: str) -> dict:
+    """Per transport launch of an ncu CSV capture (--csv with the metrics
+    dram__bytes_read.sum, dram__bytes_write.sum, gpu__time_duration.sum):
+    DRAM bytes and duration; written to TRAFFIC_FILE with the build's source
+    hash."""
+    launches = {}
+    with open(path, newline="") as f:
+        rows = [r for r in csv.reader(f) if r]
+    head = next(i for i, r in enumerate(rows) if "Metric Name" in r)
+    cols = rows[head]
+    ci = {k: cols.index(k) for k in ("ID", "Kernel Name", "Metric Name", "Metric Unit", "Metric Value")}
+    for r in rows[head + 1:]:
+        if len(r) < len(cols) or "mcfl_transport_fast" not in r[ci["Kernel Name"]]:
+            continue
+        v = float(r[ci["Metric Value"]].replace(",", "")) * _UNITS.get(r[ci["Metric Unit"]], 1.0)
+        d = launches.setdefault(int(r[ci["ID"]]), {"kernel": r[ci["Kernel Name"]]})
+        d[r[ci["Metric Name"]]] = v
+    out = []
+    for i in sorted(launches):
+        d = launches[i]
+        out.append({"launch": len(out), "kernel": d["kernel"][:80],
+                    "dram_bytes": d.get("dram__bytes_read.sum", 0.0) + d.get("dram__bytes_write.sum", 0.0),
+                    "duration_s": d.get("gpu__time_duration.sum")})
+    rec = {"source_sha256": kernel_source_sha(), "command": command, "launches": out,
+           "dram_bytes_per_launch": sum(x["dram_bytes"] for x in out) / max(1, len(out))}
+    with open(TRAFFIC_FILE, "w") as f:
+        json.dump(rec, f, indent=1)
+        f.write("\n")
+    return rec
+
+
+def traffic_of_this_build():
+    """(DRAM bytes per transport launch, note) from TRAFFIC_FILE when it was
+    captured on this build's kernel sources, else (None, why)."""
+    try:
+        with open(TRAFFIC_FILE) as f:
+            rec = json.load(f)
+    except (OSError, ValueError):
+        return None, "no ncu capture of the DRAM traffic on record"
+    if rec.get("source_sha256") != kernel_source_sha():
+        return None, "the DRAM-traffic capture on record belongs to another build of the kernel"
+    return rec["dram_bytes_per_launch"], f"ncu capture of this build: {rec['command']}"
 
 
 # ------------------------------------------------------------------ clocks
@@ -129,7 +202,8 @@ def cpu_reference_sample(nthreads: int, exc_photons: int = 4_000_000, fl_voxels:
     """The reference's transport algorithm on host threads over the benchmark
     medium (reference RNG streams and relaunch schedule, C-library math).
     Returns (photons/s, photons, seconds, description, excitation passes per
-    photon)."""
+    photon, per-phase rates: excitation-only and emission-only photons/s and
+    passes/s)."""
     from cudamcfl_gb300 import media
     from oracle import pyoracle
     pyoracle.build()
@@ -153,7 +227,13 @@ def cpu_reference_sample(nthreads: int, exc_photons: int = 4_000_000, fl_voxels:
     photons = r.photons_exc + r.photons_fl
     desc = (f"config-2 medium, {r.photons_exc} excitation photons + {r.fl_voxels} emitting voxels x {per_voxel} "
             f"emission photons; reference RNG streams (32768 MWC) and relaunch schedule, libm math")
-    return photons / dt, photons, dt, desc, r.steps_exc / max(1, r.photons_exc)
+    phases = {"excitation_photons_per_s": r.photons_exc / r.seconds_exc if r.seconds_exc > 0 else None,
+              "excitation_passes_per_s": r.steps_exc / r.seconds_exc if r.seconds_exc > 0 else None,
+              "emission_photons_per_s": r.photons_fl / r.seconds_fl if r.seconds_fl > 0 and r.photons_fl else None,
+              "emission_passes_per_s": r.steps_fl / r.seconds_fl if r.seconds_fl > 0 and r.photons_fl else None,
+              "excitation_seconds": r.seconds_exc, "emission_seconds": r.seconds_fl,
+              "passes_per_photon_fl": r.steps_fl / max(1, r.photons_fl)}
+    return photons / dt, photons, dt, desc, r.steps_exc / max(1, r.photons_exc), phases
 
 
 def run_reference_arm(args):
@@ -164,9 +244,9 @@ def run_reference_arm(args):
     for _ in range(args.warmup):
         cpu_reference_sample(nthreads, exc_photons=100_000, fl_voxels=1)
     vals, tot_p, tot_t = [], 0, 0.0
-    desc, ppp = "", 0.0
+    desc, ppp, phases = "", 0.0, {}
     for _ in range(args.steps):
-        v, p, t, desc, ppp = cpu_reference_sample(nthreads, exc_photons=600_000, fl_voxels=4)
+        v, p, t, desc, ppp, phases = cpu_reference_sample(nthreads, exc_photons=600_000, fl_voxels=4)
         vals.append(v)
         tot_p += p
         tot_t += t
@@ -177,7 +257,7 @@ def run_reference_arm(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "sample": desc},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc,
-                         "passes_per_photon_exc": ppp},
+                         "passes_per_photon_exc": ppp, "phases_last_step": phases},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -193,9 +273,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--math", default="fast", choices=["fast", "exact"])
-    ap.add_argument("--batching-scale", type=float, default=0.1,
+    ap.add_argument("--batching-scale", type=float, default=1.0,
                     help="batching section: scale of config3's per-beam budgets (1e6..5e7 at 1.0)")
-    ap.add_argument("--skip", default="", help="comma list of sections to skip: plain,exact_stepping,batching,serving,cpu,e2e")
+    ap.add_argument("--skip", default="",
+                    help="comma list of sections to skip: plain,exact_stepping,batching,serving,precision,cpu,e2e")
+    ap.add_argument("--precision-photons", type=float, default=1e8,
+                    help="precision section: photons per build (config5, FP32 builds vs FP64)")
     ap.add_argument("--profile", action="store_true",
                     help="small case for ncu: the benchmark medium, --photons excitation photons and --per-voxel "
                          "emission photons per voxel, --warmup runs then one run (2 transport launches per run)")
@@ -203,7 +286,17 @@ def main():
     ap.add_argument("--variant", type=int, default=0, help="--profile: kernel variant (0..2)")
     ap.add_argument("--per-voxel", type=int, default=20, help="--profile: emission photons per emitting voxel")
     ap.add_argument("--exact-stepping", action="store_true", help="--profile: voxel-boundary stepping")
+    ap.add_argument("--traffic-from", default="",
+                    help="write the DRAM traffic per transport launch of an ncu CSV capture (with this build's "
+                         "source hash) to profiles/transport_fast_traffic.json and exit; --traffic-command names "
+                         "the captured command")
+    ap.add_argument("--traffic-command", default="")
+    ap.add_argument("--pass-form", type=int, default=0,
+                    help="--profile: 0 the pass arranged for the SIMT warp, 1 every test as its own branch")
     args = ap.parse_args()
+    if args.traffic_from:
+        print(json.dumps(traffic_from_csv(args.traffic_from, args.traffic_command)))
+        return 0
     if args.impl == "reference":
         return run_reference_arm(args)
     if args.profile:
@@ -326,20 +419,9 @@ def main():
     n_sm = ctx.get_option("sm_count")
     xu_peak = n_sm * 16 * sm_mhz * 1e6
     fp32_peak = n_sm * 128 * sm_mhz * 1e6
-    # DRAM bytes per transport launch from the ncu launch list summarised in
-    # profiles/transport_fast_config2.md (medium and tallies stay in L2, so a
-    # launch's DRAM traffic is its footprint, independent of its passes)
-    traffic = None
-    try:
-        vals = {}
-        for line in open(os.path.join(ROOT, "profiles", "transport_fast_config2.md")):
-            if line.startswith("dram_bytes_per_launch_"):
-                k, v = line.split(":", 1)
-                vals[k.strip()] = float(v)
-        if vals:
-            traffic = sum(vals.values()) / len(vals)
-    except (OSError, ValueError):
-        pass
+    # DRAM bytes per transport launch of this workload, from an ncu capture
+    # of this build's kernel (keyed by its source hash), else null
+    traffic, traffic_note = traffic_of_this_build()
     result["roofline"] = {
         "bound": "xu", "achieved": xu_ops * pass_rate / 1e12, "peak": xu_peak / 1e12, "unit": "Top/s",
         "frac": xu_ops * pass_rate / xu_peak, "traffic": traffic,
@@ -350,7 +432,7 @@ def main():
                  f"algorithmic XU ops ({xu_ops}: 10 MUFU + 8 conversions) per transport pass x passes/s over "
                  f"{n_sm} SMs x 16 XU lanes x {sm_mhz:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json); FP32 analogue "
                  f"({fp32_ops} ops/pass over 128 lanes) beside it; traffic = mean DRAM bytes per transport launch "
-                 "(ncu, cold cache)"),
+                 f"({traffic_note})"),
     }
 
     # --- e2e through the C ABI with host buffers ---
@@ -458,12 +540,22 @@ def main():
     if "serving" not in skip:
         result["serving"] = serve_stream(mc, ctx, local, duration_s=12.0)
 
+    # --- precision: the FP32 builds against the FP64 build on identical seeds ---
+    if "precision" not in skip:
+        result["precision"] = precision_section(mc, local, args.precision_photons)
+
     # --- CPU baseline (reference algorithm on host cores) ---
     if "cpu" not in skip:
         nthreads = os.cpu_count() or 1
-        v, p, t, desc, ppp = cpu_reference_sample(nthreads)
+        v, p, t, desc, ppp, phases = cpu_reference_sample(nthreads)
         result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": desc,
-                                  "seconds": t, "passes_per_photon_exc": ppp}
+                                  "seconds": t, "passes_per_photon_exc": ppp, "phases": phases}
+        # the same phases on the GPU, for the ratio of each phase alone
+        result["cpu_baseline"]["gpu_over_cpu"] = {
+            "excitation": result["phases"]["excitation_photons_per_s"] / phases["excitation_photons_per_s"]
+            if phases.get("excitation_photons_per_s") else None,
+            "emission": result["phases"]["emission_photons_per_s"] / phases["emission_photons_per_s"]
+            if phases.get("emission_photons_per_s") else None}
     med.free()
     ctx.close()
     print(json.dumps(result), flush=True)
@@ -472,12 +564,51 @@ def main():
     return 0
 
 
+def precision_section(mc, device: int, photons: float, batches: int = 10):
+    """The config-5 precision study at a bounded budget: 512 x 512 x 256
+    voxels of 0.01 cm with a 268 MB fluorophore map, mu_s' = 20/cm, wide-field
+    source; the fast-math and the exact-math FP32 builds and the FP64 build of
+    the same kernel on the same seeds; integrated R, T and absorbed fraction
+    (relative difference, paired z) and the R image against FP64."""
+    from cudamcfl_gb300 import media, precision
+    m = media.config5()
+    ctx = mc.Context(device=device)
+    try:
+        med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
+        w, h = m.info["widefield"]
+        per_batch = int(photons) // batches
+
+        def rd_for_seed(seed):
+            return mc.run_desc(per_batch, det=m.det, fluence=0, seed_exc=seed, seed_fl=seed + 1,
+                               kind=mc.SOURCE_WIDEFIELD, width=w, height=h)
+
+        res = precision.study(ctx, med, rd_for_seed, batches, ("fast", "exact", "f64"), fluence=False)
+        med.free()
+    finally:
+        ctx.close()
+    out = precision.summarize(res)
+    keep = {}
+    for mode in ("fast", "exact"):
+        o = out[mode]
+        keep[mode] = {k: {q: o[k][q] for q in ("rel_diff", "paired_se_rel", "z")}
+                      for k in ("R_total", "T_total", "absorbed")}
+        keep[mode]["R_image"] = {q: o["R_image"].get(q) for q in ("entries", "rel_rms", "beyond_t", "t_threshold")}
+        keep[mode]["passes_ratio"] = o["steps_ratio"]
+    keep["photons_per_s"] = {k: v["photons_per_s"] for k, v in out["timing"].items()}
+    keep["workload"] = (f"config5: 512x512x256 voxels of 0.01 cm (labels + 268 MB fp32 fluorophore map), "
+                        f"mu_s' 20/cm, 5.12x5.12 cm wide-field source, {per_batch * batches:.3g} photons per build "
+                        f"in {batches} batches on identical seeds; FP32 fast-math and exact-math builds vs the FP64 "
+                        f"build of the same kernel (paired differences)")
+    return keep
+
+
 def profile_case(args):
     import cudamcfl_gb300 as mc
     from cudamcfl_gb300 import build, media
     build.build()
     ctx = mc.Context(device=0, math=mc.MATH_FAST if args.math == "fast" else mc.MATH_EXACT)
     ctx.set_option("variant", args.variant)
+    ctx.set_option("pass_form", args.pass_form)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
     rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2,
@@ -488,7 +619,8 @@ def profile_case(args):
                       "exact_stepping": bool(args.exact_stepping),
                       "emission_photons": r.photons_fl, "steps_exc": r.stats_exc["steps"],
                       "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
-                      "variant": args.variant, "regs": ctx.get_option("regs"), "grid": ctx.get_option("grid"),
+                      "variant": args.variant, "pass_form": args.pass_form, "regs": ctx.get_option("regs"),
+                      "grid": ctx.get_option("grid"),
                       "block": ctx.get_option("launch_block")}), flush=True)
     med.free()
     ctx.close()

@@ -74,7 +74,8 @@ int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool 
   *blk = block;
   *bps = 0;
   *regs = 0;
-  const int mixed = mixed_variant == 1 ? -3 : mixed_variant == 2 ? -4 : -1;
+  static const int mixed_codes[6] = {-1, -3, -4, -5, -6, -7};
+  const int mixed = mixed_codes[mixed_code()];
   const int v = exact ? (time ? 10 : 6) : uniform ? (time ? 3 : variant_code()) : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
@@ -170,6 +171,8 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
     c->variant = (int)v;
   } else if (k == "phd_agg") {
     c->phd_agg = v ? 1 : 0;
+  } else if (k == "pass_form") {
+    c->pass_form = v ? 1 : 0;
   } else if (k == "mixed_variant") {
     if (v < 0 || v > 2) return fail(MCFL_E_ARG, "mixed_variant: 0..2");
     c->mixed_variant = (int)v;
@@ -207,6 +210,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "blocks_per_sm") return c->blocks_per_sm;
   if (k == "variant") return c->variant;
   if (k == "phd_agg") return c->phd_agg;
+  if (k == "pass_form") return c->pass_form;
   if (k == "mixed_variant") return c->mixed_variant;
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;

@@ -161,9 +161,12 @@ struct mcfl_ctx {
   int block = 256;   /* threads per block, clamped to the variant's bound */
   int variant = 0;   /* occupancy variant of the single-medium kernel */
   int phd_agg = 0;   /* 1: photon-hitting-density sums held in a register (kernel variants 7..9) */
+  int pass_form = 0; /* 1: the pass with every test as its own branch (kernel variants 11..13) */
   /* the single-medium kernel variant the launches use */
-  int variant_code() const { return variant + (phd_agg ? 7 : 0); }
+  int variant_code() const { return variant + (phd_agg ? 7 : pass_form ? 11 : 0); }
   int mixed_variant = 2; /* occupancy variant of the mixed-media kernel (128 x 7 measured fastest) */
+  /* the mixed-media kernel variant the launches use (McflLaunch::variant) */
+  int mixed_code() const { return mixed_variant + (pass_form ? 3 : 0); }
   int blocks_per_sm = 0;
   uint32_t step_cap = 1u << 24;
   int l2_window = 0;            /* 1: persisting-L2 window over the medium's labels */

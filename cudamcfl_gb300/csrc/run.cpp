@@ -572,7 +572,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.ticket_counter = c->bcnt.as<unsigned long long>();
       L.ticket_end = tickets;
       if (uniform) set_uniform(c, L, m, false, nullptr, exact);
-      else L.variant = (uint32_t)c->mixed_variant;
+      else L.variant = (uint32_t)c->mixed_code();
       L.exact_step = exact ? 1u : 0u;
       if ((e = record_event(c->ev[0], st))) return e;
       if ((e = launch_fn(c->math)(&L, grid, block, st)))

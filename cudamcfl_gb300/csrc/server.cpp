@@ -311,7 +311,7 @@ void mcfl_server::loop() {
       L.ticket_end2 = tickets_end2;
     }
     L.max_iters = slice_cur;
-    L.variant = (uint32_t)ctx->mixed_variant;
+    L.variant = (uint32_t)ctx->mixed_code();
     L.ticket_counter = counter.as<unsigned long long>();
     L.ticket_end = tickets_end;
     L.mult = ctx->mult.as<uint32_t>();

@@ -130,20 +130,31 @@ constexpr real kChance = MCFL_C(0.1);            /* CUDAMCFL.h:34 */
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kEv = 6; /* event counters kept in shared memory: EXIT_TOP .. CAPPED */
 
+/* shared-memory bytes of the label records (launches over one medium) */
+__host__ __device__ constexpr size_t lab_bytes(bool uniform) {
+  return uniform ? (size_t)MCFL_MAX_LABELS * MCFL_LAB_FLOATS * sizeof(real) : 0;
+}
+
 struct Rng {
   uint64_t x;
   uint32_t a;
-  __device__ __forceinline__ real co() {
-    x = (uint64_t)(uint32_t)x * a + (x >> 32);
-    return MCFL_U2R_RZ((uint32_t)x) * MCFL_C(0x1p-32);
+  /* x <- lo(x) a + hi(x) (the MWC recurrence of CUDAMCFLrng.cu:17-29) as one
+   * carry chain: low word lo(x) a + hi(x) with carry out, high word the high
+   * half of lo(x) a plus the carry; returns the new low word */
+  __device__ __forceinline__ uint32_t step() {
+    const uint32_t lo = (uint32_t)x;
+    uint32_t hi = (uint32_t)(x >> 32), nlo;
+    asm("{\n\t.reg .u32 t;\n\tmad.lo.cc.u32 t, %2, %3, %1;\n\tmadc.hi.u32 %1, %2, %3, 0;\n\tmov.u32 %0, t;\n\t}"
+        : "=r"(nlo), "+r"(hi)
+        : "r"(lo), "r"(a));
+    x = ((uint64_t)hi << 32) | nlo;
+    return nlo;
   }
+  __device__ __forceinline__ real co() { return MCFL_U2R_RZ(step()) * MCFL_C(0x1p-32); }
   __device__ __forceinline__ real oc() { return MCFL_C(1.0) - co(); }
   /* the next draw unscaled: co() = raw() * 2^-32 exactly (a power-of-two
    * scale), so a constant times co() equals (constant * 2^-32) times raw() */
-  __device__ __forceinline__ real raw() {
-    x = (uint64_t)(uint32_t)x * a + (x >> 32);
-    return MCFL_U2R_RZ((uint32_t)x);
-  }
+  __device__ __forceinline__ real raw() { return MCFL_U2R_RZ(step()); }
 };
 
 struct Photon {
@@ -225,6 +236,15 @@ __device__ __forceinline__ Rec load_rec(const Med &m, uint32_t label) {
   return r;
 }
 #endif
+
+/* The refractive index of a label (mixed-media launches, from global memory). */
+__device__ __forceinline__ real label_n(const Med &m, uint32_t label) {
+#if MCFL_F64
+  return (real)__ldg(reinterpret_cast<const float *>(m.prop) + 4 * label + 3);
+#else
+  return __ldg(reinterpret_cast<const float *>(m.lab) + MCFL_LAB_FLOATS * label + 7);
+#endif
+}
 
 __device__ __forceinline__ uint32_t voxel_index(const Med &m, real x, real y, real z) {
   uint32_t i = MCFL_R2U_RZ((x + m.hx) * m.gx) +
@@ -698,18 +718,27 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
  * tally sums the weights of a thread's successive passes in one voxel in a
  * register and adds them to HBM when the voxel changes (and at the end),
  * instead of one atomic add per pass; the autotuner picks the form. */
-template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks, bool kPhdAgg = false>
+/* kGeneral (single medium, reference stepping): every test of the
+ * reference's pass as its own branch (the form before the SIMT arrangement),
+ * kept as an autotuner alternative. */
+template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks, bool kPhdAgg = false,
+          bool kGeneral = false>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   constexpr bool kLayered = kMode == 1;
   constexpr bool kExactStep = kMode == 2;
-  /* shared memory: kEv x blockDim.x event counters, then (uniform medium)
-   * the label records of the medium */
-  extern __shared__ unsigned long long s_ev[];
-  real4 *s_lab = reinterpret_cast<real4 *>(s_ev + kEv * blockDim.x);
+  /* the reference-stepping pass without the time of flight, arranged for
+   * the SIMT warp (see the pass below) */
+  constexpr bool kLean = kMode == 0 && !kTime && !kPhdAgg && !kGeneral;
+  /* dynamic shared memory: (uniform medium) the label records of the
+   * medium at offset 0, then kEv x kThreads event counters (compile-time
+   * offsets and strides) */
+  extern __shared__ __align__(16) unsigned char s_mem[];
+  real4 *s_lab = reinterpret_cast<real4 *>(s_mem);
+  unsigned long long *s_ev = reinterpret_cast<unsigned long long *>(s_mem + lab_bytes(kUniform));
   const unsigned lane = threadIdx.x & 31u;
   const unsigned tib = threadIdx.x;
   const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int e = 0; e < kEv; ++e) s_ev[e * blockDim.x + tib] = 0ull;
+  for (int e = 0; e < kEv; ++e) s_ev[e * kThreads + tib] = 0ull;
   if (kLayered) {
     /* per layer (and, last, the inclusion): its record and its geometry */
     const float4 *tab = (const float4 *)L.med.layer_tab;
@@ -779,6 +808,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   unsigned long long f_acc = 0ull;
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
+  uint32_t absorbed_ph = 0; /* lean pass: absorbed weight since the photon's last roulette */
   const McflJob *J = nullptr;
 
   auto flush_stats = [&]() {
@@ -788,15 +818,15 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (steps) atomicAdd(&st[MCFL_ST_STEPS], (unsigned long long)steps);
     if (absorbed) atomicAdd(&st[MCFL_ST_ABSORBED], (unsigned long long)absorbed);
     for (int e = 0; e < kEv; ++e) {
-      unsigned long long v = s_ev[e * blockDim.x + tib];
+      unsigned long long v = s_ev[e * kThreads + tib];
       if (v) atomicAdd(&st[MCFL_ST_EXIT_TOP + e], v);
-      s_ev[e * blockDim.x + tib] = 0ull;
+      s_ev[e * kThreads + tib] = 0ull;
     }
     done = 0;
     steps = 0;
     absorbed = 0;
   };
-  auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * blockDim.x + tib] += v; };
+  auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * kThreads + tib] += v; };
 
   if (!kUniform && L.max_iters && L.saved) {
     const McflSaved sv = L.saved[gtid];
@@ -1087,6 +1117,102 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         absorbed += w;
         spin(p, c2, r);
       }
+    } else if constexpr (kLean) {
+      /* ---- one transport pass of a voxelized medium (MCd3D loop body,
+       * CUDAMCFLtransport.cu:286-447), arranged for the SIMT warp.
+       * Every test of the reference's pass compiled to a divergent branch of
+       * its own.  Here the common pass — a positive step that stays inside
+       * the slab in a scattering medium and ends in the same label or in
+       * one of the same refractive index (where Reflect transmits without
+       * drawing a number) — runs as straight-line code with the hitting
+       * density tallied under a predicate, and every other case takes one
+       * shared branch that runs the reference's sequence for it.  The same
+       * operations run on the same values in the same order, so the tallies
+       * equal the general pass's bit for bit; the weight drop and the spin
+       * (the bulk of a pass) stay common to both.  A single-medium launch
+       * reads the label records from shared memory; a mixed-media launch
+       * holds the photon's record in registers and reloads it when the
+       * label changes. ---- */
+      const real mutr = kUniform ? s_lab[2 * p.label].x : rc.a.x;
+      const uint64_t x_before = r.x;
+      real s = -MCFL_LOGF(r.oc()) * mutr;
+      if (!(mutr != FLT_MAX)) r.x = x_before; /* a scattering-free voxel draws no step length */
+      const real zn = p.z + s * p.dz;
+      const real xn = p.x + p.dx * s, yn = p.y + p.dy * s;
+      const bool inside = MCFL_FABS(xn) < m.hx && MCFL_FABS(yn) < m.hy && zn < m.esp;
+      const uint32_t vi = voxel_index(m, xn, yn, zn); /* clamped: always a voxel of the grid */
+      const uint32_t g = (uint32_t)m.labels[vi];
+      const uint32_t lab = inside ? g : 1u;
+      const real n_old = kUniform ? s_lab[2 * p.label + 1].w : rc.b.w;
+      const real n_new = kUniform ? s_lab[2 * lab + 1].w : label_n(m, lab);
+      const bool clip = zn < MCFL_C(0.0) || zn > m.esp;
+      const bool rare = !(mutr != FLT_MAX) || clip || !(s > MCFL_C(0.0)) ||
+                        (lab != p.label && (n_new != n_old || lab - 1u >= m.last - 1u));
+      bool spin_now;
+      if (!rare) {
+        p.x = xn;
+        p.y = yn;
+        p.z = zn;
+        if constexpr (!kUniform) {
+          if (lab != p.label) rc = load_rec(m, lab);
+        }
+        p.label = lab;
+        if (m.fhd && inside) atomicAdd(&m.fhd[vi], (unsigned long long)p.weight);
+        spin_now = true;
+      } else {
+        uint32_t new_bulk;
+        uint32_t vr = 0xffffffffu;
+        if (!(mutr != FLT_MAX)) { /* scattering-free voxel */
+          s = MCFL_C(100.0);
+          new_bulk = move_to_first_boundary<false>(p, m, s);
+        } else if (clip) { /* the step reaches a slab face */
+          new_bulk = p.label;
+          if (p.z + s * p.dz < MCFL_C(0.0)) {
+            new_bulk = 0;
+            s = (-p.z) / p.dz;
+          }
+          if (p.z + s * p.dz > m.esp) {
+            new_bulk = m.last;
+            s = (m.esp - p.z) / p.dz;
+          }
+          p.x += p.dx * s;
+          p.y += p.dy * s;
+          p.z += p.dz * s;
+        } else { /* a zero step, a change of refractive index, or a label of the media outside */
+          p.x = xn;
+          p.y = yn;
+          p.z = zn;
+          new_bulk = lab;
+          if (inside) vr = vi;
+        }
+        if (new_bulk != p.label &&
+            reflect(p, n_old, kUniform ? s_lab[2 * new_bulk + 1].w : label_n(m, new_bulk), r)) {
+          p.label = new_bulk;
+          if constexpr (!kUniform) rc = load_rec(m, new_bulk);
+        }
+        if (m.fhd && (vr != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp)))
+          atomicAdd(&m.fhd[vr != 0xffffffffu ? vr : voxel_index(m, p.x, p.y, p.z)], (unsigned long long)p.weight);
+        if (p.label == 0u || p.label == m.last) {
+          const bool top = p.label == 0u;
+          tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+          ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
+          p.weight = 0u;
+          s = MCFL_C(0.0);
+        }
+        spin_now = s > MCFL_C(0.0);
+      }
+      if (spin_now) {
+        const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
+        const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
+        if (w > 0u) {
+          p.weight -= w;
+          absorbed_ph += w;
+        } else {
+          ev_add(MCFL_ST_W0_LOSS, p.weight);
+          p.weight = 0u;
+        }
+        spin(p, c2, r);
+      }
     } else {
     /* ---- one transport pass (MCd3D loop body) ---- */
     real s;
@@ -1165,29 +1291,38 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       spin(p, c2, r);
     }
     }
-    /* PhotonSurvive */
-    if (p.weight <= kWeightRoulette) {
-      if (p.weight == 0u) {
-        alive = false;
-      } else if (r.co() < kChance) {
-        const uint32_t w0 = p.weight;
-        p.weight = MCFL_R2U_RN(MCFL_U2R_RN(p.weight) / kChance);
-        ev_add(MCFL_ST_R_GAIN, (unsigned long long)(p.weight - w0));
-      } else {
-        ev_add(MCFL_ST_R_LOSS, p.weight);
+    /* PhotonSurvive, the pass cap and the photon's end: one branch for the
+     * lean pass (the absorbed weight of the photon, summed in 32 bits since
+     * the last roulette, moves to the launch's 64-bit sum there) */
+    if (!kLean || p.weight <= kWeightRoulette || pst >= L.step_cap) {
+      if (kLean) {
+        absorbed += absorbed_ph;
+        absorbed_ph = 0u;
+      }
+      if (p.weight <= kWeightRoulette) {
+        if (p.weight == 0u) {
+          alive = false;
+        } else if (r.co() < kChance) {
+          const uint32_t w0 = p.weight;
+          p.weight = MCFL_R2U_RN(MCFL_U2R_RN(p.weight) / kChance);
+          ev_add(MCFL_ST_R_GAIN, (unsigned long long)(p.weight - w0));
+        } else {
+          ev_add(MCFL_ST_R_LOSS, p.weight);
+          alive = false;
+        }
+      }
+      if (alive && pst >= L.step_cap) {
+        ev_add(MCFL_ST_CAPPED, 1ull);
         alive = false;
       }
-    }
-    if (alive && pst >= L.step_cap) {
-      ev_add(MCFL_ST_CAPPED, 1ull);
-      alive = false;
-    }
-    if (!alive) {
-      ++done;
-      steps += pst - pst0;
+      if (!alive) {
+        ++done;
+        steps += pst - pst0;
+      }
     }
   }
   if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
+  absorbed += absorbed_ph;         /* the absorbed weight of a parked photon so far */
   if (kPhdAgg && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 
   if (!kUniform && L.max_iters && L.saved) {
@@ -1210,24 +1345,30 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   flush_stats();
 }
 
-/* dynamic shared memory of a launch */
-static size_t smem_bytes(int block, bool uniform) {
-  return (size_t)kEv * block * sizeof(unsigned long long) +
-         (uniform ? (size_t)MCFL_MAX_LABELS * MCFL_LAB_FLOATS * sizeof(real) : 0);
+/* dynamic shared memory of a launch of a kernel variant with kThreads =
+ * threads (the event counters are laid out for the variant's block size) */
+static size_t smem_bytes(int threads, bool uniform) {
+  return lab_bytes(uniform) + (size_t)kEv * threads * sizeof(unsigned long long);
 }
 
 /* Kernel variants.  Single medium (occupancy variants: threads per block x
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner, and 7, 8, 9 the same
- * with the photon-hitting-density sums held in a register; 3 = 256 x 3 carrying
+ * with the photon-hitting-density sums held in a register, 11, 12, 13 the
+ * same with the pass in its per-test branching form; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
  * of flight; voxel-boundary stepping 6 = 256 x 4, 10 = 256 x 3 with the time
  * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
- * -2 = 256 x 2 with the time of flight. */
+ * -5, -6, -7 the same with the per-test branching pass, -2 = 256 x 2 with
+ * the time of flight. */
 typedef void (*TransportKernel)(McflLaunch);
 
-/* Mixed-media occupancy variants: 0 = 256 x 3, 1 = 256 x 4, 2 = 128 x 7. */
-static int mixed_variant_code(uint32_t v) { return v == 1 ? -3 : v == 2 ? -4 : -1; }
+/* Mixed-media occupancy variants: 0 = 256 x 3, 1 = 256 x 4, 2 = 128 x 7;
+ * 3, 4, 5 the same with the pass in its per-test branching form. */
+static int mixed_variant_code(uint32_t v) {
+  static const int code[6] = {-1, -3, -4, -5, -6, -7};
+  return v < 6 ? code[v] : -1;
+}
 
 static TransportKernel kernel_of(int variant, int *threads) {
   switch (variant) {
@@ -1235,6 +1376,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case -1: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 3>;
   case -3: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 4>;
   case -4: *threads = 128; return MCFL_KERNEL_NAME<false, false, 0, 128, 7>;
+  case -5: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 3, false, true>;
+  case -6: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 4, false, true>;
+  case -7: *threads = 128; return MCFL_KERNEL_NAME<false, false, 0, 128, 7, false, true>;
   case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4>;
   case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5>;
   case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9>;
@@ -1246,6 +1390,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case 8: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, true>;
   case 9: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, true>;
   case 10: *threads = 256; return MCFL_KERNEL_NAME<true, true, 2, 256, 3>;
+  case 11: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, false, true>;
+  case 12: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, false, true>;
+  case 13: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, false, true>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -1275,7 +1422,7 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
   memset(&cfg, 0, sizeof(cfg));
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem_bytes(block, L->uniform_medium != 0);
+  cfg.dynamicSmemBytes = smem_bytes(t, L->uniform_medium != 0);
   cfg.stream = stream;
   cudaLaunchAttribute attr[1];
   if (L->l2_bytes) {
@@ -1305,5 +1452,5 @@ extern "C" cudaError_t MCFL_ATTR_FN(int variant, int *block, int *blocks_per_sm,
   if (regs) *regs = a.numRegs;
   if (*block <= 0 || *block > t) *block = t;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void *)fn, *block,
-                                                       smem_bytes(*block, variant >= 0));
+                                                       smem_bytes(t, variant >= 0));
 }

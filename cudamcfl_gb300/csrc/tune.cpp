@@ -5,8 +5,10 @@
  * threads, CUDAMCFL.h:18-20).  The persistent kernel here is compiled in
  * several occupancy variants of the single-medium kernel (threads per block x
  * the blocks per SM the register budget is cut for), each with two forms of
- * the photon-hitting-density tally (one atomic add per pass, or the sums of
- * successive passes in one voxel held in a register), and can put a
+ * the pass (arranged for the SIMT warp, or every test of the reference's
+ * pass as its own branch) and two forms of the photon-hitting-density tally
+ * (one atomic add per pass, or the sums of successive passes in one voxel
+ * held in a register, a form of the branching pass), and can put a
  * persisting L2 access window on the labels and tallies.  Which combination is fastest
  * depends on the medium (how often photons change label, how deep they go)
  * and on the emission/excitation mix, so the tuner times every combination on
@@ -32,18 +34,20 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
     const double f = (double)r.photons / (double)(run->photons ? run->photons : r.photons);
     r.photons_per_voxel = (unsigned)std::max(1.0, (double)run->photons_per_voxel * f);
   }
-  const int old_variant = c->variant, old_l2 = c->l2_window, old_agg = c->phd_agg;
-  int best_v = old_variant, best_l2 = old_l2, best_agg = old_agg;
+  const int old_variant = c->variant, old_l2 = c->l2_window, old_agg = c->phd_agg, old_form = c->pass_form;
+  int best_v = old_variant, best_l2 = old_l2, best_agg = old_agg, best_form = old_form;
   double best = -1.0;
-  /* the form of the photon-hitting-density tally matters only when the run
-   * tallies it */
-  const int n_agg = (r.fluence || r.photons_per_voxel) ? 2 : 1;
+  /* forms: 0 SIMT-arranged pass, 1 branching pass, 2 branching pass with the
+   * register-held hitting density (only when the run tallies it) */
+  const int n_forms = (r.fluence || r.photons_per_voxel) ? 3 : 2;
   for (int v = 0; v < MCFL_N_VARIANTS; ++v) {
-    for (int cfg = 0; cfg < 2 * n_agg; ++cfg) {
-      const int l2 = cfg & 1, agg = cfg >> 1;
+    for (int cfg = 0; cfg < 2 * n_forms; ++cfg) {
+      const int l2 = cfg & 1, form = cfg >> 1;
+      const int agg = form == 2 ? 1 : 0, pass_form = form == 1 ? 1 : 0;
       c->variant = v;
       c->l2_window = l2;
       c->phd_agg = agg;
+      c->pass_form = pass_form;
       double rate = 0.0;
       for (int rep = 0; rep < 3; ++rep) { /* the first run records the graph */
         mcfl_run_out o;
@@ -53,6 +57,7 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
           c->variant = old_variant;
           c->l2_window = old_l2;
           c->phd_agg = old_agg;
+          c->pass_form = old_form;
           return rc;
         }
         const double ms = (double)o.ms_exc + (double)o.ms_fl;
@@ -64,12 +69,14 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
         best_v = v;
         best_l2 = l2;
         best_agg = agg;
+        best_form = pass_form;
       }
     }
   }
   c->variant = best_v;
   c->l2_window = best_l2;
   c->phd_agg = best_agg;
+  c->pass_form = best_form;
   if (variant_out) *variant_out = best_v;
   if (rate_out) *rate_out = best;
   return MCFL_OK;

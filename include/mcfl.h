@@ -330,7 +330,10 @@ const char *mcfl_last_error(void);
  * "l2_window" (1: persisting L2 access window on the labels and tallies),
  * "phd_agg" (1: the single-medium kernel sums a thread's successive passes
  * in one voxel in a register before adding them to the photon hitting
- * density; 0: one atomic add per pass; the tallies are the same).
+ * density; 0: one atomic add per pass; the tallies are the same),
+ * "pass_form" (0: the single-medium pass arranged for the SIMT warp, the
+ * common case straight-line and every rare case behind one branch; 1: every
+ * test of the reference's pass as its own branch; the tallies are the same).
  * The launch shape of the reference is fixed (CUDAMCFL.h:18-20). */
 int mcfl_set_option(mcfl_ctx *ctx, const char *key, long long value);
 long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
@@ -369,12 +372,13 @@ size_t mcfl_medium_bytes(const mcfl_medium *medium);
 /* Builds the medium of a parsed .mci simulation (bulk method 2). */
 int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_medium **medium);
 
-/* Times every kernel variant with and without the L2 window, and (when the
- * run tallies the photon hitting density) with each form of that tally, on a
- * sample of `run` (sample_photons excitation photons, photons_per_voxel
- * scaled by the same fraction) and keeps the fastest in ctx's options
- * ("variant", "l2_window", "phd_agg"); returns the chosen variant and its
- * photons/s.  No counterpart in the reference. */
+/* Times every kernel variant with and without the L2 window, with each form
+ * of the pass, and (when the run tallies the photon hitting density) with
+ * each form of that tally, on a sample of `run` (sample_photons excitation
+ * photons, photons_per_voxel scaled by the same fraction) and keeps the
+ * fastest in ctx's options ("variant", "l2_window", "pass_form",
+ * "phd_agg"); returns the chosen variant and its photons/s.  No counterpart
+ * in the reference. */
 int mcfl_autotune(mcfl_ctx *ctx, const mcfl_medium *medium, const struct mcfl_run_desc *run,
                   unsigned long long sample_photons, int *variant, double *photons_per_s);
 

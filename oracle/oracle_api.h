@@ -40,6 +40,9 @@ typedef struct oracle_result {
    * weights per detector and time bin, index ix + nx*(iy + ny*bin) */
   unsigned long long *time_xyt;
   long time_size;
+  /* reference streams: wall-clock seconds of the excitation phase and of the
+   * emission phase (every emitting voxel) */
+  double seconds_exc, seconds_fl;
 } oracle_result;
 
 /* Parsed method-2 simulation (the fields of SimulationStruct that the
@@ -82,7 +85,7 @@ typedef struct oracle_sim {
   int nx, ny, nz;
   float half_x, half_y;
   float vox_per_cm[3];
-  const float *fluor_map; /* optional emission-strength factor per voxel */
+  const float *fluor_map; /* optional emission-strength factor per voxel (both RNG schemes) */
   long max_fl_voxels;     /* refstream only: stop after this many emitting voxels (0: all) */
   int launch_rng_reuse;   /* photon only: photons 0..32767 of a run (of each voxel) restart their stream
                              after launch, as each reference thread's first photon does */

@@ -53,6 +53,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <thread>
 #include <vector>
 
@@ -1137,7 +1138,10 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
   sk.Rd = res->Rd; sk.Tt = res->Tt; sk.fhd = res->fhd;
   std::vector<float> tpx, tpy;
   setup_time(sim, ph, tpx, tpy, res, sk);
+  const auto t_exc0 = std::chrono::steady_clock::now();
   unsigned long long done = run_threads<M>(ph, sim->number_of_photons, x, a, sk, nthreads, 0);
+  const auto t_exc1 = std::chrono::steady_clock::now();
+  res->seconds_exc = std::chrono::duration<double>(t_exc1 - t_exc0).count();
   res->photons_exc = done;
   res->steps_exc = sk.steps;
   res->balance[0] = sk.absorbed; res->balance[1] = sk.exit_top; res->balance[2] = sk.exit_bottom;
@@ -1147,6 +1151,12 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
 
   if (init_rng_streams(x.data(), a.data(), kThreads, sp, seed_fl)) return -2;
   if (sim->do_fl_sim == 0 || sim->bulk_method != 2) return 0;
+  /* wall-clock of the emission phase, recorded when the voxel loop ends */
+  struct FlClock {
+    oracle_result *res;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    ~FlClock() { res->seconds_fl = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+  } fl_clock{res};
   Phase fl;
   make_phase(sim, fl, 1);
   fl.guard = 1;
@@ -1158,6 +1168,17 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
         unsigned index = ix + ph.num_x * (iy + iz * ph.num_y);
         short bd = sim->bulk_info[index];
         if (!(sim->bulks[bd].albedof < 1)) continue; /* adds 0 * image in the reference */
+        /* With a fluorophore map (an input the reference does not have) a
+         * voxel's weight is also multiplied by its map value, and voxels
+         * whose weight rounds to zero in the engine's fixed point
+         * (rint(w 2^40) = 0) are not simulated, as the engine's emission
+         * list leaves them out; they add nothing to the images.  Without a
+         * map every voxel of a fluorescent label runs, as in the reference. */
+        if (sim->fluor_map) {
+          const double w = (double)sim->bulks[bd].eY * (double)(1 - sim->bulks[bd].albedof) * Fx[index] *
+                           (double)sim->fluor_map[index];
+          if (nearbyint(w * 0x1p40) == 0.0) continue;
+        }
         if (sim->max_fl_voxels > 0 && res->fl_voxels >= sim->max_fl_voxels) return 0;
         float xi = ((float)ix / ph.gx) - ph.hx;
         float yi = ((float)iy / ph.gy) - ph.hy;
@@ -1177,6 +1198,7 @@ int refstream_impl(const oracle_sim *sim, const char *sp, uint64_t seed_exc, uin
         res->photons_fl += st;
         double voxelw = ((double)sim->bulks[bd].eY * (double)(1 - sim->bulks[bd].albedof) * Fx[index]) /
                         (double)(st * 0xFFFFFFFF);
+        if (sim->fluor_map) voxelw *= (double)sim->fluor_map[index];
         for (unsigned ij = 0; ij < xy; ij++) {
           double tempvwR = voxelw * (double)tR[ij];
           double tempvwT = voxelw * (double)tT[ij];

@@ -48,6 +48,8 @@ class CResult(ctypes.Structure):
         ("steps_fl", ctypes.c_ulonglong),
         ("time_xyt", u64p),
         ("time_size", ctypes.c_long),
+        ("seconds_exc", ctypes.c_double),
+        ("seconds_fl", ctypes.c_double),
     ]
 
 
@@ -142,6 +144,8 @@ class Result:
     steps_exc: int
     steps_fl: int
     time_xyt: np.ndarray | None = None  # uint64, index ix + nx*(iy + ny*bin)
+    seconds_exc: float = 0.0  # reference streams: wall-clock of the excitation phase
+    seconds_fl: float = 0.0   # reference streams: wall-clock of the emission phase
 
 
 def _to_result(lib, r: CResult) -> Result:
@@ -163,7 +167,7 @@ def _to_result(lib, r: CResult) -> Result:
         flR128=None if not r.flR128 else arr(r.flR128, 2 * xy, np.uint64).reshape(xy, 2),
         flT128=None if not r.flT128 else arr(r.flT128, 2 * xy, np.uint64).reshape(xy, 2),
         balance=tuple(r.balance), steps_exc=r.steps_exc, steps_fl=r.steps_fl,
-        time_xyt=arr(r.time_xyt, r.time_size, np.uint64),
+        time_xyt=arr(r.time_xyt, r.time_size, np.uint64), seconds_exc=r.seconds_exc, seconds_fl=r.seconds_fl,
     )
     lib.oracle_free_result(ctypes.byref(r))
     return out

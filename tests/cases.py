@@ -28,6 +28,8 @@ class Case:
     temporal: tuple | None = None
     # 1: voxel-boundary stepping in both the oracle and the engine
     exact_stepping: int = 0
+    # optional per-voxel emission-strength factor (nz, ny, nx) float32, in both engines
+    fluor_map: np.ndarray | None = None
 
     @property
     def dims(self):
@@ -66,7 +68,11 @@ class Case:
         s.start_weight = self.start_weight()
         lab = np.ascontiguousarray(self.labels.astype(np.int16))
         s.bulk_info = lab.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_short))
-        s._keep = lab
+        s._keep = [lab]
+        if self.fluor_map is not None:
+            fm = np.ascontiguousarray(self.fluor_map, dtype=np.float32)
+            s.fluor_map = fm.ctypes.data_as(pyoracle.ctypes.POINTER(pyoracle.ctypes.c_float))
+            s._keep.append(fm)
         s.exact_stepping = self.exact_stepping
         if self.temporal:
             x0, y0, tnx, tny, sx, sy, r, face, bins, tmax = self.temporal
@@ -80,7 +86,8 @@ class Case:
         nx, ny, nz = self.dims
         e = np.float32(self.esp)
         return ctx.medium(self.labels, self.bulks(), vox_per_cm=(float(self.grid),) * 3,
-                          half_x=float(np.float32(2) * e), half_y=float(np.float32(2) * e), thickness=float(e))
+                          half_x=float(np.float32(2) * e), half_y=float(np.float32(2) * e), thickness=float(e),
+                          fluor_map=self.fluor_map)
 
     def run_desc(self, seed_exc, seed_fl, photons=None):
         dx, dy, nx, ny, x0, y0 = self.det
@@ -115,6 +122,58 @@ class Case:
         with open(path, "w") as f:
             f.write("\n".join(lines) + "\n")
         return path
+
+
+def nearest_emitters(labels, bulks, voxel_cm, point, k):
+    """Linear indices (x fastest) of the k voxels of fluorescent labels
+    (albedof < 1) whose centres lie nearest to point (x, y, z in cm; the grid
+    is centred on x = y = 0 and starts at z = 0), nearest first."""
+    nz, ny, nx = labels.shape
+    fluorescent = np.array([b.albedof < 1 for b in bulks])
+    iz, iy, ix = np.nonzero(fluorescent[labels])
+    x = (ix + 0.5) * voxel_cm[0] - nx * voxel_cm[0] / 2
+    y = (iy + 0.5) * voxel_cm[1] - ny * voxel_cm[1] / 2
+    z = (iz + 0.5) * voxel_cm[2]
+    d = (x - point[0]) ** 2 + (y - point[1]) ** 2 + (z - point[2]) ** 2
+    order = np.argsort(d, kind="stable")[:k]
+    return (ix + nx * (iy + ny * iz))[order]
+
+
+def emitter_map(shape, voxels, values=None):
+    """A fluorophore map that is zero except at the given linear voxel
+    indices (1 there, or the given values): the emission phase then runs
+    exactly those voxels, in both engines, while the excitation medium is
+    unchanged (the map scales only the emission weights)."""
+    m = np.zeros(shape, dtype=np.float32)
+    m.ravel()[voxels] = 1.0 if values is None else values
+    return m
+
+
+def config1_parity(photons=1_250_000, per_voxel=33000, emitters=6) -> Case:
+    """The reference-expressible variant of the config-1 sphere medium: esp
+    = 2, grid_size = 25, i.e. 200 x 200 x 50 voxels of 0.04 cm over 8 x 8 x 2
+    cm (the reference fixes the lateral extent to 4 esp and cubic voxels);
+    background n 1.4 in air, mu_a 0.1, mu_s 100, g 0.9; a fluorescent sphere
+    r = 0.25 cm at the slab centre (fluorophore absorption 0.05/cm at both
+    wavelengths, quantum yield 0.1; the reference keeps mu_s at emission);
+    Gaussian beam at the top centre; 100 x 100 images of 0.04 cm.  The
+    emission phase runs the `emitters` sphere voxels nearest the top of the
+    sphere (a fluorophore map of ones there, zero elsewhere), since the
+    reference's schedule costs at least 32768 photons per voxel."""
+    esp, grid = 2.0, 25
+    lab = _labels(esp, grid)
+    nz, ny, nx = lab.shape
+    z = (np.arange(nz) + 0.5) / grid
+    y = (np.arange(ny) + 0.5) / grid - 2 * esp
+    x = (np.arange(nx) + 0.5) / grid - 2 * esp
+    m = (x[None, None, :] ** 2 + y[None, :, None] ** 2 + (z[:, None, None] - 1.0) ** 2) <= 0.25 ** 2
+    lab[m] = 2
+    c = Case("config1_parity", esp, grid, lab,
+             [(1.4, 0.1, 100.0, 0.0, 0.0, 0.0, 0.0, 0.9), (1.4, 0.1, 100.0, 1.0, 0.05, 0.05, 0.1, 0.9)],
+             1.0, photons, per_voxel, (0.04, 0.04, 100, 100, 0.0, 0.0))
+    v = nearest_emitters(lab, c.bulks(), (1 / grid,) * 3, (0.0, 0.0, 0.75), emitters)
+    c.fluor_map = emitter_map(lab.shape, v)
+    return c
 
 
 def _labels(esp, grid, fill=1):

@@ -1,0 +1,193 @@
+"""The benchmarked kernel against the reference's own algorithm on the
+benchmark's media.
+
+The benchmark times the fast-math kernel (hardware SFU intrinsics, the
+numerics of the reference's own GPU build) on the voxelized heterogeneous
+medium.  Here that kernel — and the exact-math one beside it — is compared
+with the oracle's reference-stream restatement (the reference's 32768
+per-thread MWC streams, relaunch schedule and C-library math; bit-identical
+to the reference's transport built for the host) on
+  (a) the reference-expressible variant of the config-1 sphere medium (esp 2,
+      grid_size 25: 200 x 200 x 50 voxels, r = 0.25 cm fluorescent sphere,
+      Gaussian beam), 16 x 1.25e6 reference photons; and
+  (b) the config-2 medium itself (200 x 200 x 100 voxels of 0.02 cm, 8
+      labels, seeded spheres and cylinders, its fp32 fluorophore map),
+      16 x 1e6 reference photons,
+with the reference's first-photon random-number reuse reproduced in the
+engine.  The emission phase runs the fluorescent voxels nearest the beam (a
+fluorophore map zero elsewhere; the reference's schedule costs at least 32768
+photons per emitting voxel) with 33000 photons each, through the engine's
+batched emission job, the benchmarked path.
+
+Gates (tests/stats.py): per pixel of the excitation R/T images and the
+emission images, and per voxel of the photon hitting density (a block of 1.2
+x 1.2 cm around the beam, all depths), within 3 sigma of the batch-means
+standard error; integrated reflectance, transmittance and absorbed fraction
+within 3 sigma, and within 0.1 % wherever the budget resolves 0.1 % (the
+test asserts that 3 sigma of the difference is below 0.1 % for R and the
+absorbed fraction; for the transmittance, 2 % of the light at 2 cm, the
+difference's 3 sigma is about 0.2 % at this budget, so it is held to 3 sigma).
+Each engine batch is the mean of 8 runs of the reference batch's photon
+count (the same share of first photons), so the engine's side of the
+standard error is small beside the reference's.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import cudamcfl_gb300 as mc
+from oracle import pyoracle
+from tests import cases, stats
+
+B = 16
+RUNS_PER_BATCH = 8
+PER_VOXEL = 33000
+
+
+def _crop(shape, voxel_cm, half_cm=0.6):
+    """Slices of the (nz, ny, nx) voxels within half_cm of the beam axis."""
+    nz, ny, nx = shape
+    sl = []
+    for n, d in ((ny, voxel_cm[1]), (nx, voxel_cm[0])):
+        i0 = int(np.floor((n * d / 2 - half_cm) / d))
+        i1 = int(np.ceil((n * d / 2 + half_cm) / d))
+        sl.append(slice(max(i0, 0), min(i1, n)))
+    return (slice(0, nz), sl[0], sl[1])
+
+
+def _reduce(r, xy, shape, crop, w0, engine):
+    """What the gates need from one run, per photon: the images, the hitting
+    density in the block around the beam, the emission images (normalised on
+    the GPU by the engine, on the host by the oracle) and the integrated
+    fractions (absorbed, exit top, exit bottom)."""
+    n = r.stats_exc["done"] if engine else r.photons_exc
+    out = {"Rd": r.Rd[:xy] / n, "Tt": r.Tt[:xy] / n,  # the image's nx * ny pixels
+           "fhd": r.fhd.reshape(shape)[crop].ravel() / n,
+           "flR": np.array(r.flR[:xy], dtype=np.float64), "flT": np.array(r.flT[:xy], dtype=np.float64)}
+    if engine:
+        out["frac"] = [r.stats_exc[k] / (n * w0) for k in ("absorbed", "exit_top", "exit_bottom")]
+    else:
+        out["frac"] = [r.balance[i] / (n * w0) for i in range(3)]
+    return out
+
+
+def _compare(eng, ref, det_shape):
+    """eng, ref: per batch the reduced per-photon tallies (the engine's a
+    mean of its runs)."""
+    summary = {}
+    for k in ("Rd", "Tt", "fhd", "flR", "flT"):
+        a = np.stack([e[k] for e in eng])
+        b = np.stack([x[k] for x in ref])
+        summary[k] = stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=det_shape if k in ("Rd", "Tt") else None)
+    for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
+        out = stats.scalar_gate([e["frac"][i] for e in eng], [x["frac"][i] for x in ref])
+        if k != "exit_bottom":
+            assert 3 * out["sigma"] / out["b"] < 1e-3, ("0.1 % not resolved", k, out)
+            assert out["rel_diff"] < 1e-3, (k, out)
+        summary[k] = out
+    return summary
+
+
+def _engine_batches(ctx, med, rd_of, reduce):
+    eng = []
+    for b in range(B):
+        runs = [reduce(ctx.run(med, rd_of(b, j))) for j in range(RUNS_PER_BATCH)]
+        eng.append({k: (np.mean([r[k] for r in runs], axis=0)) for k in runs[0]})
+    return eng
+
+
+def _config1():
+    case = cases.config1_parity(photons=1_250_000, per_voxel=PER_VOXEL, emitters=6)
+    det = case.det
+    nx, ny, nz = case.dims
+    shape = (nz, ny, nx)
+    return case, det[2] * det[3], shape, _crop(shape, (1 / case.grid,) * 3), case.start_weight()
+
+
+@pytest.fixture(scope="module")
+def config1_reference(oracle, safeprimes_file):
+    """The reference-stream batches of the config-1 parity variant (shared by
+    both kernels' tests)."""
+    nthreads = os.cpu_count() or 1
+    case, xy, shape, crop, w0 = _config1()
+    sim = case.oracle_sim()
+    ref = []
+    for b in range(B):
+        r = oracle.run_refstream(sim, safeprimes_file, 31_000 + b, 32_000 + b, libm=True, nthreads=nthreads)
+        assert r.fl_voxels == 6
+        ref.append(_reduce(r, xy, shape, crop, w0, engine=False))
+    return ref
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("math", [mc.MATH_FAST, mc.MATH_EXACT])
+def test_config1_parity_variant_agrees_with_reference_streams(math, config1_reference):
+    case, xy, shape, crop, w0 = _config1()
+    det = case.det
+    ref = config1_reference
+    ctx = mc.Context(math=math)
+    try:
+        med = case.engine_medium(ctx)
+
+        def rd_of(b, j):
+            rd = case.run_desc(50_000 + 97 * b + j, 60_000 + 97 * b + j)
+            rd.launch_rng_reuse = 1
+            return rd
+
+        def reduce(r):
+            assert r.fl_voxels == 6
+            return _reduce(r, xy, shape, crop, w0, engine=True)
+
+        eng = _engine_batches(ctx, med, rd_of, reduce)
+        med.free()
+    finally:
+        ctx.close()
+    _compare(eng, ref, (det[3], det[2]))
+
+
+@pytest.mark.gpu
+def test_config2_medium_agrees_with_reference_streams(oracle, safeprimes_file):
+    """The benchmark's own medium and its fluorophore map, fast-math kernel."""
+    from cudamcfl_gb300 import media
+    nthreads = os.cpu_count() or 1
+    m = media.config2(seed=2)
+    nz, ny, nx = m.labels.shape
+    vc = m.voxel_cm
+    vox = cases.nearest_emitters(m.labels, m.bulks, vc, (0.0, 0.0, 0.0), 4)
+    fmap = cases.emitter_map(m.labels.shape, vox, m.fluor_map.ravel()[vox])
+    assert np.all(fmap.ravel()[vox] > 0)
+    photons = 1_000_000
+    n1, n2 = np.float64(np.float32(m.bulks[0].n)), np.float64(np.float32(m.bulks[1].n))
+    w0 = int(np.float64(0xFFFFFFFF) * (1 - ((n1 - n2) / (n1 + n2)) ** 2))
+    d = m.det
+    det = (d.dx, d.dy, d.nx, d.ny, d.x0, d.y0)
+    sim = pyoracle.sim_from_arrays(
+        m.labels, m.bulks, half_x=float(np.float32(nx * vc[0] / 2)), half_y=float(np.float32(ny * vc[1] / 2)),
+        thickness=float(np.float32(nz * vc[2])), vox_per_cm=[float(np.float32(1 / v)) for v in vc],
+        photons=photons, per_voxel=PER_VOXEL, det=det, fluor_map=fmap, start_weight=w0, do_fl=1)
+    xy = d.nx * d.ny
+    shape = (nz, ny, nx)
+    crop = _crop(shape, vc)
+    ref = []
+    for b in range(B):
+        r = oracle.run_refstream(sim, safeprimes_file, 41_000 + b, 42_000 + b, libm=True, nthreads=nthreads)
+        assert r.fl_voxels == 4
+        ref.append(_reduce(r, xy, shape, crop, w0, engine=False))
+    ctx = mc.Context(math=mc.MATH_FAST)
+    try:
+        med = ctx.medium(m.labels, m.bulks, voxel_cm=vc, fluor_map=fmap)
+
+        def rd_of(b, j):
+            return mc.run_desc(photons, det=d, photons_per_voxel=PER_VOXEL, fluence=1, seed_exc=70_000 + 97 * b + j,
+                               seed_fl=80_000 + 97 * b + j, start_weight=w0, launch_rng_reuse=1)
+
+        def reduce(r):
+            assert r.fl_voxels == 4
+            return _reduce(r, xy, shape, crop, w0, engine=True)
+
+        eng = _engine_batches(ctx, med, rd_of, reduce)
+        med.free()
+    finally:
+        ctx.close()
+    _compare(eng, ref, (d.ny, d.nx))

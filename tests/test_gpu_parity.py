@@ -65,13 +65,15 @@ def test_exact_kernel_launch_shape_does_not_change_tallies(gpu_ctx, oracle, tabl
         gpu_ctx.set_option("block", 256)
         gpu_ctx.set_option("blocks_per_sm", 0)
         # every occupancy variant, with and without the persisting-L2 window,
-        # with either form of the photon-hitting-density tally
+        # with either form of the photon-hitting-density tally and either
+        # form of the pass (SIMT-arranged, per-test branching)
         for variant, bound in ((0, 256), (1, 256), (2, 128)):
             for l2 in (0, 1):
-                for agg in (0, 1):
+                for agg, form in ((0, 0), (0, 1), (1, 0)):
                     gpu_ctx.set_option("variant", variant)
                     gpu_ctx.set_option("l2_window", l2)
                     gpu_ctx.set_option("phd_agg", agg)
+                    gpu_ctx.set_option("pass_form", form)
                     assert gpu_ctx.get_option("launch_block") == bound
                     _compare(gpu_ctx.run(med, case.run_desc(5, 6)), ref)
     finally:
@@ -80,6 +82,7 @@ def test_exact_kernel_launch_shape_does_not_change_tallies(gpu_ctx, oracle, tabl
         gpu_ctx.set_option("variant", 0)
         gpu_ctx.set_option("l2_window", 0)
         gpu_ctx.set_option("phd_agg", 0)
+        gpu_ctx.set_option("pass_form", 0)
 
 
 @pytest.mark.gpu
@@ -94,11 +97,13 @@ def test_autotune_keeps_a_variant_and_tallies(gpu_ctx, oracle, table32768):
         assert variant in (0, 1, 2) and rate > 0
         assert gpu_ctx.get_option("variant") == variant
         assert gpu_ctx.get_option("phd_agg") in (0, 1)
+        assert gpu_ctx.get_option("pass_form") in (0, 1)
         _compare(gpu_ctx.run(med, case.run_desc(8, 9)), ref)
     finally:
         gpu_ctx.set_option("variant", 0)
         gpu_ctx.set_option("l2_window", 0)
         gpu_ctx.set_option("phd_agg", 0)
+        gpu_ctx.set_option("pass_form", 0)
 
 
 @pytest.mark.gpu

@@ -527,7 +527,8 @@ def batch_run(ctx: "Context", medium, runs: list, schedule: int = SCHEDULE_BATCH
               images: bool = True):
     """Runs excitation-only simulations on one medium, or on a medium each
     when `medium` is a list (one per run).  Returns (list of dicts with Rd,
-    Tt, R, T, stats; GPU ms)."""
+    Tt, R, T, stats, and time_xyt for runs with time-resolved detectors;
+    GPU ms)."""
     n = len(runs)
     arr = (RunDesc * n)(*runs)
     outs = (RunOut * n)()
@@ -535,6 +536,10 @@ def batch_run(ctx: "Context", medium, runs: list, schedule: int = SCHEDULE_BATCH
     for i, r in enumerate(runs):
         xy = r.det.nx + r.det.nx * r.det.ny
         o, k = _alloc_out(xy, images=images)
+        if r.tdet.nx:
+            t = np.zeros(r.tdet.nx * r.tdet.ny * r.tdet.bins, dtype=np.uint64)
+            o.time_xyt = u64ptr(t)
+            k["time_xyt"] = t
         outs[i] = o
         keeps.append(k)
     ms = ctypes.c_float()
@@ -587,15 +592,18 @@ class Server:
         check(load().mcfl_server_submit(self.handle, ctypes.byref(d), ctypes.byref(rd), ctypes.byref(rid)))
         self._keep[rid.value] = (d, keep, rd)
         self._shape[rid.value] = (rd.det.nx + rd.det.nx * rd.det.ny, int(np.prod(np.shape(labels))),
-                                  bool(rd.fluence))
+                                  bool(rd.fluence), rd.tdet.nx * rd.tdet.ny * rd.tdet.bins if rd.tdet.nx else 0)
         return rid.value
 
     def wait(self, rid: int, timeout_ms: int = -1) -> int:
         return int(load().mcfl_server_wait(self.handle, rid, timeout_ms))
 
     def result(self, rid: int):
-        xy, nv, fl = self._shape[rid]
+        xy, nv, fl, tsize = self._shape[rid]
         out, keep = _alloc_out(xy, nv, images=False, fluence=fl)
+        if tsize:
+            keep["time_xyt"] = np.zeros(tsize, dtype=np.uint64)
+            out.time_xyt = u64ptr(keep["time_xyt"])
         lat = ctypes.c_double()
         check(load().mcfl_server_result(self.handle, rid, ctypes.byref(out), ctypes.byref(lat)))
         self._keep.pop(rid, None)

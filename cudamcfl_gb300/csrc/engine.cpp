@@ -76,7 +76,9 @@ int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool 
   *regs = 0;
   static const int mixed_codes[6] = {-1, -3, -4, -5, -6, -7};
   const int mixed = mixed_codes[mixed_code()];
-  const int v = exact ? (time ? 10 : 6) : uniform ? (time ? 3 : variant_code()) : (time ? -2 : mixed);
+  const int v = exact ? (uniform ? (time ? 10 : 6) : (time ? -9 : -8))
+                : uniform ? (time ? 3 : variant_code())
+                          : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
@@ -170,7 +172,8 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
     if (v < 0 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant: 0..2");
     c->variant = (int)v;
   } else if (k == "phd_agg") {
-    c->phd_agg = v ? 1 : 0;
+    if (v < 0 || v > 2) return fail(MCFL_E_ARG, "phd_agg: 0 (one add per pass), 1 (register sums), 2 (warp sums)");
+    c->phd_agg = (int)v;
   } else if (k == "pass_form") {
     c->pass_form = v ? 1 : 0;
   } else if (k == "mixed_variant") {

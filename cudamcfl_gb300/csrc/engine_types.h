@@ -86,6 +86,10 @@ typedef struct MCFL_ALIGN(16) McflJob {
   uint64_t ticket_begin; /* first global ticket */
   uint64_t photon_base;  /* job photon index of ticket_begin (a server slice hands out a job's photons in parts) */
   uint64_t photons;      /* photons in the job */
+  /* voxel-boundary stepping in a mixed-media launch: the medium's label |
+   * free radius << 8 per voxel (McflMedium::lab16 of a single-medium launch) */
+  const uint16_t *lab16;
+  uint64_t pad_j;
 } McflJob;
 
 /* Photon state carried between slices of a budgeted launch. */
@@ -99,6 +103,14 @@ typedef struct MCFL_ALIGN(16) McflSaved {
   uint32_t alive;
   uint32_t src_idx;  /* voxel-list entry (MCFL_SRC_VOXELS) */
   uint32_t pad;
+  uint64_t tof;      /* time of flight [fs] (time-of-flight launches) */
+  /* voxel-boundary stepping: the pass in progress (remaining optical depth,
+   * ray origin, start of the label run), the photon's voxel, the free
+   * radius and segment count, and flags (1: a pass in progress, 2: its
+   * origin is to be set) */
+  float xtau, xox, xoy, xoz, xs0;
+  int32_t ix, iy, iz, xcr, xit;
+  uint32_t xflags;
 } McflSaved;
 
 /* Per-label constants of the transport, derived once from

@@ -91,6 +91,10 @@ constexpr int MCFL_N_VARIANTS = 3;
 int run_single_voxel_emission(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run, unsigned int voxel,
                               unsigned long long *R, unsigned long long *T, unsigned long long *stats);
 
+/* run.cpp: the label + free-radius map of voxel-boundary stepping, built on
+ * the medium's first such run (synchronously on the context's stream) */
+int ensure_free_map(mcfl_ctx *c, const mcfl_medium *m);
+
 /* mci.cpp */
 void simulation_geometry(const mcfl_simulation *sim, float *half_x, float *half_y, float *esp, float *g);
 /* Detector-array positions of time-resolved detectors, as the reference
@@ -160,10 +164,12 @@ struct mcfl_ctx {
   int math = MCFL_MATH_EXACT;
   int block = 256;   /* threads per block, clamped to the variant's bound */
   int variant = 0;   /* occupancy variant of the single-medium kernel */
-  int phd_agg = 0;   /* 1: photon-hitting-density sums held in a register (kernel variants 7..9) */
+  /* photon-hitting-density tally: 0 one add per pass, 1 sums held in a
+   * register (kernel variants 7..9), 2 adds aggregated per warp (14..16) */
+  int phd_agg = 0;
   int pass_form = 0; /* 1: the pass with every test as its own branch (kernel variants 11..13) */
   /* the single-medium kernel variant the launches use */
-  int variant_code() const { return variant + (phd_agg ? 7 : pass_form ? 11 : 0); }
+  int variant_code() const { return variant + (phd_agg == 1 ? 7 : phd_agg == 2 ? 14 : pass_form ? 11 : 0); }
   int mixed_variant = 2; /* occupancy variant of the mixed-media kernel (128 x 7 measured fastest) */
   /* the mixed-media kernel variant the launches use (McflLaunch::variant) */
   int mixed_code() const { return mixed_variant + (pass_form ? 3 : 0); }

@@ -40,6 +40,7 @@ unsigned int default_start_weight(const mcfl_medium *m) {
  * fluorophore's absorption at the phase's wavelength) */
 void fill_medium(McflJob &j, const mcfl_medium *m, bool emission, bool exact = false) {
   j.labels = m->labels.as<uint8_t>();
+  j.lab16 = exact ? m->lab16.as<uint16_t>() : nullptr; /* built by ensure_free_map */
   j.prop = m->prop_of(emission, exact);
   j.lab = m->lab_of(emission, exact);
   j.hx = m->hx;
@@ -82,23 +83,6 @@ void fill_source(McflJob &j, const mcfl_run_desc &r, const mcfl_medium *m) {
       }
 }
 
-/* The free-radius map of voxel-boundary stepping, built on the medium's
- * first such run (synchronously, before any recorded graph uses it). */
-int ensure_free_map(mcfl_ctx *c, const mcfl_medium *m) {
-  if (m->lab16.p) return MCFL_OK;
-  const size_t n = (size_t)m->total;
-  mcfl::DevBuf tmp;
-  MCFL_CUDA_TRY(tmp.reserve(2 * n));
-  MCFL_CUDA_TRY(m->lab16.reserve(2 * n));
-  cudaError_t e = mcfl_launch_free_map(m->labels.as<uint8_t>(), m->nx, m->ny, m->nz, tmp.as<uint8_t>(),
-                                       m->lab16.as<uint16_t>(), c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) {
-    m->lab16.release();
-    return cuda_fail(e, "free-radius map");
-  }
-  return MCFL_OK;
-}
 
 int check_run(const mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *run) {
   if (!c || !m || !run) return fail(MCFL_E_ARG, "null argument");
@@ -275,6 +259,24 @@ void set_uniform(const mcfl_ctx *c, McflLaunch &L, const mcfl_medium *m, bool em
 }
 
 } // namespace
+
+/* The free-radius map of voxel-boundary stepping, built on the medium's
+ * first such run (synchronously, before any recorded graph uses it). */
+int mcfl::ensure_free_map(mcfl_ctx *c, const mcfl_medium *m) {
+  if (m->lab16.p) return MCFL_OK;
+  const size_t n = (size_t)m->total;
+  mcfl::DevBuf tmp;
+  MCFL_CUDA_TRY(tmp.reserve(2 * n));
+  MCFL_CUDA_TRY(m->lab16.reserve(2 * n));
+  cudaError_t e = mcfl_launch_free_map(m->labels.as<uint8_t>(), m->nx, m->ny, m->nz, tmp.as<uint8_t>(),
+                                       m->lab16.as<uint16_t>(), c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    m->lab16.release();
+    return cuda_fail(e, "free-radius map");
+  }
+  return MCFL_OK;
+}
 
 /* ------------------------------------------------------------------ run */
 
@@ -508,22 +510,25 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
   for (int i = 0; i < n; ++i)
     if ((runs[i].exact_stepping != 0) != exact)
       return fail(MCFL_E_ARG, "mcfl_batch_run: the runs of a batch share the stepping");
-  if (exact && !uniform) return fail(MCFL_E_ARG, "mcfl_batch_run: exact stepping over one medium only");
   for (int i = 0; i < n; ++i) {
     if (!media[i]) return fail(MCFL_E_ARG, "mcfl_batch_run: null medium");
     if (!uniform && media[i]->layered)
       return fail(MCFL_E_ARG, "mcfl_batch_run: layered media batch with their own medium only");
     int rc = check_run(c, media[i], &runs[i]);
     if (rc) return rc;
-    if (runs[i].photons_per_voxel || runs[i].fluence || runs[i].tdet.nx)
-      return fail(MCFL_E_ARG, "mcfl_batch_run: excitation images only (no fluence, emission or time detectors)");
+    if (runs[i].photons_per_voxel || runs[i].fluence)
+      return fail(MCFL_E_ARG, "mcfl_batch_run: excitation images and time detectors only (no fluence or emission)");
+    if (runs[i].tdet.nx && media[i]->layered && !uniform)
+      return fail(MCFL_E_ARG, "mcfl_batch_run: time detectors on layered media batch with their own medium only");
     const mcfl_detector &d = runs[i].det;
     if (d.nx != det.nx || d.ny != det.ny) return fail(MCFL_E_ARG, "mcfl_batch_run: detectors must share a size");
   }
   if (exact) {
     MCFL_CUDA_TRY(cudaSetDevice(c->device));
-    const int rcm = ensure_free_map(c, m);
-    if (rcm != MCFL_OK) return rcm;
+    for (int i = 0; i < n; ++i) {
+      const int rcm = ensure_free_map(c, media[i]);
+      if (rcm != MCFL_OK) return rcm;
+    }
   }
   MCFL_CUDA_TRY(cudaSetDevice(c->device));
   cudaGetLastError();
@@ -536,6 +541,24 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
   MCFL_CUDA_TRY(c->bcnt.reserve(N * 8 + 8));
   MCFL_CUDA_TRY(c->jobs.reserve(N * sizeof(McflJob) + sizeof(McflJob)));
   MCFL_CUDA_TRY(ensure_pinned(c, N, N * MCFL_ST_COUNT + N + 8));
+  /* time-resolved detectors: each timed run's histogram and disc positions
+   * at its own offset in one buffer */
+  std::vector<size_t> toff(N + 1, 0), poff(N + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    const mcfl_time_detectors &td = runs[i].tdet;
+    toff[i + 1] = toff[i] + (td.nx ? (size_t)td.nx * td.ny * td.bins : 0);
+    poff[i + 1] = poff[i] + (td.nx ? (size_t)(td.nx + td.ny) : 0);
+  }
+  const size_t tsize = toff[N];
+  const bool timed = tsize > 0;
+  if (timed) {
+    MCFL_CUDA_TRY(c->tarr.reserve(tsize * 8));
+    MCFL_CUDA_TRY(c->tpos.reserve(poff[N] * 4));
+    std::vector<float> pos(poff[N]);
+    for (int i = 0; i < n; ++i)
+      if (runs[i].tdet.nx) time_positions(runs[i].tdet, pos.data() + poff[i], pos.data() + poff[i] + runs[i].tdet.nx);
+    MCFL_CUDA_TRY(cudaMemcpyAsync(c->tpos.p, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice, s));
+  }
   McflJob *jobs = c->h_jobs;
   std::memset(jobs, 0, N * sizeof(McflJob));
   unsigned long long tickets = 0;
@@ -553,10 +576,22 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
     j.ticket_begin = schedule == MCFL_SCHEDULE_BATCHED ? tickets : 0;
     j.photons = runs[i].photons;
     tickets += runs[i].photons;
+    const mcfl_time_detectors &td = runs[i].tdet;
+    if (td.nx) {
+      j.time_on = 1;
+      j.tpos_x = c->tpos.as<float>() + poff[i];
+      j.tpos_y = c->tpos.as<float>() + poff[i] + td.nx;
+      j.time_xyt = c->tarr.as<unsigned long long>() + toff[i];
+      j.tmax = td.max_fs;
+      j.tdet_r = td.radius;
+      j.tnx = (uint32_t)td.nx;
+      j.tny = (uint32_t)td.ny;
+      j.tbins = (uint32_t)td.bins;
+      j.tdet_face = (uint32_t)td.face;
+    }
   }
   int block = 0, block_one = 0;
-  const int grid = c->grid_for(uniform, &block, nullptr, false, exact);
-  const int grid_one = c->grid_for(true, &block_one, nullptr, false, exact); /* plain schedule: one medium per launch */
+  const int grid = c->grid_for(uniform, &block, nullptr, timed, exact);
   float ms = 0.f;
   if (schedule == MCFL_SCHEDULE_BATCHED) {
     auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -565,6 +600,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       if ((e = cudaMemsetAsync(c->bT.p, 0, N * xy * 8, st))) return e;
       if ((e = cudaMemsetAsync(c->bstats.p, 0, N * MCFL_ST_COUNT * 8, st))) return e;
       if ((e = cudaMemsetAsync(c->bcnt.p, 0, 8, st))) return e;
+      if (timed && (e = cudaMemsetAsync(c->tarr.p, 0, tsize * 8, st))) return e;
       if ((e = cudaMemcpyAsync(c->jobs.p, c->h_jobs, N * sizeof(McflJob), cudaMemcpyHostToDevice, st))) return e;
       McflLaunch L = base_launch(c);
       L.jobs = c->jobs.as<McflJob>();
@@ -574,6 +610,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       if (uniform) set_uniform(c, L, m, false, nullptr, exact);
       else L.variant = (uint32_t)c->mixed_code();
       L.exact_step = exact ? 1u : 0u;
+      L.time_on = timed ? 1u : 0u;
       if ((e = record_event(c->ev[0], st))) return e;
       if ((e = launch_fn(c->math)(&L, grid, block, st)))
         return e;
@@ -582,10 +619,12 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       return cudaMemcpyAsync(c->h_out, c->bstats.p, N * MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, st);
     };
     std::string key =
-        ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s},
+        ptr_key({m, c->bR.p, c->bT.p, c->bstats.p, c->bcnt.p, c->jobs.p, c->h_jobs, c->h_out, (const void *)s,
+                 timed ? c->tarr.p : nullptr},
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
                  c->step_cap, (unsigned long long)c->variant_code(), (unsigned long long)c->l2_window,
-                 (unsigned long long)uniform, (unsigned long long)exact, m->serial});
+                 (unsigned long long)uniform, (unsigned long long)exact, m->serial, tsize,
+                 (unsigned long long)c->mixed_code()});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
@@ -595,9 +634,13 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
     MCFL_CUDA_TRY(cudaMemsetAsync(c->bT.p, 0, N * xy * 8, s));
     MCFL_CUDA_TRY(cudaMemsetAsync(c->bstats.p, 0, N * MCFL_ST_COUNT * 8, s));
     MCFL_CUDA_TRY(cudaMemsetAsync(c->bcnt.p, 0, N * 8, s));
+    if (timed) MCFL_CUDA_TRY(cudaMemsetAsync(c->tarr.p, 0, tsize * 8, s));
     MCFL_CUDA_TRY(cudaMemcpyAsync(c->jobs.p, c->h_jobs, N * sizeof(McflJob), cudaMemcpyHostToDevice, s));
     MCFL_CUDA_TRY(cudaEventRecord(c->ev[0], s));
     for (int i = 0; i < n; ++i) {
+      /* plain schedule: one medium per launch */
+      const bool timed_i = runs[i].tdet.nx > 0;
+      const int grid_one = c->grid_for(true, &block_one, nullptr, timed_i, exact);
       McflLaunch L = base_launch(c);
       L.jobs = c->jobs.as<McflJob>() + i;
       L.n_jobs = 1;
@@ -605,6 +648,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       L.ticket_end = runs[i].photons;
       set_uniform(c, L, media[i], false, nullptr, exact);
       L.exact_step = exact ? 1u : 0u;
+      L.time_on = timed_i ? 1u : 0u;
       MCFL_CUDA_TRY(c->launch_transport(L, grid_one, block_one));
       MCFL_CUDA_TRY(cudaStreamSynchronize(s)); /* one simulation per call, as DoOneSimulation */
     }
@@ -638,6 +682,9 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
       if (o.Tt) MCFL_CUDA_TRY(cudaMemcpyAsync(o.Tt, c->bT.as<unsigned long long>() + i * xy, xy * 8, cudaMemcpyDeviceToHost, s));
       if (o.R) MCFL_CUDA_TRY(cudaMemcpyAsync(o.R, c->outd.as<double>() + i * xy, xy * 8, cudaMemcpyDeviceToHost, s));
       if (o.T) MCFL_CUDA_TRY(cudaMemcpyAsync(o.T, c->outd.as<double>() + (N + i) * xy, xy * 8, cudaMemcpyDeviceToHost, s));
+      if (o.time_xyt && toff[i + 1] > toff[i])
+        MCFL_CUDA_TRY(cudaMemcpyAsync(o.time_xyt, c->tarr.as<unsigned long long>() + toff[i],
+                                      (toff[i + 1] - toff[i]) * 8, cudaMemcpyDeviceToHost, s));
     }
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));
     for (int i = 0; i < n; ++i) {

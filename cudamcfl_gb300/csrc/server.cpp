@@ -49,7 +49,8 @@ struct Request {
   size_t footprint = 0;
   /* device state while admitted */
   mcfl_medium *medium = nullptr;
-  DevBuf R, T, fhd, stats;
+  DevBuf R, T, fhd, stats, tpos, tarr;
+  unsigned mode = 0;         /* bit 0: voxel-boundary stepping, bit 1: time-resolved detectors */
   int slot = -1;
   uint64_t ticket_begin = 0; /* in the current slice */
   uint64_t started = 0;      /* photons handed to the GPU so far */
@@ -57,7 +58,7 @@ struct Request {
   /* results */
   bool done = false;
   int status = MCFL_OK;
-  std::vector<unsigned long long> Rd, Tt, fhd_host;
+  std::vector<unsigned long long> Rd, Tt, fhd_host, time_host;
   unsigned long long st[MCFL_ST_COUNT] = {0};
 };
 
@@ -67,6 +68,8 @@ size_t footprint_of(const mcfl_medium_desc &d, const mcfl_run_desc &r) {
   size_t b = nv + (d.fluor_map ? nv * 4 : 0) + 3 * 16 * (size_t)(d.n_bulks + 2);
   b += 2 * xy * 8 + MCFL_ST_COUNT * 8;
   if (r.fluence) b += nv * 8;
+  if (r.tdet.nx) b += (size_t)r.tdet.nx * r.tdet.ny * r.tdet.bins * 8 + (size_t)(r.tdet.nx + r.tdet.ny) * 4;
+  if (r.exact_stepping) b += 6 * 16 * (size_t)(d.n_bulks + 2) + 2 * nv; /* its tables and free-radius map */
   return b;
 }
 
@@ -88,7 +91,15 @@ struct mcfl_server {
   int fatal = MCFL_OK;
   std::thread worker;
   /* device state */
-  DevBuf slot_jobs, order, counter, parked, stats_all;
+  DevBuf slot_jobs, order, counter, stats_all;
+  /* Modes: bit 0 voxel-boundary stepping, bit 1 time of flight.  A launch
+   * runs the requests of one mode with that mode's kernel variant; each mode
+   * keeps one launch shape and its own photons in flight (parked per
+   * thread), so slices of different modes take turns. */
+  static constexpr unsigned kModes = 4;
+  DevBuf parked[kModes];
+  int grid_m[kModes] = {0, 0, 0, 0}, block_m[kModes] = {256, 256, 256, 256};
+  unsigned next_mode = 0;
   McflJob *h_jobs = nullptr;
   uint32_t *h_order = nullptr;
   unsigned long long *h_read = nullptr;
@@ -128,9 +139,15 @@ int mcfl_server::upload(Request &r) {
   }
   McflJob &j = h_jobs[r.slot];
   std::memset(&j, 0, sizeof(j));
+  const bool exact = r.run.exact_stepping != 0;
+  if (exact) {
+    const int rcm = ensure_free_map(ctx, m);
+    if (rcm != MCFL_OK) return rcm;
+  }
   j.labels = m->labels.as<uint8_t>();
-  j.prop = m->prop_exc.as<float>();
-  j.lab = m->lab_exc.as<float>();
+  j.prop = m->prop_of(false, exact);
+  j.lab = m->lab_of(false, exact);
+  j.lab16 = exact ? m->lab16.as<uint16_t>() : nullptr;
   j.hx = m->hx; j.hy = m->hy; j.esp = m->esp;
   j.gx = m->gx; j.gy = m->gy; j.gz = m->gz;
   j.nx = (uint32_t)m->nx; j.ny = (uint32_t)m->ny; j.nz = (uint32_t)m->nz; j.total = m->total;
@@ -162,6 +179,27 @@ int mcfl_server::upload(Request &r) {
   j.rng_offset = r.run.photon_offset;
   j.ticket_begin = r.ticket_begin;
   j.photons = r.run.photons;
+  const mcfl_time_detectors &td = r.run.tdet;
+  if (td.nx) {
+    const size_t tsize = (size_t)td.nx * td.ny * td.bins;
+    MCFL_CUDA_TRY(r.tpos.reserve((size_t)(td.nx + td.ny) * 4));
+    MCFL_CUDA_TRY(r.tarr.reserve(tsize * 8));
+    std::vector<float> pos((size_t)(td.nx + td.ny));
+    time_positions(td, pos.data(), pos.data() + td.nx);
+    MCFL_CUDA_TRY(cudaMemcpyAsync(r.tpos.p, pos.data(), pos.size() * 4, cudaMemcpyHostToDevice, s));
+    MCFL_CUDA_TRY(cudaMemsetAsync(r.tarr.p, 0, tsize * 8, s));
+    j.time_on = 1;
+    j.tpos_x = r.tpos.as<float>();
+    j.tpos_y = r.tpos.as<float>() + td.nx;
+    j.time_xyt = r.tarr.as<unsigned long long>();
+    j.tmax = td.max_fs;
+    j.tdet_r = td.radius;
+    j.tnx = (uint32_t)td.nx;
+    j.tny = (uint32_t)td.ny;
+    j.tbins = (uint32_t)td.bins;
+    j.tdet_face = (uint32_t)td.face;
+  }
+  r.mode = (exact ? 1u : 0u) | (td.nx ? 2u : 0u);
   return MCFL_OK;
 }
 
@@ -172,6 +210,8 @@ void mcfl_server::release(Request &r) {
   r.T.release();
   r.fhd.release();
   r.stats.release();
+  r.tpos.release();
+  r.tarr.release();
 }
 
 int mcfl_server::admit_locked(std::vector<std::shared_ptr<Request>> &to_upload) {
@@ -248,11 +288,19 @@ void mcfl_server::loop() {
     unsigned n = 0, n_active = 0;
     int head = -1;
     std::vector<uint32_t> h_stat_slot;
+    /* the mode of this slice: the next one, in turn, with admitted requests */
+    unsigned have = 0;
+    for (unsigned i = 0; i < slots; ++i)
+      if (active[i]) have |= 1u << active[i]->mode;
+    if (!have) continue;
+    unsigned mode = next_mode;
+    while (!(have & (1u << mode))) mode = (mode + 1) % kModes;
+    next_mode = (mode + 1) % kModes;
     for (unsigned i = 0; i < slots; ++i)
       if (active[i]) {
         ++n_active;
         h_stat_slot.push_back(i);
-        if (active[i]->started < active[i]->run.photons) {
+        if (active[i]->mode == mode && active[i]->started < active[i]->run.photons) {
           h_order[n++] = i;
           if (head < 0 || active[i]->t_admit < active[head]->t_admit ||
               (active[i]->t_admit == active[head]->t_admit && active[i]->id < active[head]->id))
@@ -312,12 +360,14 @@ void mcfl_server::loop() {
     }
     L.max_iters = slice_cur;
     L.variant = (uint32_t)ctx->mixed_code();
+    L.exact_step = (mode & 1u) ? 1u : 0u;
+    L.time_on = (mode & 2u) ? 1u : 0u;
     L.ticket_counter = counter.as<unsigned long long>();
     L.ticket_end = tickets_end;
     L.mult = ctx->mult.as<uint32_t>();
-    L.saved = parked.as<McflSaved>();
+    L.saved = parked[mode].as<McflSaved>();
     L.step_cap = ctx->step_cap;
-    cudaError_t e = ctx->launch_transport(L, grid, block);
+    cudaError_t e = ctx->launch_transport(L, grid_m[mode], block_m[mode]);
     cudaMemcpyAsync(h_read, counter.p, 16, cudaMemcpyDeviceToHost, s);
     for (unsigned i = 0; i < n_active; ++i) {
       Request &r = *active[h_stat_slot[i]];
@@ -368,6 +418,11 @@ void mcfl_server::loop() {
         r->fhd_host.resize(r->medium->total);
         cudaMemcpyAsync(r->fhd_host.data(), r->fhd.p, (size_t)r->medium->total * 8, cudaMemcpyDeviceToHost, s);
       }
+      if (r->run.tdet.nx) {
+        const size_t tsize = (size_t)r->run.tdet.nx * r->run.tdet.ny * r->run.tdet.bins;
+        r->time_host.resize(tsize);
+        cudaMemcpyAsync(r->time_host.data(), r->tarr.p, tsize * 8, cudaMemcpyDeviceToHost, s);
+      }
       std::memcpy(r->st, st, sizeof(r->st));
       cudaStreamSynchronize(s);
       release(*r);
@@ -408,13 +463,16 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   }
   sv->active.assign(sv->slots, nullptr);
   sv->grid = ctx->grid_for(false, &sv->block);
-  const size_t threads = (size_t)sv->grid * sv->block;
   cudaError_t e = sv->slot_jobs.reserve(sv->slots * sizeof(McflJob));
   if (!e) e = sv->order.reserve(sv->slots * 4);
   if (!e) e = sv->counter.reserve(16); /* the two queues' ticket counters */
-  if (!e) e = sv->parked.reserve(threads * sizeof(McflSaved));
   if (!e) e = cudaMemset(sv->counter.p, 0, 8);
-  if (!e) e = cudaMemset(sv->parked.p, 0, threads * sizeof(McflSaved));
+  for (unsigned mode = 0; mode < mcfl_server::kModes && !e; ++mode) {
+    sv->grid_m[mode] = ctx->grid_for(false, &sv->block_m[mode], nullptr, (mode & 2u) != 0, (mode & 1u) != 0);
+    const size_t threads = (size_t)sv->grid_m[mode] * sv->block_m[mode];
+    e = sv->parked[mode].reserve(threads * sizeof(McflSaved));
+    if (!e) e = cudaMemset(sv->parked[mode].p, 0, threads * sizeof(McflSaved));
+  }
   if (!e) e = cudaHostAlloc((void **)&sv->h_jobs, sv->slots * sizeof(McflJob), cudaHostAllocDefault);
   if (!e) e = cudaHostAlloc((void **)&sv->h_order, sv->slots * 4, cudaHostAllocDefault);
   if (!e) e = cudaHostAlloc((void **)&sv->h_read, (2 + (size_t)sv->slots * MCFL_ST_COUNT) * 8, cudaHostAllocDefault);
@@ -432,8 +490,10 @@ extern "C" int mcfl_server_submit(mcfl_server *sv, const mcfl_medium_desc *mediu
                                   unsigned long long *id) {
   if (!sv || !medium || !run || !id) return fail(MCFL_E_ARG, "mcfl_server_submit: null argument");
   if (run->photons_per_voxel) return fail(MCFL_E_ARG, "server requests are excitation runs (photons_per_voxel = 0)");
-  if (run->tdet.nx) return fail(MCFL_E_ARG, "server requests carry no time-resolved detectors (use mcfl_run)");
-  if (run->exact_stepping) return fail(MCFL_E_ARG, "server requests use the reference's stepping (exact stepping: mcfl_run)");
+  const mcfl_time_detectors &td = run->tdet;
+  if (td.nx < 0 || (td.nx && (td.ny <= 0 || td.bins <= 0 || td.max_fs == 0 || !(td.radius > 0) ||
+                             (td.face != 0 && td.face != 1))))
+    return fail(MCFL_E_ARG, "bad time-resolved detectors");
   if (run->photons == 0 || run->det.nx <= 0 || run->det.ny <= 0) return fail(MCFL_E_ARG, "bad run");
   if (!medium->labels || !medium->bulks || medium->n_bulks < 1 || medium->n_bulks > MCFL_MAX_BULKS)
     return fail(MCFL_E_ARG, "bad medium");
@@ -483,6 +543,8 @@ extern "C" int mcfl_server_result(mcfl_server *sv, unsigned long long id, mcfl_r
     if (out->Rd) std::memcpy(out->Rd, r->Rd.data(), r->Rd.size() * 8);
     if (out->Tt) std::memcpy(out->Tt, r->Tt.data(), r->Tt.size() * 8);
     if (out->fhd && !r->fhd_host.empty()) std::memcpy(out->fhd, r->fhd_host.data(), r->fhd_host.size() * 8);
+    if (out->time_xyt && !r->time_host.empty())
+      std::memcpy(out->time_xyt, r->time_host.data(), r->time_host.size() * 8);
     std::memcpy(out->stats_exc, r->st, sizeof(r->st));
   }
   if (latency_ms) *latency_ms = std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();

@@ -210,6 +210,8 @@ __device__ __forceinline__ void load_med(const McflJob *J, Med &m) {
   m.ny = __ldg(&J->ny);
   m.total = __ldg(&J->total);
   m.last = __ldg(&J->last_label);
+  m.nz = __ldg(&J->nz);
+  m.lab16 = (const uint16_t *)__ldg((const unsigned long long *)&J->lab16);
 }
 
 /* The label record: a = (mutr, mu_a*mutr, 1-g^2, 1-g), b = (2g, 1+g^2, 1/(2g), n). */
@@ -721,8 +723,10 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
 /* kGeneral (single medium, reference stepping): every test of the
  * reference's pass as its own branch (the form before the SIMT arrangement),
  * kept as an autotuner alternative. */
+/* kPhdWarp (single medium, the SIMT-arranged pass): the hitting-density adds
+ * of a warp's lanes aggregated per voxel, one add per distinct voxel. */
 template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks, bool kPhdAgg = false,
-          bool kGeneral = false>
+          bool kGeneral = false, bool kPhdWarp = false>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   constexpr bool kLayered = kMode == 1;
   constexpr bool kExactStep = kMode == 2;
@@ -808,7 +812,6 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   unsigned long long f_acc = 0ull;
   uint32_t job = 0xffffffffu, src_idx = 0, pst = 0, pst0 = 0, done = 0, steps = 0;
   uint64_t k = 0, absorbed = 0;
-  uint32_t absorbed_ph = 0; /* lean pass: absorbed weight since the photon's last roulette */
   const McflJob *J = nullptr;
 
   auto flush_stats = [&]() {
@@ -835,6 +838,21 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       J = &L.jobs[job];
       if (!kUniform) load_med(J, m);
       p = Photon{sv.x, sv.y, sv.z, sv.dx, sv.dy, sv.dz, sv.weight, sv.label};
+      p.tof = sv.tof;
+      if (kExactStep) {
+        p.ix = sv.ix;
+        p.iy = sv.iy;
+        p.iz = sv.iz;
+        xtau = sv.xtau;
+        xox = sv.xox;
+        xoy = sv.xoy;
+        xoz = sv.xoz;
+        xs0 = sv.xs0;
+        xcr = sv.xcr;
+        xit = sv.xit;
+        xmid = (sv.xflags & 1u) != 0u;
+        xbegin = (sv.xflags & 2u) != 0u;
+      }
       r.x = sv.rng_x;
       r.a = sv.rng_a;
       k = sv.k;
@@ -849,7 +867,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   for (uint32_t it = 0;; ++it) {
     /* single-medium launches always run to the end of their tickets */
     if (!kUniform && L.max_iters && it >= L.max_iters) break;
-    /* one vote per pass while every lane carries a photon */
+    /* one vote per pass while every lane carries a photon; live: the lanes
+     * that run this pass (lanes without a photon skip it), the member mask
+     * of any warp-wide operation inside the pass */
+    unsigned live = kFull;
     if (__ballot_sync(kFull, !alive)) {
     const bool need = !alive && !(ex0 && ex1);
     const unsigned nm = __ballot_sync(kFull, need);
@@ -898,6 +919,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       }
     }
     if (__all_sync(kFull, !alive) && ex0 && ex1) break;
+    if constexpr (kPhdWarp) live = __ballot_sync(kFull, alive);
     if (!alive) continue;
     }
 
@@ -944,7 +966,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       if (++xit > cap) {
         outcome = 3;
       } else {
-        const real4 ca = s_lab[2 * p.label];
+        const real4 ca = kUniform ? s_lab[2 * p.label] : rc.a;
         const int cr = xcr;
         const bool in = in_grid(m, p.ix, p.iy);
         const int lx = in ? max(p.ix - cr, 0) : p.ix - cr, ux = in ? min(p.ix + cr, (int)m.nx - 1) : p.ix + cr;
@@ -981,7 +1003,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.x = x;
           p.y = y;
           p.z = z;
-          if (kTime) p.tof += tof_fs((sj - xs0) * s_lab[2 * p.label + 1].w); /* the run's optical path */
+          if (kTime) p.tof += tof_fs((sj - xs0) * (kUniform ? s_lab[2 * p.label + 1].w : rc.b.w)); /* the run's optical path */
           outcome = 1;
         } else {
           /* the region across the face */
@@ -1001,7 +1023,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             xcr = nr;
           } else {
             /* the run of this label ends at the face */
-            const real n_here = s_lab[2 * p.label + 1].w, n_next = s_lab[2 * next + 1].w;
+            const real n_here = kUniform ? s_lab[2 * p.label + 1].w : rc.b.w;
+            const real n_next = kUniform ? s_lab[2 * next + 1].w : label_n(m, next);
             if (ca.x != FLT_MAX) {
               xtau -= (db - xs0) / ca.x;
               if (xtau < MCFL_C(0.0)) xtau = MCFL_C(0.0);
@@ -1018,6 +1041,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               xbegin = true;
             } else {
               p.label = next;
+              if constexpr (!kUniform) rc = load_rec(m, next);
               p.ix = nix;
               p.iy = niy;
               p.iz = niz;
@@ -1043,7 +1067,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         if (m.fhd && in_grid(m, p.ix, p.iy))
           atomicAdd(&m.fhd[(uint32_t)p.ix + m.nx * ((uint32_t)p.iy + m.ny * (uint32_t)p.iz)],
                     (unsigned long long)p.weight);
-        const Rec c2 = Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]};
+        const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
         const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
         if (w > 0u) {
           p.weight -= w;
@@ -1149,6 +1173,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       const bool rare = !(mutr != FLT_MAX) || clip || !(s > MCFL_C(0.0)) ||
                         (lab != p.label && (n_new != n_old || lab - 1u >= m.last - 1u));
       bool spin_now;
+      /* the hitting-density add of the pass (made after both forms join, so
+       * that the warp-aggregated form runs converged) */
+      bool phd_on;
+      uint32_t phd_idx = vi, phd_w = p.weight;
       if (!rare) {
         p.x = xn;
         p.y = yn;
@@ -1157,7 +1185,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           if (lab != p.label) rc = load_rec(m, lab);
         }
         p.label = lab;
-        if (m.fhd && inside) atomicAdd(&m.fhd[vi], (unsigned long long)p.weight);
+        phd_on = m.fhd && inside;
         spin_now = true;
       } else {
         uint32_t new_bulk;
@@ -1190,8 +1218,9 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.label = new_bulk;
           if constexpr (!kUniform) rc = load_rec(m, new_bulk);
         }
-        if (m.fhd && (vr != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp)))
-          atomicAdd(&m.fhd[vr != 0xffffffffu ? vr : voxel_index(m, p.x, p.y, p.z)], (unsigned long long)p.weight);
+        phd_on = m.fhd && (vr != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp));
+        if (phd_on) phd_idx = vr != 0xffffffffu ? vr : voxel_index(m, p.x, p.y, p.z);
+        phd_w = p.weight; /* before an exit takes it */
         if (p.label == 0u || p.label == m.last) {
           const bool top = p.label == 0u;
           tally_exit(J, p.x, p.y, p.weight, top, src_idx);
@@ -1201,12 +1230,29 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         }
         spin_now = s > MCFL_C(0.0);
       }
+      if constexpr (kPhdWarp) {
+        /* Warp-aggregated: the lanes adding to the same voxel are grouped
+         * (__match_any_sync), their weights summed in two 16-bit halves (a
+         * sum of 32 weights of 32 bits needs 37 bits), and one lane of each
+         * group adds the sum.  The tally is the same integer sum. */
+        if (__any_sync(live, phd_on)) {
+          const uint32_t key = phd_on ? phd_idx : 0xffffffffu;
+          const unsigned peers = __match_any_sync(live, key);
+          const uint32_t w = phd_on ? phd_w : 0u;
+          const uint32_t lo = __reduce_add_sync(peers, w & 0xffffu);
+          const uint32_t hi = __reduce_add_sync(peers, w >> 16);
+          if (phd_on && lane == (unsigned)(__ffs(peers) - 1))
+            atomicAdd(&m.fhd[phd_idx], ((unsigned long long)hi << 16) + lo);
+        }
+      } else {
+        if (phd_on) atomicAdd(&m.fhd[phd_idx], (unsigned long long)phd_w);
+      }
       if (spin_now) {
         const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
         const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
         if (w > 0u) {
           p.weight -= w;
-          absorbed_ph += w;
+          absorbed += w;
         } else {
           ev_add(MCFL_ST_W0_LOSS, p.weight);
           p.weight = 0u;
@@ -1292,13 +1338,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
     }
     /* PhotonSurvive, the pass cap and the photon's end: one branch for the
-     * lean pass (the absorbed weight of the photon, summed in 32 bits since
-     * the last roulette, moves to the launch's 64-bit sum there) */
+     * lean pass */
     if (!kLean || p.weight <= kWeightRoulette || pst >= L.step_cap) {
-      if (kLean) {
-        absorbed += absorbed_ph;
-        absorbed_ph = 0u;
-      }
       if (p.weight <= kWeightRoulette) {
         if (p.weight == 0u) {
           alive = false;
@@ -1322,7 +1363,6 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
   }
   if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
-  absorbed += absorbed_ph;         /* the absorbed weight of a parked photon so far */
   if (kPhdAgg && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 
   if (!kUniform && L.max_iters && L.saved) {
@@ -1339,6 +1379,20 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       sv.k = k;
       sv.steps = pst;
       sv.src_idx = src_idx;
+      sv.tof = kTime ? p.tof : 0ull;
+      if (kExactStep) {
+        sv.ix = p.ix;
+        sv.iy = p.iy;
+        sv.iz = p.iz;
+        sv.xtau = (float)xtau;
+        sv.xox = (float)xox;
+        sv.xoy = (float)xoy;
+        sv.xoz = (float)xoz;
+        sv.xs0 = (float)xs0;
+        sv.xcr = xcr;
+        sv.xit = xit;
+        sv.xflags = (xmid ? 1u : 0u) | (xbegin ? 2u : 0u);
+      }
     }
     L.saved[gtid] = sv;
   }
@@ -1355,11 +1409,13 @@ static size_t smem_bytes(int threads, bool uniform) {
  * the blocks per SM the register budget is cut for): 0 = 256 x 4,
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner, and 7, 8, 9 the same
  * with the photon-hitting-density sums held in a register, 11, 12, 13 the
- * same with the pass in its per-test branching form; 3 = 256 x 3 carrying
+ * same with the pass in its per-test branching form, 14, 15, 16 the same
+ * with the hitting-density adds aggregated per warp; 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
  * of flight; voxel-boundary stepping 6 = 256 x 4, 10 = 256 x 3 with the time
  * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
  * -5, -6, -7 the same with the per-test branching pass, -2 = 256 x 2 with
+ * the time of flight; voxel-boundary stepping -8 = 256 x 3, -9 = 256 x 2 with
  * the time of flight. */
 typedef void (*TransportKernel)(McflLaunch);
 
@@ -1379,6 +1435,8 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case -5: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 3, false, true>;
   case -6: *threads = 256; return MCFL_KERNEL_NAME<false, false, 0, 256, 4, false, true>;
   case -7: *threads = 128; return MCFL_KERNEL_NAME<false, false, 0, 128, 7, false, true>;
+  case -8: *threads = 256; return MCFL_KERNEL_NAME<false, false, 2, 256, 3>;
+  case -9: *threads = 256; return MCFL_KERNEL_NAME<false, true, 2, 256, 2>;
   case 0: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4>;
   case 1: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5>;
   case 2: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9>;
@@ -1393,6 +1451,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case 11: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, false, true>;
   case 12: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, false, true>;
   case 13: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, false, true>;
+  case 14: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, false, false, true>;
+  case 15: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, false, false, true>;
+  case 16: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, false, false, true>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -1406,11 +1467,10 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
 #if MCFL_F64
   if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
 #endif
-  if (L->max_iters && L->time_on) return cudaErrorNotSupported; /* parked photons carry no time of flight */
   if (L->max_iters && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
   if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
     return cudaErrorInvalidValue;
-  const int v = L->exact_step ? (L->time_on ? 10 : 6)
+  const int v = L->exact_step ? (!L->uniform_medium ? (L->time_on ? -9 : -8) : L->time_on ? 10 : 6)
                 : L->med.layered ? (L->time_on ? 5 : 4)
                 : L->uniform_medium ? (L->time_on ? 3 : (int)L->variant)
                 : L->time_on        ? -2

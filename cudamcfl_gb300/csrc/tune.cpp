@@ -37,13 +37,14 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
   const int old_variant = c->variant, old_l2 = c->l2_window, old_agg = c->phd_agg, old_form = c->pass_form;
   int best_v = old_variant, best_l2 = old_l2, best_agg = old_agg, best_form = old_form;
   double best = -1.0;
-  /* forms: 0 SIMT-arranged pass, 1 branching pass, 2 branching pass with the
-   * register-held hitting density (only when the run tallies it) */
-  const int n_forms = (r.fluence || r.photons_per_voxel) ? 3 : 2;
+  /* forms: 0 SIMT-arranged pass, 1 branching pass, and when the run tallies
+   * the hitting density 2 the branching pass with the register-held sums,
+   * 3 the SIMT-arranged pass with the warp-aggregated adds */
+  const int n_forms = (r.fluence || r.photons_per_voxel) ? 4 : 2;
   for (int v = 0; v < MCFL_N_VARIANTS; ++v) {
     for (int cfg = 0; cfg < 2 * n_forms; ++cfg) {
       const int l2 = cfg & 1, form = cfg >> 1;
-      const int agg = form == 2 ? 1 : 0, pass_form = form == 1 ? 1 : 0;
+      const int agg = form == 2 ? 1 : form == 3 ? 2 : 0, pass_form = form == 1 ? 1 : 0;
       c->variant = v;
       c->l2_window = l2;
       c->phd_agg = agg;

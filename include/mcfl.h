@@ -328,9 +328,10 @@ const char *mcfl_last_error(void);
  * 2 = 128 x 7, the default),
  * "blocks_per_sm" (0 = occupancy maximum), "step_cap" (passes per photon),
  * "l2_window" (1: persisting L2 access window on the labels and tallies),
- * "phd_agg" (1: the single-medium kernel sums a thread's successive passes
- * in one voxel in a register before adding them to the photon hitting
- * density; 0: one atomic add per pass; the tallies are the same),
+ * "phd_agg" (the photon-hitting-density tally of the single-medium kernel:
+ * 0 one atomic add per pass; 1 a thread's successive passes in one voxel
+ * summed in a register before the add; 2 the adds of a warp's lanes summed
+ * per voxel, one add per distinct voxel; the tallies are the same),
  * "pass_form" (0: the single-medium pass arranged for the SIMT warp, the
  * common case straight-line and every rare case behind one branch; 1: every
  * test of the reference's pass as its own branch; the tallies are the same).

@@ -27,9 +27,13 @@ within 3 sigma, and within 0.1 % wherever the budget resolves 0.1 % (the
 test asserts that 3 sigma of the difference is below 0.1 % for R and the
 absorbed fraction; for the transmittance, 2 % of the light at 2 cm, the
 difference's 3 sigma is about 0.2 % at this budget, so it is held to 3 sigma).
-Each engine batch is the mean of 8 runs of the reference batch's photon
-count (the same share of first photons), so the engine's side of the
-standard error is small beside the reference's.
+The per-pixel and per-voxel gates compare batches of the same design on
+both sides (one run of the reference batch's photon count per batch, so the
+same share of first photons): most transmittance and emission pixels hold a
+few photons per batch, and a t statistic between a low-count side and a side
+averaged over many runs has mismatched tails.  The integrated fractions use
+every engine run (8 per batch), so the engine's side of their standard error
+is small beside the reference's.
 """
 import os
 
@@ -73,15 +77,16 @@ def _reduce(r, xy, shape, crop, w0, engine):
 
 
 def _compare(eng, ref, det_shape):
-    """eng, ref: per batch the reduced per-photon tallies (the engine's a
-    mean of its runs)."""
+    """eng: per batch the engine's reduced runs (the first gated per pixel,
+    all for the integrated fractions); ref: per batch one reduced reference
+    run."""
     summary = {}
     for k in ("Rd", "Tt", "fhd", "flR", "flT"):
-        a = np.stack([e[k] for e in eng])
+        a = np.stack([runs[0][k] for runs in eng])
         b = np.stack([x[k] for x in ref])
         summary[k] = stats.gate(a, b, frac_max=0.02, min_rel=1e-2, shape=det_shape if k in ("Rd", "Tt") else None)
     for i, k in enumerate(("absorbed", "exit_top", "exit_bottom")):
-        out = stats.scalar_gate([e["frac"][i] for e in eng], [x["frac"][i] for x in ref])
+        out = stats.scalar_gate([r["frac"][i] for runs in eng for r in runs], [x["frac"][i] for x in ref])
         if k != "exit_bottom":
             assert 3 * out["sigma"] / out["b"] < 1e-3, ("0.1 % not resolved", k, out)
             assert out["rel_diff"] < 1e-3, (k, out)
@@ -90,10 +95,17 @@ def _compare(eng, ref, det_shape):
 
 
 def _engine_batches(ctx, med, rd_of, reduce):
+    """Per batch, RUNS_PER_BATCH reduced runs (only the first keeps its
+    images)."""
     eng = []
     for b in range(B):
-        runs = [reduce(ctx.run(med, rd_of(b, j))) for j in range(RUNS_PER_BATCH)]
-        eng.append({k: (np.mean([r[k] for r in runs], axis=0)) for k in runs[0]})
+        runs = []
+        for j in range(RUNS_PER_BATCH):
+            r = reduce(ctx.run(med, rd_of(b, j)))
+            if j:
+                r = {"frac": r["frac"]}
+            runs.append(r)
+        eng.append(runs)
     return eng
 
 

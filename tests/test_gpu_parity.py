@@ -65,11 +65,12 @@ def test_exact_kernel_launch_shape_does_not_change_tallies(gpu_ctx, oracle, tabl
         gpu_ctx.set_option("block", 256)
         gpu_ctx.set_option("blocks_per_sm", 0)
         # every occupancy variant, with and without the persisting-L2 window,
-        # with either form of the photon-hitting-density tally and either
-        # form of the pass (SIMT-arranged, per-test branching)
+        # with each form of the photon-hitting-density tally (one add per
+        # pass, register sums, warp sums) and either form of the pass
+        # (SIMT-arranged, per-test branching)
         for variant, bound in ((0, 256), (1, 256), (2, 128)):
             for l2 in (0, 1):
-                for agg, form in ((0, 0), (0, 1), (1, 0)):
+                for agg, form in ((0, 0), (0, 1), (1, 0), (2, 0)):
                     gpu_ctx.set_option("variant", variant)
                     gpu_ctx.set_option("l2_window", l2)
                     gpu_ctx.set_option("phd_agg", agg)
@@ -96,7 +97,7 @@ def test_autotune_keeps_a_variant_and_tallies(gpu_ctx, oracle, table32768):
         variant, rate = gpu_ctx.autotune(med, case.run_desc(8, 9), sample_photons=20000)
         assert variant in (0, 1, 2) and rate > 0
         assert gpu_ctx.get_option("variant") == variant
-        assert gpu_ctx.get_option("phd_agg") in (0, 1)
+        assert gpu_ctx.get_option("phd_agg") in (0, 1, 2)
         assert gpu_ctx.get_option("pass_form") in (0, 1)
         _compare(gpu_ctx.run(med, case.run_desc(8, 9)), ref)
     finally:
@@ -453,8 +454,7 @@ def test_voxel_boundary_stepping_bit_identical_to_oracle(name, gpu_ctx, oracle, 
 
 @pytest.mark.gpu
 def test_voxel_boundary_stepping_inputs_fail_with_status(gpu_ctx):
-    """Exact stepping has no layered media; a batch shares one stepping; the
-    server runs the reference's stepping."""
+    """Exact stepping has no layered media; a batch shares one stepping."""
     med = cases.mismatch().engine_medium(gpu_ctx)
     a = cases.mismatch().run_desc(1, 2)
     a.photons_per_voxel, a.fluence = 0, 0

@@ -176,3 +176,100 @@ def test_recorded_graph_follows_a_new_medium_at_a_reused_address(gpu_ctx, oracle
         res = gpu_ctx.run(med, case.run_desc(12, 13))
         med.free()
         _compare(res, ref, emission=False)
+
+
+def _same(res, one, timed=False):
+    assert np.array_equal(res["Rd"], one.Rd) and np.array_equal(res["Tt"], one.Tt)
+    for k in ("done", "steps", "absorbed", "exit_top", "exit_bottom"):
+        assert res["stats"][k] == one.stats_exc[k], k
+    if timed:
+        assert np.array_equal(res["time_xyt"], one.time_xyt.ravel())
+        assert one.time_xyt.sum() > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("exact", [0, 1])
+def test_batch_time_detectors_equal_alone(exact, gpu_ctx):
+    """Runs with and without time-resolved detectors in one batch, over one
+    medium (single-medium timed kernel) and over several (mixed-media timed
+    kernel), with the reference's and with voxel-boundary stepping: each run's
+    histograms, images and weight accounting equal the run alone."""
+    base = [cases.timed(face=0), cases.timed(face=1, base=cases.glass), cases.timed(face=1)]
+    meds = [c.engine_medium(gpu_ctx) for c in base]
+    try:
+        det = mc.Detector(0.0, 0.0, 0.1, 0.1, 20, 20)
+        runs, media_of = [], []
+        for i, b in enumerate([6000, 15000, 900, 9000, 4000, 1]):
+            c = base[i % 3]
+            runs.append(mc.run_desc(b, source=(0.02 * i, -0.03 * i, 0.0), det=det, seed_exc=700 + i,
+                                    start_weight=c.start_weight(), tdet=c.temporal if i % 2 == 0 else None,
+                                    exact_stepping=exact))
+            media_of.append(meds[i % 3])
+        for medium in (meds[0], media_of):  # one medium, then several
+            for sched in (mc.SCHEDULE_BATCHED, mc.SCHEDULE_PLAIN):
+                got, _ = mc.batch_run(gpu_ctx, medium, runs, sched)
+                for i, rd in enumerate(runs):
+                    m = medium if not isinstance(medium, list) else medium[i]
+                    _same(got[i], gpu_ctx.run(m, rd, images=True, raw=True), timed=bool(rd.tdet.nx))
+    finally:
+        for m in meds:
+            m.free()
+
+
+@pytest.mark.gpu
+def test_batch_voxel_boundary_stepping_over_several_media_equals_alone(gpu_ctx):
+    """Voxel-boundary stepping over four media in one launch of the
+    mixed-media kernel (each job carrying its medium's label + free-radius
+    map): every run equals its run alone, bit for bit."""
+    chosen = [cases.tiny(), cases.mismatch(), cases.glass(), cases.sparse()]
+    meds = [c.engine_medium(gpu_ctx) for c in chosen]
+    try:
+        det = mc.Detector(0.0, 0.0, 0.1, 0.1, 20, 20)
+        runs, media_of = [], []
+        for i, b in enumerate([4000, 25000, 900, 12000, 7000, 3000, 16000, 1]):
+            k = i % len(chosen)
+            runs.append(mc.run_desc(b, source=(0.05 * k, -0.02 * k, 0.0), det=det, seed_exc=300 + i,
+                                    start_weight=chosen[k].start_weight(), exact_stepping=1))
+            media_of.append(meds[k])
+        bat, _ = mc.batch_run(gpu_ctx, media_of, runs, mc.SCHEDULE_BATCHED)
+        for i, rd in enumerate(runs):
+            _same(bat[i], gpu_ctx.run(media_of[i], rd, images=True, raw=True))
+    finally:
+        for m in meds:
+            m.free()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("slice_passes", [64, 4096])
+def test_server_time_detectors_and_stepping_equal_alone(slice_passes, gpu_ctx):
+    """Requests of all four kinds (the reference's or voxel-boundary
+    stepping, with or without time-resolved detectors) served together: the
+    kinds take turns in slices, each with its own photons in flight, and
+    every result equals the request run alone, bit for bit."""
+    meds = _request_media(11)
+    det = mc.Detector(0.0, 0.0, 0.05, 0.05, 30, 30)
+    tdet = (0.0, 0.0, 2, 2, 0.3, 0.3, 0.2, 1, 24, 300000)
+    reqs = []
+    for i in range(12):
+        lab, bulks, vox = meds[i % len(meds)]
+        rd = mc.run_desc(1500 + 1300 * i, source=(0.04 * i - 0.2, 0.01 * i, 0.0), det=det, fluence=i % 2,
+                         seed_exc=900 + i, tdet=tdet if (i // 2) % 2 else None, exact_stepping=i % 2)
+        reqs.append((lab, bulks, vox, rd))
+    ctx2 = mc.Context(math=mc.MATH_EXACT)
+    srv = mc.Server(ctx2, hbm_budget_bytes=64 << 20, max_jobs=5, slice_passes=slice_passes)
+    try:
+        ids = [srv.submit(lab, bulks, vox, rd) for lab, bulks, vox, rd in reqs]
+        results = []
+        for rid in ids:
+            assert srv.wait(rid, 120000) == 0
+            results.append(srv.result(rid))
+    finally:
+        srv.close()
+        ctx2.close()
+    for (lab, bulks, vox, rd), res in zip(reqs, results):
+        med = gpu_ctx.medium(lab, bulks, voxel_cm=vox)
+        one = gpu_ctx.run(med, rd)
+        _same(res, one, timed=bool(rd.tdet.nx))
+        if rd.fluence:
+            assert np.array_equal(res["fhd"], one.fhd)
+        med.free()

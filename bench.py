@@ -293,6 +293,8 @@ def main():
     ap.add_argument("--traffic-command", default="")
     ap.add_argument("--pass-form", type=int, default=0,
                     help="--profile: 0 the pass arranged for the SIMT warp, 1 every test as its own branch")
+    ap.add_argument("--phd-agg", type=int, default=0,
+                    help="--profile: hitting-density tally, 0 one add per pass, 1 register sums, 2 warp sums")
     args = ap.parse_args()
     if args.traffic_from:
         print(json.dumps(traffic_from_csv(args.traffic_from, args.traffic_command)))
@@ -609,17 +611,22 @@ def profile_case(args):
     ctx = mc.Context(device=0, math=mc.MATH_FAST if args.math == "fast" else mc.MATH_EXACT)
     ctx.set_option("variant", args.variant)
     ctx.set_option("pass_form", args.pass_form)
+    ctx.set_option("phd_agg", args.phd_agg)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
     rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2,
                      exact_stepping=1 if args.exact_stepping else 0)
+    best_exc = best_fl = float("inf")
     for _ in range(args.warmup + 1):
         r = ctx.run(med, rd, images=False, raw=False)
+        best_exc, best_fl = min(best_exc, r.ms_exc), min(best_fl, r.ms_fl)
     print(json.dumps({"profile_case": "config2", "math": args.math, "photons": args.photons,
                       "exact_stepping": bool(args.exact_stepping),
                       "emission_photons": r.photons_fl, "steps_exc": r.stats_exc["steps"],
                       "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
-                      "variant": args.variant, "pass_form": args.pass_form, "regs": ctx.get_option("regs"),
+                      "best_ms_exc": best_exc, "best_ms_fl": best_fl,
+                      "variant": args.variant, "pass_form": args.pass_form, "phd_agg": args.phd_agg,
+                      "regs": ctx.get_option("regs"),
                       "grid": ctx.get_option("grid"),
                       "block": ctx.get_option("launch_block")}), flush=True)
     med.free()

@@ -88,7 +88,8 @@ def kernel_source_sha() -> str:
 
 
 _UNITS = {"byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "Tbyte": 1e12,
-          "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0}
+          "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0,
+          "ns": 1e-9, "us": 1e-6, "ms": 1e-3, "s": 1.0}
 
 
 def traffic_from_csv(path: str, command: str) -> dict:

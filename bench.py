@@ -689,6 +689,7 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
         srv.wait(rid, -1)
     mtr = srv.metrics()
     served_lat = [srv.result(rid)["latency_ms"] for rid, _ in ids]
+    sizes = [p for _, p in ids]
     srv.close()
     photons_total = sum(p for _, p in ids)
     served = photons_total / mtr["span_s"] if mtr["span_s"] > 0 else None
@@ -742,7 +743,11 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
                      "max_ms": float(np.max(fifo_lat)), "photons_per_s": photons_total / fifo_span,
                      "note": "the same arrivals, one request at a time in arrival order"},
             "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
-            "slices": mtr["slices"],
+            "slices": mtr["slices"], "server_busy_s": mtr["busy_s"], "server_upload_s": mtr["upload_s"],
+            "server_finish_s": mtr["finish_s"], "server_span_s": mtr["span_s"],
+            "slowest": {"served": sorted(((round(l, 1), p) for l, p in zip(served_lat, sizes)), reverse=True)[:4],
+                        "fifo": sorted(((round(l, 1), p) for l, p in zip(fifo_lat, sizes)), reverse=True)[:4],
+                        "note": "(latency ms, photons) of the four slowest requests"},
             "saturated": {"requests": len(burst), "photons": burst_photons,
                           "served_photons_per_s": burst_photons / t_served,
                           "plain_photons_per_s": burst_photons / t_plain, "served_over_plain": t_plain / t_served},

@@ -109,7 +109,7 @@ struct mcfl_server {
   /* metrics */
   std::vector<double> latencies_ms;
   unsigned long long photons_done = 0, slices = 0, max_inflight = 0, inflight_sum = 0;
-  double busy_s = 0;
+  double busy_s = 0, upload_s = 0, finish_s = 0;
   Clock::time_point t_first, t_last;
   bool any = false;
 
@@ -262,6 +262,7 @@ void mcfl_server::loop() {
     /* Short slices let waiting requests in soon; with nobody waiting the
      * slices lengthen, which saves the per-slice host round trips. */
     slice_cur = (waiting || !fresh.empty()) ? slice_iters : std::min(slice_cur * 2u, slice_iters * 8u);
+    const auto t_up0 = Clock::now();
     for (auto &r : fresh) {
       r->t_admit = Clock::now();
       r->started = 0;
@@ -276,6 +277,7 @@ void mcfl_server::loop() {
         cv_done.notify_all();
       }
     }
+    upload_s += std::chrono::duration<double>(Clock::now() - t_up0).count();
     /* Tickets of this slice, in two queues: the oldest admitted request
      * alone in the second (three warps in four); in the first (one warp in
      * four) the requests at most an eighth of its remaining size, shortest
@@ -404,6 +406,7 @@ void mcfl_server::loop() {
       const uint64_t handed = c > r.ticket_begin ? c - r.ticket_begin : 0;
       r.started += std::min<uint64_t>(handed, r.run.photons - r.started);
     }
+    const auto t_fin0 = Clock::now();
     for (unsigned i = 0; i < n_active; ++i) {
       const uint32_t slot = h_stat_slot[i];
       std::shared_ptr<Request> r = active[slot];
@@ -440,6 +443,7 @@ void mcfl_server::loop() {
       used -= r->footprint;
       cv_done.notify_all();
     }
+    finish_s += std::chrono::duration<double>(Clock::now() - t_fin0).count();
   }
 }
 
@@ -576,6 +580,8 @@ extern "C" int mcfl_server_metrics(mcfl_server *sv, mcfl_server_metrics_t *m) {
   m->span_s = sv->any ? std::chrono::duration<double>(sv->t_last - sv->t_first).count() : 0.0;
   m->hbm_used = sv->used;
   m->hbm_budget = sv->budget;
+  m->upload_s = sv->upload_s;
+  m->finish_s = sv->finish_s;
   return MCFL_OK;
 }
 

@@ -55,6 +55,8 @@
  */
 #include <cuda_runtime.h>
 #include <float.h>
+
+#include <algorithm>
 #include <stdint.h>
 #include <string.h>
 
@@ -128,8 +130,6 @@ constexpr real kPi = MCFL_C(3.141592654);        /* CUDAMCFL.h:22 */
 constexpr uint32_t kWeightRoulette = 429497u; /* CUDAMCFL.h:33 */
 constexpr real kChance = MCFL_C(0.1);            /* CUDAMCFL.h:34 */
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kEv = 6; /* event counters kept in shared memory: EXIT_TOP .. CAPPED */
-
 /* shared-memory bytes of the label records (launches over one medium) */
 __host__ __device__ constexpr size_t lab_bytes(bool uniform) {
   return uniform ? (size_t)MCFL_MAX_LABELS * MCFL_LAB_FLOATS * sizeof(real) : 0;
@@ -734,15 +734,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
    * the SIMT warp (see the pass below) */
   constexpr bool kLean = kMode == 0 && !kTime && !kPhdAgg && !kGeneral;
   /* dynamic shared memory: (uniform medium) the label records of the
-   * medium at offset 0, then kEv x kThreads event counters (compile-time
-   * offsets and strides) */
+   * medium */
   extern __shared__ __align__(16) unsigned char s_mem[];
   real4 *s_lab = reinterpret_cast<real4 *>(s_mem);
-  unsigned long long *s_ev = reinterpret_cast<unsigned long long *>(s_mem + lab_bytes(kUniform));
   const unsigned lane = threadIdx.x & 31u;
   const unsigned tib = threadIdx.x;
   const size_t gtid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (int e = 0; e < kEv; ++e) s_ev[e * kThreads + tib] = 0ull;
   if (kLayered) {
     /* per layer (and, last, the inclusion): its record and its geometry */
     const float4 *tab = (const float4 *)L.med.layer_tab;
@@ -820,16 +817,15 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (done) atomicAdd(&st[MCFL_ST_DONE], (unsigned long long)done);
     if (steps) atomicAdd(&st[MCFL_ST_STEPS], (unsigned long long)steps);
     if (absorbed) atomicAdd(&st[MCFL_ST_ABSORBED], (unsigned long long)absorbed);
-    for (int e = 0; e < kEv; ++e) {
-      unsigned long long v = s_ev[e * kThreads + tib];
-      if (v) atomicAdd(&st[MCFL_ST_EXIT_TOP + e], v);
-      s_ev[e * kThreads + tib] = 0ull;
-    }
     done = 0;
     steps = 0;
     absorbed = 0;
   };
-  auto ev_add = [&](int e, unsigned long long v) { s_ev[(e - MCFL_ST_EXIT_TOP) * kThreads + tib] += v; };
+  /* the events of a photon (exits, roulette, zero-drop kills, the pass cap:
+   * a few per photon) go straight to the job's counters */
+  auto ev_add = [&](int e, unsigned long long v) {
+    if (v) atomicAdd((unsigned long long *)__ldg((const unsigned long long *)&J->stats) + e, v);
+  };
 
   if (!kUniform && L.max_iters && L.saved) {
     const McflSaved sv = L.saved[gtid];
@@ -1399,10 +1395,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   flush_stats();
 }
 
-/* dynamic shared memory of a launch of a kernel variant with kThreads =
- * threads (the event counters are laid out for the variant's block size) */
+/* dynamic shared memory of a launch (threads: the variant's block size) */
 static size_t smem_bytes(int threads, bool uniform) {
-  return lab_bytes(uniform) + (size_t)kEv * threads * sizeof(unsigned long long);
+  (void)threads;
+  return lab_bytes(uniform) + 16;
 }
 
 /* Kernel variants.  Single medium (occupancy variants: threads per block x
@@ -1511,6 +1507,24 @@ extern "C" cudaError_t MCFL_ATTR_FN(int variant, int *block, int *blocks_per_sm,
   if (e != cudaSuccess) return e;
   if (regs) *regs = a.numRegs;
   if (*block <= 0 || *block > t) *block = t;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void *)fn, *block,
-                                                       smem_bytes(t, variant >= 0));
+  const size_t smem = smem_bytes(t, variant >= 0);
+  /* The L1/shared split: just the shared memory the blocks that the
+   * registers allow need, the rest as L1 (the label gather of every pass
+   * hits it).  Occupancy first with the whole shared memory available. */
+  e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);
+  if (e != cudaSuccess) return e;
+  int bps = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, (const void *)fn, *block, smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, max_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&max_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)) != cudaSuccess) return e;
+  if (bps > 0 && max_sm > 0) {
+    const size_t need = (size_t)bps * (smem + a.sharedSizeBytes + 1024); /* 1 KB per block reserved by the system */
+    const int pct = (int)std::min<size_t>(100, (need * 100 + (size_t)max_sm - 1) / (size_t)max_sm + 1);
+    e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void *)fn, *block, smem);
 }

@@ -440,6 +440,8 @@ typedef struct mcfl_server_metrics_t {
   double mean_inflight;             /* jobs per slice, mean */
   unsigned long long max_inflight;  /* jobs per slice, maximum */
   unsigned long long hbm_used, hbm_budget;
+  double upload_s;                  /* server-thread wall time uploading admitted requests' media */
+  double finish_s;                  /* server-thread wall time copying out and releasing finished requests */
 } mcfl_server_metrics_t;
 
 /* Starts the server thread; it owns ctx (and its stream) until

@@ -383,7 +383,9 @@ def main():
                    "emitting_voxels": stats_out.fl_voxels, "emission_photons": stats_out.photons_fl,
                    "math": args.math, "l2": "flushed between steps (512 MB write)", "parallelism": "replicas only",
                    "schedule": "batched: one persistent launch per phase, CUDA-graph replay",
-                   "variant": variant, "block": ctx.get_option("launch_block"), "grid": ctx.get_option("grid"),
+                   "variant": variant, "variant_emission": ctx.get_option("variant_fl"),
+                   "pass_form": ctx.get_option("pass_form"),
+                   "block": ctx.get_option("launch_block"), "grid": ctx.get_option("grid"),
                    "regs": ctx.get_option("regs"), "l2_window": ctx.get_option("l2_window"),
                    "phd_agg": ctx.get_option("phd_agg"),
                    "autotune_sample_photons_per_s": tune_rate},

@@ -70,21 +70,21 @@ unsigned long long next_medium_serial() {
   return ++counter;
 }
 
-int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool exact) {
+int mcfl_ctx::attr(bool uniform, int *blk, int *bps, int *regs, bool time, bool exact, bool fl) {
   *blk = block;
   *bps = 0;
   *regs = 0;
   static const int mixed_codes[6] = {-1, -3, -4, -5, -6, -7};
   const int mixed = mixed_codes[mixed_code()];
   const int v = exact ? (uniform ? (time ? 10 : 6) : (time ? -9 : -8))
-                : uniform ? (time ? 3 : variant_code())
+                : uniform ? (time ? 3 : variant_code(fl))
                           : (time ? -2 : mixed);
   return (int)attr_fn(math)(v, blk, bps, regs);
 }
 
-int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out, bool time, bool exact) {
+int mcfl_ctx::grid_for(bool uniform, int *block_out, int *bps_out, bool time, bool exact, bool fl) {
   int blk = 0, bps = 0, regs = 0;
-  if (attr(uniform, &blk, &bps, &regs, time, exact) != 0 || bps <= 0) bps = 1;
+  if (attr(uniform, &blk, &bps, &regs, time, exact, fl) != 0 || bps <= 0) bps = 1;
   if (blocks_per_sm > 0 && blocks_per_sm < bps) bps = blocks_per_sm;
   if (bps_out) *bps_out = bps;
   if (block_out) *block_out = blk;
@@ -171,6 +171,10 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
   } else if (k == "variant") {
     if (v < 0 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant: 0..2");
     c->variant = (int)v;
+    c->variant_fl = -1;
+  } else if (k == "variant_fl") {
+    if (v < -1 || v >= MCFL_N_VARIANTS) return fail(MCFL_E_ARG, "variant_fl: -1 (as variant) or 0..2");
+    c->variant_fl = (int)v;
   } else if (k == "phd_agg") {
     if (v < 0 || v > 2) return fail(MCFL_E_ARG, "phd_agg: 0 (one add per pass), 1 (register sums), 2 (warp sums)");
     c->phd_agg = (int)v;
@@ -212,6 +216,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "block") return c->block;
   if (k == "blocks_per_sm") return c->blocks_per_sm;
   if (k == "variant") return c->variant;
+  if (k == "variant_fl") return c->variant_fl;
   if (k == "phd_agg") return c->phd_agg;
   if (k == "pass_form") return c->pass_form;
   if (k == "mixed_variant") return c->mixed_variant;

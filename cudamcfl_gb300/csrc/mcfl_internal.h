@@ -168,8 +168,14 @@ struct mcfl_ctx {
    * register (kernel variants 7..9), 2 adds aggregated per warp (14..16) */
   int phd_agg = 0;
   int pass_form = 0; /* 1: the pass with every test as its own branch (kernel variants 11..13) */
-  /* the single-medium kernel variant the launches use */
-  int variant_code() const { return variant + (phd_agg == 1 ? 7 : phd_agg == 2 ? 14 : pass_form ? 11 : 0); }
+  /* the occupancy variant of the emission phase's launch (-1: variant) */
+  int variant_fl = -1;
+  /* the single-medium kernel variant the launches use (fl: an emission
+   * launch, which tallies no hitting density) */
+  int variant_code(bool fl = false) const {
+    const int v = fl && variant_fl >= 0 ? variant_fl : variant;
+    return v + (phd_agg == 1 ? 7 : phd_agg == 2 ? 14 : pass_form ? 11 : 0);
+  }
   int mixed_variant = 2; /* occupancy variant of the mixed-media kernel (128 x 7 measured fastest) */
   /* the mixed-media kernel variant the launches use (McflLaunch::variant) */
   int mixed_code() const { return mixed_variant + (pass_form ? 3 : 0); }
@@ -183,8 +189,9 @@ struct mcfl_ctx {
 
   /* Grid (SMs x resident blocks) and threads per block of the single-medium
    * (uniform) or mixed-media kernel under the current options. */
-  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr, bool time = false, bool exact = false);
-  int attr(bool uniform, int *block, int *bps, int *regs, bool time = false, bool exact = false);
+  int grid_for(bool uniform, int *block_out, int *bps_out = nullptr, bool time = false, bool exact = false,
+               bool fl = false);
+  int attr(bool uniform, int *block, int *bps, int *regs, bool time = false, bool exact = false, bool fl = false);
   cudaError_t launch_transport(const McflLaunch &L, int grid, int block_size);
 };
 

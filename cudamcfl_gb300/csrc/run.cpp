@@ -365,9 +365,9 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
   unsigned long long *cnt = c->counters.as<unsigned long long>();
   const bool exact = run->exact_stepping != 0;
   int block = 0, block_exc = 0;
-  const int grid = c->grid_for(true, &block, nullptr, false, exact);
-  const int grid_exc = timed ? c->grid_for(true, &block_exc, nullptr, true, exact) : grid;
-  if (!timed) block_exc = block;
+  /* the emission launch may run its own occupancy variant */
+  const int grid = c->grid_for(true, &block, nullptr, false, exact, true);
+  const int grid_exc = c->grid_for(true, &block_exc, nullptr, timed, exact);
   const unsigned long long photons = run->photons;
   const unsigned per_voxel = run->photons_per_voxel;
   auto record = [&](cudaStream_t st, unsigned *k) -> cudaError_t {
@@ -410,6 +410,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
       Lf.ticket_counter = cnt + 1;
       Lf.ticket_end_dev = cnt + 3;
       set_uniform(c, Lf, m, true, nullptr, exact);
+      Lf.variant = (uint32_t)c->variant_code(true);
       REC(record_event(c->ev[2], st));
       REC(launch_fn(c->math)(&Lf, grid, block, st));
       ++*k;
@@ -426,6 +427,7 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                   {xy, nv, (unsigned long long)emission, (unsigned long long)fluence, photons,
                                    per_voxel, (unsigned long long)c->math, (unsigned long long)grid,
                                    (unsigned long long)block, c->step_cap, (unsigned long long)c->variant_code(),
+                                   (unsigned long long)c->variant_code(true),
                                    (unsigned long long)c->l2_window, tsize, (unsigned long long)grid_exc,
                                    (unsigned long long)block_exc, (unsigned long long)exact, m->serial});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);

@@ -322,7 +322,9 @@ const char *mcfl_last_error(void);
 
 /* Options: "math" (MCFL_MATH_*), "block" (threads per block, at most the
  * variant's bound), "variant" (occupancy variant of the single-medium kernel:
- * 0 = 256 threads x 4 blocks per SM, 1 = 256 x 5, 2 = 128 x 9),
+ * 0 = 256 threads x 4 blocks per SM, 1 = 256 x 5, 2 = 128 x 9; setting it
+ * also resets "variant_fl"), "variant_fl" (the emission phase's own
+ * occupancy variant in mcfl_run; -1: as "variant"),
  * "mixed_variant" (occupancy variant of the mixed-media kernel that batches
  * over several media and the server run: 0 = 256 x 3, 1 = 256 x 4,
  * 2 = 128 x 7, the default),
@@ -377,9 +379,10 @@ int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_
  * of the pass, and (when the run tallies the photon hitting density) with
  * each form of that tally, on a sample of `run` (sample_photons excitation
  * photons, photons_per_voxel scaled by the same fraction) and keeps the
- * fastest in ctx's options ("variant", "l2_window", "pass_form",
- * "phd_agg"); returns the chosen variant and its photons/s.  No counterpart
- * in the reference. */
+ * fastest in ctx's options ("variant" for the excitation phase, "variant_fl"
+ * for the emission phase, "l2_window", "pass_form", "phd_agg"); returns the
+ * excitation phase's variant and the photons/s of the kept combination.  No
+ * counterpart in the reference. */
 int mcfl_autotune(mcfl_ctx *ctx, const mcfl_medium *medium, const struct mcfl_run_desc *run,
                   unsigned long long sample_photons, int *variant, double *photons_per_s);
 

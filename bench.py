@@ -292,8 +292,14 @@ def main():
                          "source hash) to profiles/transport_fast_traffic.json and exit; --traffic-command names "
                          "the captured command")
     ap.add_argument("--traffic-command", default="")
+    ap.add_argument("--express-period", type=int, default=0,
+                    help="serving: one warp in this many draws the express queue first (0: the server's default)")
+    ap.add_argument("--express-ratio", type=int, default=0,
+                    help="serving: express requests are at most 1/ratio of the head's remaining (0: default)")
     ap.add_argument("--pass-form", type=int, default=0,
                     help="--profile: 0 the pass arranged for the SIMT warp, 1 every test as its own branch")
+    ap.add_argument("--relaunch", type=int, default=0,
+                    help="--profile: free lanes of a warp that start new photons together (0: the context's)")
     ap.add_argument("--phd-agg", type=int, default=0,
                     help="--profile: hitting-density tally, 0 one add per pass, 1 register sums, 2 warp sums")
     args = ap.parse_args()
@@ -543,7 +549,8 @@ def main():
 
     # --- continuous-batching server ---
     if "serving" not in skip:
-        result["serving"] = serve_stream(mc, ctx, local, duration_s=12.0)
+        result["serving"] = serve_stream(mc, ctx, local, duration_s=12.0, express_period=args.express_period,
+                                         express_ratio=args.express_ratio)
 
     # --- precision: the FP32 builds against the FP64 build on identical seeds ---
     if "precision" not in skip:
@@ -615,6 +622,8 @@ def profile_case(args):
     ctx.set_option("variant", args.variant)
     ctx.set_option("pass_form", args.pass_form)
     ctx.set_option("phd_agg", args.phd_agg)
+    if args.relaunch:
+        ctx.set_option("relaunch", args.relaunch)
     m = media.config2(seed=2)
     med = ctx.medium(m.labels, m.bulks, voxel_cm=m.voxel_cm, fluor_map=m.fluor_map)
     rd = mc.run_desc(args.photons, det=m.det, photons_per_voxel=args.per_voxel, fluence=1, seed_exc=1, seed_fl=2,
@@ -629,6 +638,7 @@ def profile_case(args):
                       "steps_fl": r.stats_fl["steps"], "ms_exc": r.ms_exc, "ms_fl": r.ms_fl,
                       "best_ms_exc": best_exc, "best_ms_fl": best_fl,
                       "variant": args.variant, "pass_form": args.pass_form, "phd_agg": args.phd_agg,
+                      "relaunch": ctx.get_option("relaunch"),
                       "regs": ctx.get_option("regs"),
                       "grid": ctx.get_option("grid"),
                       "block": ctx.get_option("launch_block")}), flush=True)
@@ -637,7 +647,8 @@ def profile_case(args):
     return 0
 
 
-def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
+def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4, express_period: int = 0,
+                 express_ratio: int = 0, fifo: bool = True, saturated: bool = True):
     """Poisson arrivals at ~80 % of the measured service rate."""
     from cudamcfl_gb300 import media
     rng = np.random.default_rng(seed)
@@ -665,7 +676,8 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
     lam = 0.8 * rate_photons / mean_photons
     import cudamcfl_gb300 as mcm
     sctx = mcm.Context(device=device, math=ctx_main.get_option("math"))
-    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048)
+    policy = dict(express_period=express_period, express_ratio=express_ratio)
+    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048, **policy)
     ids, plain_ms_est = [], 0.0
     arrivals = []  # (offset s, pool index, run desc) to replay through a FIFO
     t_start = time.perf_counter()
@@ -695,68 +707,70 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4):
     srv.close()
     photons_total = sum(p for _, p in ids)
     served = photons_total / mtr["span_s"] if mtr["span_s"] > 0 else None
+    out = {"requests": len(ids), "arrival_rate_per_s": lam, "target_load": 0.8, "p50_ms": mtr["p50_ms"],
+           "p99_ms": mtr["p99_ms"], "max_ms": mtr["max_ms"], "mean_ms": float(np.mean(served_lat)),
+           "photons_per_s": served, "express_period": express_period, "express_ratio": express_ratio,
+           "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
+           "slices": mtr["slices"], "server_busy_s": mtr["busy_s"], "server_upload_s": mtr["upload_s"],
+           "server_finish_s": mtr["finish_s"], "server_span_s": mtr["span_s"],
+           "workload": "Poisson requests at 80 % of the calibrated single-run rate, own media 64^3..256x256x128 "
+                       "(labels + fp32 map), 1e5..1e8 photons log-uniform, Gaussian beam or 4x4 cm wide field; "
+                       "saturated: 24 such requests queued at once vs run one per launch (upload, run, read back)"}
+    out["slowest"] = {"served": sorted(((round(l, 1), p) for l, p in zip(served_lat, sizes)), reverse=True)[:4],
+                      "note": "(latency ms, photons) of the four slowest requests"}
 
-    # the same arrivals through a FIFO that runs one request at a time
-    # (upload, run, read back), the plain schedule a queue alone gives
-    fifo_lat = []
-    t0 = time.perf_counter()
-    for off, lab, bulks, vox, fmap, rd in arrivals:
-        now = time.perf_counter() - t0
-        if now < off:
-            time.sleep(off - now)
-        med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
-        sctx.run(med, rd, images=False, raw=True)
-        med.free()
-        fifo_lat.append(1e3 * (time.perf_counter() - t0 - off))
-    fifo_span = time.perf_counter() - t0
+    if fifo:
+        # the same arrivals through a FIFO that runs one request at a time
+        # (upload, run, read back), the plain schedule a queue alone gives
+        fifo_lat = []
+        t0 = time.perf_counter()
+        for off, lab, bulks, vox, fmap, rd in arrivals:
+            now = time.perf_counter() - t0
+            if now < off:
+                time.sleep(off - now)
+            med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
+            sctx.run(med, rd, images=False, raw=True)
+            med.free()
+            fifo_lat.append(1e3 * (time.perf_counter() - t0 - off))
+        fifo_span = time.perf_counter() - t0
+        out["fifo"] = {"p50_ms": float(np.percentile(fifo_lat, 50)), "p99_ms": float(np.percentile(fifo_lat, 99)),
+                       "mean_ms": float(np.mean(fifo_lat)),
+                       "max_ms": float(np.max(fifo_lat)), "photons_per_s": photons_total / fifo_span,
+                       "note": "the same arrivals, one request at a time in arrival order"}
+        out["slowest"]["fifo"] = sorted(((round(l, 1), p) for l, p in zip(fifo_lat, sizes)), reverse=True)[:4]
 
-    # saturation: the same kind of requests all queued at once (served), and
-    # one request per launch after another (plain), same requests both ways
-    burst = []
-    for i in range(24):
-        photons = int(math.exp(rng.uniform(math.log(1e5), math.log(1e8))))
-        lab, bulks, vox, fmap = pool[int(rng.integers(0, len(pool)))]
-        wide = rng.uniform() < 0.5
-        burst.append((lab, bulks, vox, fmap, mcm.run_desc(photons, det=det, seed_exc=90_000 + i, width=4.0,
-                                                         height=4.0, kind=mcm.SOURCE_WIDEFIELD if wide else
-                                                         mcm.SOURCE_GAUSS_BEAM)))
-    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048)
-    t0 = time.perf_counter()
-    bids = [srv.submit(lab, bulks, vox, rd, fluor_map=fmap) for lab, bulks, vox, fmap, rd in burst]
-    for rid in bids:
-        srv.wait(rid, -1)
-    t_served = time.perf_counter() - t0
-    for rid in bids:
-        srv.result(rid)
-    srv.close()
-    t0 = time.perf_counter()
-    for lab, bulks, vox, fmap, rd in burst:
-        med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
-        sctx.run(med, rd, images=False, raw=True)
-        med.free()
-    t_plain = time.perf_counter() - t0
+    if saturated:
+        # saturation: the same kind of requests all queued at once (served),
+        # and one request per launch after another (plain), same requests
+        burst = []
+        for i in range(24):
+            photons = int(math.exp(rng.uniform(math.log(1e5), math.log(1e8))))
+            lab, bulks, vox, fmap = pool[int(rng.integers(0, len(pool)))]
+            wide = rng.uniform() < 0.5
+            burst.append((lab, bulks, vox, fmap, mcm.run_desc(photons, det=det, seed_exc=90_000 + i, width=4.0,
+                                                             height=4.0, kind=mcm.SOURCE_WIDEFIELD if wide else
+                                                             mcm.SOURCE_GAUSS_BEAM)))
+        srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048, **policy)
+        t0 = time.perf_counter()
+        bids = [srv.submit(lab, bulks, vox, rd, fluor_map=fmap) for lab, bulks, vox, fmap, rd in burst]
+        for rid in bids:
+            srv.wait(rid, -1)
+        t_served = time.perf_counter() - t0
+        for rid in bids:
+            srv.result(rid)
+        srv.close()
+        t0 = time.perf_counter()
+        for lab, bulks, vox, fmap, rd in burst:
+            med = sctx.medium(lab, bulks, voxel_cm=vox, fluor_map=fmap)
+            sctx.run(med, rd, images=False, raw=True)
+            med.free()
+        t_plain = time.perf_counter() - t0
+        burst_photons = sum(b[4].photons for b in burst)
+        out["saturated"] = {"requests": len(burst), "photons": burst_photons,
+                            "served_photons_per_s": burst_photons / t_served,
+                            "plain_photons_per_s": burst_photons / t_plain, "served_over_plain": t_plain / t_served}
     sctx.close()
-    burst_photons = sum(b[4].photons for b in burst)
-    return {"requests": len(ids), "arrival_rate_per_s": lam, "target_load": 0.8, "p50_ms": mtr["p50_ms"],
-            "p99_ms": mtr["p99_ms"], "max_ms": mtr["max_ms"], "mean_ms": float(np.mean(served_lat)),
-            "photons_per_s": served,
-            "fifo": {"p50_ms": float(np.percentile(fifo_lat, 50)), "p99_ms": float(np.percentile(fifo_lat, 99)),
-                     "mean_ms": float(np.mean(fifo_lat)),
-                     "max_ms": float(np.max(fifo_lat)), "photons_per_s": photons_total / fifo_span,
-                     "note": "the same arrivals, one request at a time in arrival order"},
-            "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
-            "slices": mtr["slices"], "server_busy_s": mtr["busy_s"], "server_upload_s": mtr["upload_s"],
-            "server_finish_s": mtr["finish_s"], "server_span_s": mtr["span_s"],
-            "slowest": {"served": sorted(((round(l, 1), p) for l, p in zip(served_lat, sizes)), reverse=True)[:4],
-                        "fifo": sorted(((round(l, 1), p) for l, p in zip(fifo_lat, sizes)), reverse=True)[:4],
-                        "note": "(latency ms, photons) of the four slowest requests"},
-            "saturated": {"requests": len(burst), "photons": burst_photons,
-                          "served_photons_per_s": burst_photons / t_served,
-                          "plain_photons_per_s": burst_photons / t_plain, "served_over_plain": t_plain / t_served},
-            "workload": "Poisson requests at 80 % of the calibrated single-run rate, own media 64^3..256x256x128 "
-                        "(labels + fp32 map), 1e5..1e8 photons log-uniform, Gaussian beam or 4x4 cm wide field; "
-                        "saturated: 24 such requests queued at once vs run one per launch (upload, run, read back)"}
-
+    return out
 
 if __name__ == "__main__":
     sys.exit(main())

@@ -189,6 +189,9 @@ extern "C" int mcfl_set_option(mcfl_ctx *c, const char *key, long long v) {
   } else if (k == "step_cap") {
     if (v < 1 || v > 0x7fffffffLL) return fail(MCFL_E_ARG, "step_cap: 1..2^31-1");
     c->step_cap = (uint32_t)v;
+  } else if (k == "relaunch") {
+    if (v < 1 || v > 32) return fail(MCFL_E_ARG, "relaunch: 1..32");
+    c->relaunch = (uint32_t)v;
   } else if (k == "l2_window") {
     MCFL_CUDA_TRY(cudaSetDevice(c->device));
     if (v) {
@@ -222,6 +225,7 @@ extern "C" long long mcfl_get_option(mcfl_ctx *c, const char *key) {
   if (k == "mixed_variant") return c->mixed_variant;
   if (k == "step_cap") return c->step_cap;
   if (k == "l2_window") return c->l2_window;
+  if (k == "relaunch") return c->relaunch;
   if (k == "graphs") return c->use_graphs;
   if (k == "graph_failed") return c->graph_error.empty() ? 0 : 1;
   if (k == "sm_count") return c->sm_count;

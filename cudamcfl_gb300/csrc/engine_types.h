@@ -155,14 +155,14 @@ typedef struct McflLaunch {
   unsigned long long *ticket_counter;
   uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */
   const unsigned long long *ticket_end_dev; /* ticket end written by an earlier kernel */
-  /* A second ticket queue (mixed-media launches): one warp in four draws
-   * from the first queue, the others from the second, each from the other
-   * once its own is exhausted.  NULL order2: one queue. */
+  /* A second ticket queue (mixed-media launches): one warp in
+   * express_period draws from the first queue, the others from the second,
+   * each from the other once its own is exhausted.  NULL order2: one queue. */
   const uint32_t *order2;
   unsigned long long *ticket_counter2;
   uint64_t ticket_end2;
   uint32_t n_jobs2;
-  uint32_t pad3;
+  uint32_t express_period; /* two queues: warp w draws from the first queue first when w % period == 0 (0: 4) */
   const uint32_t *mult; /* 32768 MWC multipliers */
   McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
@@ -170,6 +170,9 @@ typedef struct McflLaunch {
   uint32_t variant;        /* occupancy variant of the single-medium kernel */
   uint32_t time_on;        /* 1: carry the time of flight (some job has time-resolved detectors) */
   uint32_t exact_step;     /* 1: voxel-boundary stepping (single voxelized medium) */
+  /* lanes of a warp without a photon wait until at least this many are
+   * free (or every lane is), then draw new photons together (0: 1) */
+  uint32_t relaunch_min;
   float l2_hit_ratio;      /* host side: persisting-L2 window over [l2_base, +l2_bytes) when l2_bytes > 0 */
   const void *l2_base;
   unsigned long long l2_bytes;

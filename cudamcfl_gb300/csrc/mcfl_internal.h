@@ -181,6 +181,7 @@ struct mcfl_ctx {
   int mixed_code() const { return mixed_variant + (pass_form ? 3 : 0); }
   int blocks_per_sm = 0;
   uint32_t step_cap = 1u << 24;
+  uint32_t relaunch = 1; /* McflLaunch::relaunch_min */
   int l2_window = 0;            /* 1: persisting-L2 window over the medium's labels */
   size_t l2_persist_bytes = 0;  /* persisting set-aside this context asked for */
   size_t l2_max_window = 0;     /* cudaDevAttrMaxAccessPolicyWindowSize */

@@ -219,6 +219,7 @@ McflLaunch base_launch(mcfl_ctx *c) {
   L.mult = c->mult.as<uint32_t>();
   L.step_cap = c->step_cap;
   L.variant = (uint32_t)c->variant_code();
+  L.relaunch_min = c->relaunch;
   return L;
 }
 
@@ -429,7 +430,8 @@ extern "C" int mcfl_run(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_desc *
                                    (unsigned long long)block, c->step_cap, (unsigned long long)c->variant_code(),
                                    (unsigned long long)c->variant_code(true),
                                    (unsigned long long)c->l2_window, tsize, (unsigned long long)grid_exc,
-                                   (unsigned long long)block_exc, (unsigned long long)exact, m->serial});
+                                   (unsigned long long)block_exc, (unsigned long long)exact, m->serial,
+                                   c->relaunch});
   rc = replay(c, &c->graph_run, &c->graph_run_key, &c->graph_run_kernels, key, record);
   if (rc != MCFL_OK) return rc;
 
@@ -626,7 +628,7 @@ extern "C" int mcfl_batch_run_media(mcfl_ctx *c, const mcfl_medium *const *media
                 {N, xy, tickets, (unsigned long long)c->math, (unsigned long long)grid, (unsigned long long)block,
                  c->step_cap, (unsigned long long)c->variant_code(), (unsigned long long)c->l2_window,
                  (unsigned long long)uniform, (unsigned long long)exact, m->serial, tsize,
-                 (unsigned long long)c->mixed_code()});
+                 (unsigned long long)c->mixed_code(), c->relaunch});
     const int rcb = replay(c, &c->graph_batch, &c->graph_batch_key, &c->graph_batch_kernels, key, record);
     if (rcb != MCFL_OK) return rcb;
     MCFL_CUDA_TRY(cudaStreamSynchronize(s));

@@ -80,6 +80,7 @@ struct mcfl_server {
   size_t budget = 0, used = 0;
   unsigned slots = 64;
   uint32_t slice_iters = 2048; /* passes per slice while requests wait */
+  uint32_t express_period = 4, express_ratio = 8; /* see mcfl_server_opts */
   uint32_t slice_cur = 2048;   /* grows to 8 x slice_iters while none waits */
   std::mutex mu;
   std::condition_variable cv, cv_done;
@@ -279,14 +280,15 @@ void mcfl_server::loop() {
     }
     upload_s += std::chrono::duration<double>(Clock::now() - t_up0).count();
     /* Tickets of this slice, in two queues: the oldest admitted request
-     * alone in the second (three warps in four); in the first (one warp in
-     * four) the requests at most an eighth of its remaining size, shortest
-     * remaining first; each warp turns to the other queue once its own is
-     * exhausted.  Larger requests wait for the head, in admission order.  So
-     * a small request arriving behind a large one starts at once on a
-     * quarter of the GPU, and large requests keep their admission order and
-     * at least three quarters of the GPU.  Photon k of a request still draws the stream of index k,
-     * whatever slice or queue hands it out. */
+     * alone in the second (drawn first by all warps but one in
+     * express_period); in the first (one warp in express_period) the
+     * requests whose remaining size is at most 1/express_ratio of the head's,
+     * shortest remaining first; each warp turns to the other queue once its
+     * own is exhausted.  Larger requests wait for the head, in admission
+     * order.  So a small request arriving behind a large one starts at once
+     * on a share of the GPU, and large requests keep their admission order
+     * and the rest of the GPU.  Photon k of a request still draws the stream
+     * of index k, whatever slice or queue hands it out. */
     unsigned n = 0, n_active = 0;
     int head = -1;
     std::vector<uint32_t> h_stat_slot;
@@ -316,7 +318,8 @@ void mcfl_server::loop() {
       unsigned w = 0;
       for (unsigned i = 0; i < n; ++i) {
         const Request &r = *active[h_order[i]];
-        if ((int)h_order[i] != head && (r.run.photons - r.started) * 8 <= head_left) h_order[w++] = h_order[i];
+        if ((int)h_order[i] != head && (r.run.photons - r.started) * express_ratio <= head_left)
+          h_order[w++] = h_order[i];
       }
       n0 = w;
       if (n0 == 0) {
@@ -361,6 +364,7 @@ void mcfl_server::loop() {
       L.ticket_end2 = tickets_end2;
     }
     L.max_iters = slice_cur;
+    L.express_period = express_period;
     L.variant = (uint32_t)ctx->mixed_code();
     L.exact_step = (mode & 1u) ? 1u : 0u;
     L.time_on = (mode & 2u) ? 1u : 0u;
@@ -369,6 +373,7 @@ void mcfl_server::loop() {
     L.mult = ctx->mult.as<uint32_t>();
     L.saved = parked[mode].as<McflSaved>();
     L.step_cap = ctx->step_cap;
+    L.relaunch_min = ctx->relaunch;
     cudaError_t e = ctx->launch_transport(L, grid_m[mode], block_m[mode]);
     cudaMemcpyAsync(h_read, counter.p, 16, cudaMemcpyDeviceToHost, s);
     for (unsigned i = 0; i < n_active; ++i) {
@@ -461,6 +466,8 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   sv->slots = opts && opts->max_jobs ? (unsigned)opts->max_jobs : 64u;
   sv->slice_iters = opts && opts->slice_passes ? (uint32_t)opts->slice_passes : 2048u;
   sv->slice_cur = sv->slice_iters;
+  if (opts && opts->express_period) sv->express_period = opts->express_period;
+  if (opts && opts->express_ratio) sv->express_ratio = opts->express_ratio;
   if (sv->slots > 4096) {
     delete sv;
     return fail(MCFL_E_RANGE, "max_jobs above 4096");

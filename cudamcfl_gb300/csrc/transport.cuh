@@ -769,7 +769,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   /* the warp's ticket queue and which queues it found exhausted (warp-uniform;
    * a missing second queue counts as exhausted) */
   const bool two_queues = !kUniform && L.order2 != nullptr;
-  uint32_t q = two_queues ? (((gtid >> 5) & 3u) != 0u ? 1u : 0u) : 0u;
+  const uint32_t period = L.express_period ? L.express_period : 4u;
+  uint32_t q = two_queues ? (((uint32_t)(gtid >> 5) % period) != 0u ? 1u : 0u) : 0u;
   bool ex0 = false, ex1 = !two_queues;
   Photon p;
   Rng r;
@@ -867,7 +868,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
      * that run this pass (lanes without a photon skip it), the member mask
      * of any warp-wide operation inside the pass */
     unsigned live = kFull;
-    if (__ballot_sync(kFull, !alive)) {
+    const unsigned dead = __ballot_sync(kFull, !alive);
+    if (dead) {
+    /* lanes without a photon draw new ones together once at least
+     * relaunch_min of them are free (0 or 1: at once), or every lane is;
+     * until then they skip the pass below */
+    if ((uint32_t)__popc(dead) >= L.relaunch_min || dead == kFull) {
     const bool need = !alive && !(ex0 && ex1);
     const unsigned nm = __ballot_sync(kFull, need);
     if (nm) {
@@ -915,8 +921,9 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       }
     }
     if (__all_sync(kFull, !alive) && ex0 && ex1) break;
+    }
     if constexpr (kPhdWarp) live = __ballot_sync(kFull, alive);
-    if (!alive) continue;
+    if (!alive) continue; /* a lane without a photon never runs the pass */
     }
 
     if constexpr (!kExactStep) ++pst;

@@ -336,7 +336,12 @@ const char *mcfl_last_error(void);
  * per voxel, one add per distinct voxel; the tallies are the same),
  * "pass_form" (0: the single-medium pass arranged for the SIMT warp, the
  * common case straight-line and every rare case behind one branch; 1: every
- * test of the reference's pass as its own branch; the tallies are the same).
+ * test of the reference's pass as its own branch; the tallies are the same),
+ * "relaunch" (1..32: the lanes of a warp whose photons ended wait until at
+ * least this many of them are free, or the warp's tickets are gone, and
+ * then start their next photons together; 1 starts each photon as soon as
+ * its lane is free; every photon still draws its own stream, so the tallies
+ * are the same).
  * The launch shape of the reference is fixed (CUDAMCFL.h:18-20). */
 int mcfl_set_option(mcfl_ctx *ctx, const char *key, long long value);
 long long mcfl_get_option(mcfl_ctx *ctx, const char *key);
@@ -431,6 +436,14 @@ typedef struct mcfl_server_opts {
   unsigned long long hbm_budget_bytes; /* admission budget (0: half the free HBM) */
   unsigned int max_jobs;               /* concurrent jobs (0: 64) */
   unsigned int slice_passes;           /* transport passes per thread per slice (0: 2048) */
+  /* Scheduling of a slice's photon tickets: the oldest admitted request (the
+   * head) has a queue of its own; the requests whose remaining photons are
+   * at most 1/express_ratio of the head's remaining (0: 8) share an express
+   * queue, shortest remaining first, drawn first by one warp in
+   * express_period (0: 4); every warp turns to the other queue when its own
+   * is empty. */
+  unsigned int express_period;
+  unsigned int express_ratio;
 } mcfl_server_opts;
 
 typedef struct mcfl_server_metrics_t {

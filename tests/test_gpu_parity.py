@@ -77,7 +77,16 @@ def test_exact_kernel_launch_shape_does_not_change_tallies(gpu_ctx, oracle, tabl
                     gpu_ctx.set_option("pass_form", form)
                     assert gpu_ctx.get_option("launch_block") == bound
                     _compare(gpu_ctx.run(med, case.run_desc(5, 6)), ref)
+        # free lanes waiting for others before they start new photons
+        gpu_ctx.set_option("l2_window", 0)
+        gpu_ctx.set_option("phd_agg", 0)
+        gpu_ctx.set_option("pass_form", 0)
+        for relaunch in (2, 7, 32):
+            gpu_ctx.set_option("relaunch", relaunch)
+            assert gpu_ctx.get_option("relaunch") == relaunch
+            _compare(gpu_ctx.run(med, case.run_desc(5, 6)), ref)
     finally:
+        gpu_ctx.set_option("relaunch", 1)
         gpu_ctx.set_option("block", 256)
         gpu_ctx.set_option("blocks_per_sm", 0)
         gpu_ctx.set_option("variant", 0)
@@ -238,6 +247,10 @@ def test_bad_inputs_fail_with_status(gpu_ctx):
     with pytest.raises(mc.McflError) as e:
         gpu_ctx.medium(lab, case.bulks(), vox_per_cm=(4.0, 4.0, 4.0), half_x=1.0, half_y=1.0, thickness=0.5)
     assert e.value.code == mc.E_ARG
+    for bad in (0, 33):
+        with pytest.raises(mc.McflError) as e:
+            gpu_ctx.set_option("relaunch", bad)
+        assert e.value.code == mc.E_ARG
     gpu_ctx.set_option("step_cap", 50)  # photons live for hundreds of passes: the cap must report
     try:
         with pytest.raises(mc.McflError) as e:

@@ -112,8 +112,9 @@ def _request_media(seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("slice_passes", [64, 4096])
-def test_server_results_equal_alone(slice_passes, gpu_ctx):
+@pytest.mark.parametrize("slice_passes,express_period,express_ratio,relaunch",
+                         [(64, 0, 0, 1), (4096, 0, 0, 1), (64, 2, 2, 8), (256, 7, 1, 32)])
+def test_server_results_equal_alone(slice_passes, express_period, express_ratio, relaunch, gpu_ctx):
     meds = _request_media(7)
     det = mc.Detector(0.0, 0.0, 0.05, 0.05, 30, 30)
     reqs = []
@@ -124,7 +125,9 @@ def test_server_results_equal_alone(slice_passes, gpu_ctx):
                          seed_exc=500 + i, kind=kind, width=1.0, height=0.8)
         reqs.append((lab, bulks, vox, rd))
     ctx2 = mc.Context(math=mc.MATH_EXACT)
-    srv = mc.Server(ctx2, hbm_budget_bytes=64 << 20, max_jobs=4, slice_passes=slice_passes)
+    ctx2.set_option("relaunch", relaunch)
+    srv = mc.Server(ctx2, hbm_budget_bytes=64 << 20, max_jobs=4, slice_passes=slice_passes,
+                    express_period=express_period, express_ratio=express_ratio)
     try:
         ids = [srv.submit(lab, bulks, vox, rd) for lab, bulks, vox, rd in reqs]
         results = []

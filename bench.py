@@ -393,7 +393,7 @@ def main():
                    "pass_form": ctx.get_option("pass_form"),
                    "block": ctx.get_option("launch_block"), "grid": ctx.get_option("grid"),
                    "regs": ctx.get_option("regs"), "l2_window": ctx.get_option("l2_window"),
-                   "phd_agg": ctx.get_option("phd_agg"),
+                   "phd_agg": ctx.get_option("phd_agg"), "relaunch": ctx.get_option("relaunch"),
                    "autotune_sample_photons_per_s": tune_rate},
         "phases": {"excitation_ms": statistics.mean(exc_ms), "emission_ms": statistics.mean(fl_ms),
                    "excitation_photons_per_s": EXC_PHOTONS / (statistics.mean(exc_ms) / 1e3),
@@ -677,7 +677,7 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4, 
     import cudamcfl_gb300 as mcm
     sctx = mcm.Context(device=device, math=ctx_main.get_option("math"))
     policy = dict(express_period=express_period, express_ratio=express_ratio)
-    srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048, **policy)
+    srv = mcm.Server(sctx, max_jobs=64, **policy)
     ids, plain_ms_est = [], 0.0
     arrivals = []  # (offset s, pool index, run desc) to replay through a FIFO
     t_start = time.perf_counter()
@@ -750,7 +750,7 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4, 
             burst.append((lab, bulks, vox, fmap, mcm.run_desc(photons, det=det, seed_exc=90_000 + i, width=4.0,
                                                              height=4.0, kind=mcm.SOURCE_WIDEFIELD if wide else
                                                              mcm.SOURCE_GAUSS_BEAM)))
-        srv = mcm.Server(sctx, max_jobs=64, slice_passes=2048, **policy)
+        srv = mcm.Server(sctx, max_jobs=64, **policy)
         t0 = time.perf_counter()
         bids = [srv.submit(lab, bulks, vox, rd, fluor_map=fmap) for lab, bulks, vox, fmap, rd in burst]
         for rid in bids:

@@ -140,7 +140,8 @@ SCHEDULE_PLAIN = 1
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_ulonglong), ("max_jobs", ctypes.c_uint),
-                ("slice_passes", ctypes.c_uint), ("express_period", ctypes.c_uint), ("express_ratio", ctypes.c_uint)]
+                ("slice_passes", ctypes.c_uint), ("express_period", ctypes.c_uint), ("express_ratio", ctypes.c_uint),
+                ("slice_us", ctypes.c_uint)]
 
 
 class ServerMetrics(ctypes.Structure):
@@ -579,8 +580,8 @@ class Server:
     """Continuous-batching server over one context."""
 
     def __init__(self, ctx: "Context", hbm_budget_bytes: int = 0, max_jobs: int = 0, slice_passes: int = 0,
-                 express_period: int = 0, express_ratio: int = 0):
-        o = ServerOpts(hbm_budget_bytes, max_jobs, slice_passes, express_period, express_ratio)
+                 express_period: int = 0, express_ratio: int = 0, slice_us: int = 0):
+        o = ServerOpts(hbm_budget_bytes, max_jobs, slice_passes, express_period, express_ratio, slice_us)
         h = ctypes.c_void_p()
         check(load().mcfl_server_create(ctx.handle, ctypes.byref(o), ctypes.byref(h)))
         self.handle = h

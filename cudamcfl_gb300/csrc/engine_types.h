@@ -152,6 +152,10 @@ typedef struct McflLaunch {
   const uint32_t *order; /* slots sorted by ticket_begin, or NULL: slots 0..n_jobs-1 in order */
   uint32_t n_jobs;       /* entries of order (or slots) */
   uint32_t max_iters; /* loop iterations per launch; 0 = run until no ticket is left */
+  /* a slice (mixed-media launches with saved): every warp stops at the
+   * first multiple of 16 iterations at least slice_ns after its start
+   * (0: no time limit); with max_iters, whichever comes first */
+  uint64_t slice_ns;
   unsigned long long *ticket_counter;
   uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */
   const unsigned long long *ticket_end_dev; /* ticket end written by an earlier kernel */
@@ -164,7 +168,7 @@ typedef struct McflLaunch {
   uint32_t n_jobs2;
   uint32_t express_period; /* two queues: warp w draws from the first queue first when w % period == 0 (0: 4) */
   const uint32_t *mult; /* 32768 MWC multipliers */
-  McflSaved *saved;     /* one per thread of the grid, when max_iters > 0 */
+  McflSaved *saved;     /* one per thread of the grid, when max_iters or slice_ns > 0 */
   uint32_t step_cap;    /* passes after which a photon is stopped and counted in MCFL_ST_CAPPED */
   uint32_t uniform_medium; /* 1: every job uses med (and fhd_on agrees with med.fhd) */
   uint32_t variant;        /* occupancy variant of the single-medium kernel */

@@ -79,9 +79,12 @@ struct mcfl_server {
   mcfl_ctx *ctx = nullptr;
   size_t budget = 0, used = 0;
   unsigned slots = 64;
-  uint32_t slice_iters = 2048; /* passes per slice while requests wait */
+  /* a slice's limits while requests wait: passes per thread (0: none) and
+   * nanoseconds; both grow to 8 times while none waits (slice_mult) */
+  uint32_t slice_iters = 0;
+  uint64_t slice_ns = 2000000;
+  uint32_t slice_mult = 1;
   uint32_t express_period = 4, express_ratio = 8; /* see mcfl_server_opts */
-  uint32_t slice_cur = 2048;   /* grows to 8 x slice_iters while none waits */
   std::mutex mu;
   std::condition_variable cv, cv_done;
   std::deque<std::shared_ptr<Request>> queue;
@@ -262,7 +265,7 @@ void mcfl_server::loop() {
     }
     /* Short slices let waiting requests in soon; with nobody waiting the
      * slices lengthen, which saves the per-slice host round trips. */
-    slice_cur = (waiting || !fresh.empty()) ? slice_iters : std::min(slice_cur * 2u, slice_iters * 8u);
+    slice_mult = (waiting || !fresh.empty()) ? 1u : std::min(slice_mult * 2u, 8u);
     const auto t_up0 = Clock::now();
     for (auto &r : fresh) {
       r->t_admit = Clock::now();
@@ -279,16 +282,18 @@ void mcfl_server::loop() {
       }
     }
     upload_s += std::chrono::duration<double>(Clock::now() - t_up0).count();
-    /* Tickets of this slice, in two queues: the oldest admitted request
-     * alone in the second (drawn first by all warps but one in
-     * express_period); in the first (one warp in express_period) the
-     * requests whose remaining size is at most 1/express_ratio of the head's,
-     * shortest remaining first; each warp turns to the other queue once its
-     * own is exhausted.  Larger requests wait for the head, in admission
-     * order.  So a small request arriving behind a large one starts at once
-     * on a share of the GPU, and large requests keep their admission order
-     * and the rest of the GPU.  Photon k of a request still draws the stream
-     * of index k, whatever slice or queue hands it out. */
+    /* Tickets of this slice, in two queues.  The head queue: the oldest
+     * admitted request (the head), then the other requests larger than
+     * 1/express_ratio of the head's remaining photons, in admission order,
+     * which take over the warps as the head's tickets run out (no warp idles
+     * while its last photons finish).  The express queue: the requests at
+     * most 1/express_ratio of the head's remaining, shortest remaining
+     * first, drawn first by one warp in express_period; every warp turns to
+     * the other queue once its own is exhausted.  So a small request
+     * arriving behind a large one starts at once on a share of the GPU, and
+     * large requests keep their admission order and the rest of the GPU.
+     * Photon k of a request still draws the stream of index k, whatever
+     * slice or queue hands it out. */
     unsigned n = 0, n_active = 0;
     int head = -1;
     std::vector<uint32_t> h_stat_slot;
@@ -300,40 +305,40 @@ void mcfl_server::loop() {
     unsigned mode = next_mode;
     while (!(have & (1u << mode))) mode = (mode + 1) % kModes;
     next_mode = (mode + 1) % kModes;
+    auto older = [&](uint32_t a, uint32_t b) {
+      return active[a]->t_admit != active[b]->t_admit ? active[a]->t_admit < active[b]->t_admit
+                                                      : active[a]->id < active[b]->id;
+    };
     for (unsigned i = 0; i < slots; ++i)
       if (active[i]) {
         ++n_active;
         h_stat_slot.push_back(i);
         if (active[i]->mode == mode && active[i]->started < active[i]->run.photons) {
           h_order[n++] = i;
-          if (head < 0 || active[i]->t_admit < active[head]->t_admit ||
-              (active[i]->t_admit == active[head]->t_admit && active[i]->id < active[head]->id))
-            head = (int)i;
+          if (head < 0 || older(i, (uint32_t)head)) head = (int)i;
         }
       }
     if (n_active == 0) continue;
     unsigned n0 = n, n2 = 0;
-    if (n > 1) { /* the head leaves the first queue for the second */
-      const uint64_t head_left = active[head]->run.photons - active[head]->started;
-      unsigned w = 0;
+    if (n > 1) {
+      auto left = [&](uint32_t a) { return active[a]->run.photons - active[a]->started; };
+      const uint64_t head_left = left((uint32_t)head);
+      std::vector<uint32_t> express, main_q{(uint32_t)head}, rest;
       for (unsigned i = 0; i < n; ++i) {
-        const Request &r = *active[h_order[i]];
-        if ((int)h_order[i] != head && (r.run.photons - r.started) * express_ratio <= head_left)
-          h_order[w++] = h_order[i];
+        if ((int)h_order[i] == head) continue;
+        (left(h_order[i]) * express_ratio <= head_left ? express : rest).push_back(h_order[i]);
       }
-      n0 = w;
-      if (n0 == 0) {
-        h_order[0] = (uint32_t)head;
-        n0 = 1;
-      } else {
-        h_order[n0] = (uint32_t)head;
-        n2 = 1;
-      }
+      std::sort(express.begin(), express.end(),
+                [&](uint32_t a, uint32_t b) { return left(a) != left(b) ? left(a) < left(b) : a < b; });
+      std::sort(rest.begin(), rest.end(), older);
+      main_q.insert(main_q.end(), rest.begin(), rest.end());
+      /* the first queue (express, if any) and the second (the head queue) */
+      unsigned w = 0;
+      for (uint32_t x : express) h_order[w++] = x;
+      for (uint32_t x : main_q) h_order[w++] = x;
+      n0 = express.empty() ? (unsigned)main_q.size() : (unsigned)express.size();
+      n2 = express.empty() ? 0u : (unsigned)main_q.size();
     }
-    std::sort(h_order, h_order + n0, [&](uint32_t a, uint32_t b) {
-      const uint64_t ra = active[a]->run.photons - active[a]->started, rb = active[b]->run.photons - active[b]->started;
-      return ra != rb ? ra < rb : a < b;
-    });
     uint64_t tickets = 0, tickets2 = 0;
     for (unsigned i = 0; i < n0 + n2; ++i) {
       Request &r = *active[h_order[i]];
@@ -363,7 +368,8 @@ void mcfl_server::loop() {
       L.ticket_counter2 = counter.as<unsigned long long>() + 1;
       L.ticket_end2 = tickets_end2;
     }
-    L.max_iters = slice_cur;
+    L.max_iters = (uint32_t)std::min<uint64_t>((uint64_t)slice_iters * slice_mult, 0xffffffffull);
+    L.slice_ns = slice_ns * slice_mult;
     L.express_period = express_period;
     L.variant = (uint32_t)ctx->mixed_code();
     L.exact_step = (mode & 1u) ? 1u : 0u;
@@ -464,8 +470,8 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   cudaMemGetInfo(&free_b, &total_b);
   sv->budget = opts && opts->hbm_budget_bytes ? (size_t)opts->hbm_budget_bytes : free_b / 2;
   sv->slots = opts && opts->max_jobs ? (unsigned)opts->max_jobs : 64u;
-  sv->slice_iters = opts && opts->slice_passes ? (uint32_t)opts->slice_passes : 2048u;
-  sv->slice_cur = sv->slice_iters;
+  sv->slice_iters = opts ? (uint32_t)opts->slice_passes : 0u;
+  if (opts && opts->slice_us) sv->slice_ns = (uint64_t)opts->slice_us * 1000u;
   if (opts && opts->express_period) sv->express_period = opts->express_period;
   if (opts && opts->express_ratio) sv->express_ratio = opts->express_ratio;
   if (sv->slots > 4096) {

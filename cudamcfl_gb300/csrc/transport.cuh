@@ -166,6 +166,13 @@ struct Photon {
   int ix, iy, iz;
 };
 
+/* The GPU's global nanosecond clock (PTX %globaltimer). */
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 /* Time-of-flight increment (unsigned long)(v / c) of a path of optical
  * length v [cm] (CUDAMCFLtransport.cu:316,725,832,840; c = 2.99792e-5 cm/fs,
  * CUDAMCFL.h:29), converted with saturation (a negative value adds 0). */
@@ -413,7 +420,11 @@ __device__ __forceinline__ Rec rec_of(float4 q) {
  * expressions, with its per-label subexpressions (1-g^2, 1-g, 2g, 1+g^2)
  * taken from the label record: the same roundings.  The fast kernel uses
  * reciprocals and one reciprocal square root for the rotation instead of
- * divisions: the same physics at fast-math accuracy. */
+ * divisions, and an isotropic label (g = 0) takes cos(theta) = 2u - 1 from
+ * the uniform u already drawn for the Henyey-Greenstein form instead of a
+ * second draw (the reference's g = 0 branch draws again): the same
+ * distribution, one random number fewer, no predicated draw in every
+ * pass. */
 __device__ __forceinline__ void spin(Photon &p, const Rec &c, Rng &r) {
   real cost, sint, cosp, sinp;
   const real two_g = c.b.x;
@@ -441,9 +452,10 @@ __device__ __forceinline__ void spin(Photon &p, const Rec &c, Rng &r) {
   p.dy = p.dy * temp;
   p.dz = p.dz * temp;
 #else
-  const real temp = c.a.z / (c.a.w + two_g * r.co());
+  const real u_hg = r.co();
+  const real temp = c.a.z / (c.a.w + two_g * u_hg);
   cost = (c.b.y - temp * temp) * c.b.z;
-  if (two_g == MCFL_C(0.0)) cost = MCFL_C(2.0) * r.co() - MCFL_C(1.0);
+  if (two_g == MCFL_C(0.0)) cost = MCFL_C(2.0) * u_hg - MCFL_C(1.0);
   sint = MCFL_SQRT(MCFL_C(1.0) - cost * cost);
   /* 2*pi*co() with the 2^-32 scale folded into the constant: the same value */
   __sincosf((MCFL_C(2.0) * kPi * MCFL_C(0x1p-32)) * r.raw(), &cosp, &sinp);
@@ -828,7 +840,12 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (v) atomicAdd((unsigned long long *)__ldg((const unsigned long long *)&J->stats) + e, v);
   };
 
-  if (!kUniform && L.max_iters && L.saved) {
+  /* a slice of a served run: photons in flight are parked at its end and
+   * resumed by the next slice */
+  const bool sliced = !kUniform && (L.max_iters || L.slice_ns) && L.saved;
+  uint64_t t_begin = 0;
+  if (!kUniform && L.slice_ns) t_begin = __shfl_sync(kFull, global_ns(), 0);
+  if (sliced) {
     const McflSaved sv = L.saved[gtid];
     if (sv.alive) {
       job = sv.job;
@@ -864,6 +881,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   for (uint32_t it = 0;; ++it) {
     /* single-medium launches always run to the end of their tickets */
     if (!kUniform && L.max_iters && it >= L.max_iters) break;
+    /* time-limited slice: the warps stop together, whatever their pace
+     * (a warp-uniform test: lane 0's clock) */
+    if (!kUniform && L.slice_ns && (it & 15u) == 0u && __shfl_sync(kFull, global_ns(), 0) - t_begin >= L.slice_ns)
+      break;
     /* one vote per pass while every lane carries a photon; live: the lanes
      * that run this pass (lanes without a photon skip it), the member mask
      * of any warp-wide operation inside the pass */
@@ -1368,7 +1389,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   if (alive) steps += pst - pst0; /* passes of the photon parked by this slice */
   if (kPhdAgg && f_acc) atomicAdd(&m.fhd[f_idx], f_acc);
 
-  if (!kUniform && L.max_iters && L.saved) {
+  if (sliced) {
     McflSaved sv;
     sv.alive = alive ? 1u : 0u;
     if (alive) {
@@ -1468,9 +1489,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
 extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, cudaStream_t stream) {
   if (L->uniform_medium && L->med.n_labels > MCFL_MAX_LABELS) return cudaErrorInvalidValue;
 #if MCFL_F64
-  if (L->max_iters) return cudaErrorNotSupported; /* parked photons are stored in single precision */
+  if (L->max_iters || L->slice_ns) return cudaErrorNotSupported; /* parked photons are stored in single precision */
 #endif
-  if (L->max_iters && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
+  if ((L->max_iters || L->slice_ns) && L->uniform_medium) return cudaErrorNotSupported; /* slices run the mixed-media kernel */
   if (L->med.layered && (!L->uniform_medium || 3 * (L->med.n_layers + 3) > (MCFL_MAX_LABELS * MCFL_LAB_FLOATS) / 4))
     return cudaErrorInvalidValue;
   const int v = L->exact_step ? (!L->uniform_medium ? (L->time_on ? -9 : -8) : L->time_on ? 10 : 6)

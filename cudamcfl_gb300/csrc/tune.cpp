@@ -9,7 +9,9 @@
  * pass as its own branch) and two forms of the photon-hitting-density tally
  * (one atomic add per pass, or the sums of successive passes in one voxel
  * held in a register, a form of the branching pass), and can put a
- * persisting L2 access window on the labels and tallies.  Which combination is fastest
+ * persisting L2 access window on the labels and tallies; the SIMT-arranged
+ * pass is also timed with the free lanes of a warp starting new photons in
+ * pairs (option "relaunch" 2).  Which combination is fastest
  * depends on the medium (how often photons change label, how deep they go)
  * and on the emission/excitation mix, so the tuner times every combination on
  * a sample of the caller's own run and keeps the fastest in the context,
@@ -40,23 +42,30 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
   }
   const int old_variant = c->variant, old_variant_fl = c->variant_fl, old_l2 = c->l2_window, old_agg = c->phd_agg,
             old_form = c->pass_form;
+  const uint32_t old_relaunch = c->relaunch;
   /* forms: 0 SIMT-arranged pass, 1 branching pass, and when the run tallies
    * the hitting density 2 the branching pass with the register-held sums,
-   * 3 the SIMT-arranged pass with the warp-aggregated adds */
-  const int n_forms = (r.fluence || r.photons_per_voxel) ? 4 : 2;
+   * 3 the SIMT-arranged pass with the warp-aggregated adds; last, form 0
+   * with relaunch 2.  Each with and without the L2 window. */
+  const int n_forms = (r.fluence || r.photons_per_voxel) ? 5 : 3;
   const int n_cfg = 2 * n_forms;
+  auto apply = [&](int cfg) {
+    const int form = cfg >> 1;
+    const bool pairs = form == n_forms - 1;
+    c->l2_window = cfg & 1;
+    c->phd_agg = pairs ? 0 : form == 2 ? 1 : form == 3 ? 2 : 0;
+    c->pass_form = form == 1 ? 1 : 0;
+    c->relaunch = pairs ? 2u : 1u;
+  };
   /* per (variant, configuration): the best excitation and emission launch
    * times of the sample runs; each phase then takes its fastest variant */
   std::vector<double> ms_exc((size_t)MCFL_N_VARIANTS * n_cfg, 1e30), ms_fl((size_t)MCFL_N_VARIANTS * n_cfg, 1e30);
   double photons = 0.0;
   for (int v = 0; v < MCFL_N_VARIANTS; ++v) {
     for (int cfg = 0; cfg < n_cfg; ++cfg) {
-      const int l2 = cfg & 1, form = cfg >> 1;
       c->variant = v;
       c->variant_fl = -1;
-      c->l2_window = l2;
-      c->phd_agg = form == 2 ? 1 : form == 3 ? 2 : 0;
-      c->pass_form = form == 1 ? 1 : 0;
+      apply(cfg);
       for (int rep = 0; rep < 3; ++rep) { /* the first run records the graph */
         mcfl_run_out o;
         std::memset(&o, 0, sizeof(o));
@@ -67,6 +76,7 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
           c->l2_window = old_l2;
           c->phd_agg = old_agg;
           c->pass_form = old_form;
+          c->relaunch = old_relaunch;
           return rc;
         }
         photons = (double)o.stats_exc[0] + (double)o.stats_fl[0];
@@ -94,12 +104,9 @@ extern "C" int mcfl_autotune(mcfl_ctx *c, const mcfl_medium *m, const mcfl_run_d
       best_vf = r.photons_per_voxel ? vf : ve;
     }
   }
-  const int form = best_cfg >> 1;
   c->variant = best_v;
   c->variant_fl = best_vf;
-  c->l2_window = best_cfg & 1;
-  c->phd_agg = form == 2 ? 1 : form == 3 ? 2 : 0;
-  c->pass_form = form == 1 ? 1 : 0;
+  apply(best_cfg);
   const double rate = best > 0 && best < 1e299 ? photons / (best * 1e-3) : 0.0;
   if (variant_out) *variant_out = best_v;
   if (rate_out) *rate_out = rate;

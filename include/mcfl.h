@@ -381,11 +381,12 @@ size_t mcfl_medium_bytes(const mcfl_medium *medium);
 int mcfl_medium_from_simulation(mcfl_ctx *ctx, const mcfl_simulation *sim, mcfl_medium **medium);
 
 /* Times every kernel variant with and without the L2 window, with each form
- * of the pass, and (when the run tallies the photon hitting density) with
- * each form of that tally, on a sample of `run` (sample_photons excitation
- * photons, photons_per_voxel scaled by the same fraction) and keeps the
- * fastest in ctx's options ("variant" for the excitation phase, "variant_fl"
- * for the emission phase, "l2_window", "pass_form", "phd_agg"); returns the
+ * of the pass, with "relaunch" 1 and 2 for the SIMT-arranged pass, and (when
+ * the run tallies the photon hitting density) with each form of that tally,
+ * on a sample of `run` (sample_photons excitation photons,
+ * photons_per_voxel scaled by the same fraction) and keeps the fastest in
+ * ctx's options ("variant" for the excitation phase, "variant_fl" for the
+ * emission phase, "l2_window", "pass_form", "phd_agg", "relaunch"); returns the
  * excitation phase's variant and the photons/s of the kept combination.  No
  * counterpart in the reference. */
 int mcfl_autotune(mcfl_ctx *ctx, const mcfl_medium *medium, const struct mcfl_run_desc *run,
@@ -435,7 +436,11 @@ typedef struct mcfl_server mcfl_server;
 typedef struct mcfl_server_opts {
   unsigned long long hbm_budget_bytes; /* admission budget (0: half the free HBM) */
   unsigned int max_jobs;               /* concurrent jobs (0: 64) */
-  unsigned int slice_passes;           /* transport passes per thread per slice (0: 2048) */
+  /* A slice (one launch of the transport kernel over the admitted
+   * requests) ends after slice_us microseconds (0: 2000), or after
+   * slice_passes transport passes per thread (0: no such cap), whichever
+   * comes first; both double, up to 8 times, while no request waits. */
+  unsigned int slice_passes;
   /* Scheduling of a slice's photon tickets: the oldest admitted request (the
    * head) has a queue of its own; the requests whose remaining photons are
    * at most 1/express_ratio of the head's remaining (0: 8) share an express
@@ -444,6 +449,7 @@ typedef struct mcfl_server_opts {
    * is empty. */
   unsigned int express_period;
   unsigned int express_ratio;
+  unsigned int slice_us;
 } mcfl_server_opts;
 
 typedef struct mcfl_server_metrics_t {

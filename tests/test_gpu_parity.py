@@ -108,8 +108,10 @@ def test_autotune_keeps_a_variant_and_tallies(gpu_ctx, oracle, table32768):
         assert gpu_ctx.get_option("variant") == variant
         assert gpu_ctx.get_option("phd_agg") in (0, 1, 2)
         assert gpu_ctx.get_option("pass_form") in (0, 1)
+        assert gpu_ctx.get_option("relaunch") in (1, 2)
         _compare(gpu_ctx.run(med, case.run_desc(8, 9)), ref)
     finally:
+        gpu_ctx.set_option("relaunch", 1)
         gpu_ctx.set_option("variant", 0)
         gpu_ctx.set_option("l2_window", 0)
         gpu_ctx.set_option("phd_agg", 0)

@@ -112,9 +112,13 @@ def _request_media(seed):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("slice_passes,express_period,express_ratio,relaunch",
-                         [(64, 0, 0, 1), (4096, 0, 0, 1), (64, 2, 2, 8), (256, 7, 1, 32)])
-def test_server_results_equal_alone(slice_passes, express_period, express_ratio, relaunch, gpu_ctx):
+@pytest.mark.parametrize("slice_passes,slice_us,express_period,express_ratio,relaunch",
+                         [(64, 0, 0, 0, 1), (4096, 0, 0, 0, 1), (64, 0, 2, 2, 8), (256, 0, 7, 1, 32),
+                          (0, 200, 0, 0, 1), (0, 0, 0, 0, 2)])
+def test_server_results_equal_alone(slice_passes, slice_us, express_period, express_ratio, relaunch, gpu_ctx):
+    """Each served result equals the same request run alone, bit for bit, for
+    slices ended by a pass cap or by the clock, any queue policy and any
+    relaunch threshold."""
     meds = _request_media(7)
     det = mc.Detector(0.0, 0.0, 0.05, 0.05, 30, 30)
     reqs = []
@@ -127,7 +131,7 @@ def test_server_results_equal_alone(slice_passes, express_period, express_ratio,
     ctx2 = mc.Context(math=mc.MATH_EXACT)
     ctx2.set_option("relaunch", relaunch)
     srv = mc.Server(ctx2, hbm_budget_bytes=64 << 20, max_jobs=4, slice_passes=slice_passes,
-                    express_period=express_period, express_ratio=express_ratio)
+                    express_period=express_period, express_ratio=express_ratio, slice_us=slice_us)
     try:
         ids = [srv.submit(lab, bulks, vox, rd) for lab, bulks, vox, rd in reqs]
         results = []
@@ -243,7 +247,7 @@ def test_batch_voxel_boundary_stepping_over_several_media_equals_alone(gpu_ctx):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("slice_passes", [64, 4096])
+@pytest.mark.parametrize("slice_passes", [64, 4096, 0])
 def test_server_time_detectors_and_stepping_equal_alone(slice_passes, gpu_ctx):
     """Requests of all four kinds (the reference's or voxel-boundary
     stepping, with or without time-resolved detectors) served together: the

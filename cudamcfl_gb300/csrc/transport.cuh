@@ -778,6 +778,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
 
   const uint64_t ticket_end = L.ticket_end_dev ? *L.ticket_end_dev : L.ticket_end;
   bool alive = false;
+  /* lean single-medium pass: 1/mu_t and n of the photon's label */
+  real mutr_c = MCFL_C(0.0), n_c = MCFL_C(0.0);
   /* the warp's ticket queue and which queues it found exhausted (warp-uniform;
    * a missing second queue counts as exhausted) */
   const bool two_queues = !kUniform && L.order2 != nullptr;
@@ -928,6 +930,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
                 (t - __ldg((const unsigned long long *)&J->ticket_begin));
             launch_photon<kMode>(J, m, k, L.mult, p, r, src_idx);
             if (!kUniform) rc = load_rec(m, p.label);
+            if (kUniform && kLean) {
+              mutr_c = s_lab[2 * p.label].x;
+              n_c = s_lab[2 * p.label + 1].w;
+            }
             pst = 0;
             pst0 = 0;
             alive = true;
@@ -1181,17 +1187,16 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
        * reads the label records from shared memory; a mixed-media launch
        * holds the photon's record in registers and reloads it when the
        * label changes. ---- */
-      const real mutr = kUniform ? s_lab[2 * p.label].x : rc.a.x;
+      const real mutr = kUniform ? mutr_c : rc.a.x;
       const uint64_t x_before = r.x;
       real s = -MCFL_LOGF(r.oc()) * mutr;
-      if (!(mutr != FLT_MAX)) r.x = x_before; /* a scattering-free voxel draws no step length */
       const real zn = p.z + s * p.dz;
       const real xn = p.x + p.dx * s, yn = p.y + p.dy * s;
       const bool inside = MCFL_FABS(xn) < m.hx && MCFL_FABS(yn) < m.hy && zn < m.esp;
       const uint32_t vi = voxel_index(m, xn, yn, zn); /* clamped: always a voxel of the grid */
       const uint32_t g = (uint32_t)m.labels[vi];
       const uint32_t lab = inside ? g : 1u;
-      const real n_old = kUniform ? s_lab[2 * p.label + 1].w : rc.b.w;
+      const real n_old = kUniform ? n_c : rc.b.w;
       const real n_new = kUniform ? s_lab[2 * lab + 1].w : label_n(m, lab);
       const bool clip = zn < MCFL_C(0.0) || zn > m.esp;
       const bool rare = !(mutr != FLT_MAX) || clip || !(s > MCFL_C(0.0)) ||
@@ -1214,7 +1219,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       } else {
         uint32_t new_bulk;
         uint32_t vr = 0xffffffffu;
-        if (!(mutr != FLT_MAX)) { /* scattering-free voxel */
+        if (!(mutr != FLT_MAX)) { /* scattering-free voxel: it draws no step length */
+          r.x = x_before;
           s = MCFL_C(100.0);
           new_bulk = move_to_first_boundary<false>(p, m, s);
         } else if (clip) { /* the step reaches a slab face */
@@ -1253,6 +1259,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           s = MCFL_C(0.0);
         }
         spin_now = s > MCFL_C(0.0);
+        if (kUniform) {
+          mutr_c = s_lab[2 * p.label].x;
+          n_c = s_lab[2 * p.label + 1].w;
+        }
       }
       if constexpr (kPhdWarp) {
         /* Warp-aggregated: the lanes adding to the same voxel are grouped
@@ -1273,6 +1283,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       }
       if (spin_now) {
         const Rec c2 = kUniform ? Rec{s_lab[2 * p.label], s_lab[2 * p.label + 1]} : rc;
+        if (kUniform) {
+          mutr_c = c2.a.x;
+          n_c = c2.b.w;
+        }
         const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
         if (w > 0u) {
           p.weight -= w;

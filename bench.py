@@ -712,7 +712,7 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4, 
            "photons_per_s": served, "express_period": express_period, "express_ratio": express_ratio,
            "mean_jobs_in_flight": mtr["mean_inflight"], "max_jobs_in_flight": mtr["max_inflight"],
            "slices": mtr["slices"], "server_busy_s": mtr["busy_s"], "server_upload_s": mtr["upload_s"],
-           "server_finish_s": mtr["finish_s"], "server_span_s": mtr["span_s"],
+           "server_finish_s": mtr["finish_s"], "server_kernel_s": mtr["kernel_s"], "server_span_s": mtr["span_s"],
            "workload": "Poisson requests at 80 % of the calibrated single-run rate, own media 64^3..256x256x128 "
                        "(labels + fp32 map), 1e5..1e8 photons log-uniform, Gaussian beam or 4x4 cm wide field; "
                        "saturated: 24 such requests queued at once vs run one per launch (upload, run, read back)"}

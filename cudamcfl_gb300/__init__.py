@@ -149,7 +149,8 @@ class ServerMetrics(ctypes.Structure):
                 ("max_ms", ctypes.c_double), ("photons", ctypes.c_ulonglong), ("slices", ctypes.c_ulonglong),
                 ("busy_s", ctypes.c_double), ("span_s", ctypes.c_double), ("mean_inflight", ctypes.c_double),
                 ("max_inflight", ctypes.c_ulonglong), ("hbm_used", ctypes.c_ulonglong),
-                ("hbm_budget", ctypes.c_ulonglong), ("upload_s", ctypes.c_double), ("finish_s", ctypes.c_double)]
+                ("hbm_budget", ctypes.c_ulonglong), ("upload_s", ctypes.c_double), ("finish_s", ctypes.c_double),
+                ("kernel_s", ctypes.c_double)]
 
 
 # ----------------------------------------------------------------- loading

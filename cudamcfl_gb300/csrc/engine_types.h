@@ -156,6 +156,9 @@ typedef struct McflLaunch {
    * first multiple of 16 iterations at least slice_ns after its start
    * (0: no time limit); with max_iters, whichever comes first */
   uint64_t slice_ns;
+  /* a served slice (with saved): also ends once this word is nonzero; the
+   * kernel sets it when a request's last photon finishes */
+  unsigned int *stop_flag;
   unsigned long long *ticket_counter;
   uint64_t ticket_end;                       /* used when ticket_end_dev is NULL */
   const unsigned long long *ticket_end_dev; /* ticket end written by an earlier kernel */

@@ -79,11 +79,12 @@ struct mcfl_server {
   mcfl_ctx *ctx = nullptr;
   size_t budget = 0, used = 0;
   unsigned slots = 64;
-  /* a slice's limits while requests wait: passes per thread (0: none) and
-   * nanoseconds; both grow to 8 times while none waits (slice_mult) */
+  /* a slice's limits: passes per thread (0: none) and nanoseconds; a slice
+   * also ends at once when a request arrives that can be admitted (the
+   * submitting thread raises the stop word) or when a request's last photon
+   * finishes (the kernel raises it) */
   uint32_t slice_iters = 0;
-  uint64_t slice_ns = 2000000;
-  uint32_t slice_mult = 1;
+  uint64_t slice_ns = 32000000;
   uint32_t express_period = 4, express_ratio = 8; /* see mcfl_server_opts */
   std::mutex mu;
   std::condition_variable cv, cv_done;
@@ -96,6 +97,11 @@ struct mcfl_server {
   std::thread worker;
   /* device state */
   DevBuf slot_jobs, order, counter, stats_all;
+  DevBuf stop_word;              /* the running slice's stop flag */
+  cudaStream_t sig = nullptr;    /* the submitting threads' stop signals */
+  cudaEvent_t ev_reset = nullptr; /* the stop word's reset before the running slice */
+  unsigned int *h_one = nullptr; /* pinned 1 */
+  bool in_slice = false;         /* a slice is running (under mu) */
   /* Modes: bit 0 voxel-boundary stepping, bit 1 time of flight.  A launch
    * runs the requests of one mode with that mode's kernel variant; each mode
    * keeps one launch shape and its own photons in flight (parked per
@@ -113,7 +119,8 @@ struct mcfl_server {
   /* metrics */
   std::vector<double> latencies_ms;
   unsigned long long photons_done = 0, slices = 0, max_inflight = 0, inflight_sum = 0;
-  double busy_s = 0, upload_s = 0, finish_s = 0;
+  double busy_s = 0, upload_s = 0, finish_s = 0, kernel_s = 0;
+  cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr; /* around each slice's launch */
   Clock::time_point t_first, t_last;
   bool any = false;
 
@@ -250,7 +257,6 @@ void mcfl_server::loop() {
   cudaStream_t s = ctx->stream;
   for (;;) {
     std::vector<std::shared_ptr<Request>> fresh;
-    bool waiting = false;
     {
       std::unique_lock<std::mutex> lk(mu);
       bool have_active = false;
@@ -261,11 +267,7 @@ void mcfl_server::loop() {
         continue;
       }
       admit_locked(fresh);
-      waiting = !queue.empty();
     }
-    /* Short slices let waiting requests in soon; with nobody waiting the
-     * slices lengthen, which saves the per-slice host round trips. */
-    slice_mult = (waiting || !fresh.empty()) ? 1u : std::min(slice_mult * 2u, 8u);
     const auto t_up0 = Clock::now();
     for (auto &r : fresh) {
       r->t_admit = Clock::now();
@@ -368,8 +370,9 @@ void mcfl_server::loop() {
       L.ticket_counter2 = counter.as<unsigned long long>() + 1;
       L.ticket_end2 = tickets_end2;
     }
-    L.max_iters = (uint32_t)std::min<uint64_t>((uint64_t)slice_iters * slice_mult, 0xffffffffull);
-    L.slice_ns = slice_ns * slice_mult;
+    L.max_iters = slice_iters;
+    L.slice_ns = slice_ns;
+    L.stop_flag = stop_word.as<unsigned int>();
     L.express_period = express_period;
     L.variant = (uint32_t)ctx->mixed_code();
     L.exact_step = (mode & 1u) ? 1u : 0u;
@@ -380,14 +383,28 @@ void mcfl_server::loop() {
     L.saved = parked[mode].as<McflSaved>();
     L.step_cap = ctx->step_cap;
     L.relaunch_min = ctx->relaunch;
+    cudaMemsetAsync(stop_word.p, 0, 4, s);
+    cudaEventRecord(ev_reset, s);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      in_slice = true;
+    }
+    cudaEventRecord(ev_k0, s);
     cudaError_t e = ctx->launch_transport(L, grid_m[mode], block_m[mode]);
+    cudaEventRecord(ev_k1, s);
     cudaMemcpyAsync(h_read, counter.p, 16, cudaMemcpyDeviceToHost, s);
     for (unsigned i = 0; i < n_active; ++i) {
       Request &r = *active[h_stat_slot[i]];
       cudaMemcpyAsync(h_read + 2 + (size_t)i * MCFL_ST_COUNT, r.stats.p, MCFL_ST_COUNT * 8, cudaMemcpyDeviceToHost, s);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      in_slice = false;
+    }
     const auto t1 = Clock::now();
+    float k_ms = 0.f;
+    if (e == cudaSuccess && cudaEventElapsedTime(&k_ms, ev_k0, ev_k1) == cudaSuccess) kernel_s += 1e-3 * k_ms;
     busy_s += std::chrono::duration<double>(t1 - t0).count();
     ++slices;
     inflight_sum += n_active;
@@ -484,6 +501,12 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   if (!e) e = sv->order.reserve(sv->slots * 4);
   if (!e) e = sv->counter.reserve(16); /* the two queues' ticket counters */
   if (!e) e = cudaMemset(sv->counter.p, 0, 8);
+  if (!e) e = sv->stop_word.reserve(4);
+  if (!e) e = cudaMemset(sv->stop_word.p, 0, 4);
+  if (!e) e = cudaStreamCreateWithFlags(&sv->sig, cudaStreamNonBlocking);
+  if (!e) e = cudaEventCreateWithFlags(&sv->ev_reset, cudaEventDisableTiming);
+  if (!e) e = cudaEventCreate(&sv->ev_k0);
+  if (!e) e = cudaEventCreate(&sv->ev_k1);
   for (unsigned mode = 0; mode < mcfl_server::kModes && !e; ++mode) {
     sv->grid_m[mode] = ctx->grid_for(false, &sv->block_m[mode], nullptr, (mode & 2u) != 0, (mode & 1u) != 0);
     const size_t threads = (size_t)sv->grid_m[mode] * sv->block_m[mode];
@@ -493,6 +516,8 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   if (!e) e = cudaHostAlloc((void **)&sv->h_jobs, sv->slots * sizeof(McflJob), cudaHostAllocDefault);
   if (!e) e = cudaHostAlloc((void **)&sv->h_order, sv->slots * 4, cudaHostAllocDefault);
   if (!e) e = cudaHostAlloc((void **)&sv->h_read, (2 + (size_t)sv->slots * MCFL_ST_COUNT) * 8, cudaHostAllocDefault);
+  if (!e) e = cudaHostAlloc((void **)&sv->h_one, 4, cudaHostAllocDefault);
+  if (!e) *sv->h_one = 1u;
   if (e) {
     mcfl_server_destroy(sv);
     return cuda_fail(e, "mcfl_server_create");
@@ -528,6 +553,21 @@ extern "C" int mcfl_server_submit(mcfl_server *sv, const mcfl_medium_desc *mediu
   sv->all[r->id] = r;
   *id = r->id;
   sv->cv.notify_all();
+  /* a running slice ends early when this request can join the next one (a
+   * free slot and room in the budget); the signal is ordered after that
+   * slice's reset of its stop word */
+  if (sv->in_slice && sv->queue.size() == 1 && sv->used + r->footprint <= sv->budget) {
+    unsigned used_slots = 0;
+    for (auto &a : sv->active) used_slots += a ? 1u : 0u;
+    if (used_slots < sv->slots) {
+      int dev_old = -1;
+      cudaGetDevice(&dev_old);
+      if (dev_old != sv->ctx->device) cudaSetDevice(sv->ctx->device);
+      cudaStreamWaitEvent(sv->sig, sv->ev_reset, 0);
+      cudaMemcpyAsync(sv->stop_word.p, sv->h_one, 4, cudaMemcpyHostToDevice, sv->sig);
+      if (dev_old >= 0 && dev_old != sv->ctx->device) cudaSetDevice(dev_old);
+    }
+  }
   return MCFL_OK;
 }
 
@@ -595,6 +635,7 @@ extern "C" int mcfl_server_metrics(mcfl_server *sv, mcfl_server_metrics_t *m) {
   m->hbm_budget = sv->budget;
   m->upload_s = sv->upload_s;
   m->finish_s = sv->finish_s;
+  m->kernel_s = sv->kernel_s;
   return MCFL_OK;
 }
 
@@ -611,5 +652,10 @@ extern "C" void mcfl_server_destroy(mcfl_server *sv) {
   if (sv->h_jobs) cudaFreeHost(sv->h_jobs);
   if (sv->h_order) cudaFreeHost(sv->h_order);
   if (sv->h_read) cudaFreeHost(sv->h_read);
+  if (sv->h_one) cudaFreeHost(sv->h_one);
+  if (sv->ev_reset) cudaEventDestroy(sv->ev_reset);
+  if (sv->ev_k0) cudaEventDestroy(sv->ev_k0);
+  if (sv->ev_k1) cudaEventDestroy(sv->ev_k1);
+  if (sv->sig) cudaStreamDestroy(sv->sig);
   delete sv;
 }

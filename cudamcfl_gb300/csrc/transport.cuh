@@ -883,10 +883,17 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   for (uint32_t it = 0;; ++it) {
     /* single-medium launches always run to the end of their tickets */
     if (!kUniform && L.max_iters && it >= L.max_iters) break;
-    /* time-limited slice: the warps stop together, whatever their pace
-     * (a warp-uniform test: lane 0's clock) */
-    if (!kUniform && L.slice_ns && (it & 15u) == 0u && __shfl_sync(kFull, global_ns(), 0) - t_begin >= L.slice_ns)
-      break;
+    /* a served slice ends when its time is up or its stop flag is raised
+     * (a request arrived, or one finished); the warps stop together,
+     * whatever their pace (a warp-uniform test: lane 0 reads the clock and
+     * the flag every 16 iterations) */
+    if (!kUniform && (L.slice_ns || L.stop_flag) && (it & 63u) == 0u) {
+      int stop = 0;
+      if (lane == 0)
+        stop = (L.slice_ns && global_ns() - t_begin >= L.slice_ns) ||
+               (L.stop_flag && *(volatile const unsigned int *)L.stop_flag != 0u);
+      if (__shfl_sync(kFull, stop, 0)) break;
+    }
     /* one vote per pass while every lane carries a photon; live: the lanes
      * that run this pass (lanes without a photon skip it), the member mask
      * of any warp-wide operation inside the pass */
@@ -1395,8 +1402,18 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         alive = false;
       }
       if (!alive) {
-        ++done;
         steps += pst - pst0;
+        if (!kUniform && L.stop_flag) {
+          /* a served slice counts each finished photon at once, and the
+           * request's last one raises the stop flag */
+          const unsigned long long before =
+              atomicAdd((unsigned long long *)__ldg((const unsigned long long *)&J->stats) + MCFL_ST_DONE, 1ull);
+          if (before + 1ull == __ldg((const unsigned long long *)&J->photon_base) +
+                                   __ldg((const unsigned long long *)&J->photons))
+            *(volatile unsigned int *)L.stop_flag = 1u;
+        } else {
+          ++done;
+        }
       }
     }
   }

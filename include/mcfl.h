@@ -326,8 +326,8 @@ const char *mcfl_last_error(void);
  * also resets "variant_fl"), "variant_fl" (the emission phase's own
  * occupancy variant in mcfl_run; -1: as "variant"),
  * "mixed_variant" (occupancy variant of the mixed-media kernel that batches
- * over several media and the server run: 0 = 256 x 3, 1 = 256 x 4,
- * 2 = 128 x 7, the default),
+ * over several media and the server run: 0 = 256 x 3, 1 = 256 x 4, the
+ * default, 2 = 128 x 7),
  * "blocks_per_sm" (0 = occupancy maximum), "step_cap" (passes per photon),
  * "l2_window" (1: persisting L2 access window on the labels and tallies),
  * "phd_agg" (the photon-hitting-density tally of the single-medium kernel:
@@ -437,9 +437,10 @@ typedef struct mcfl_server_opts {
   unsigned long long hbm_budget_bytes; /* admission budget (0: half the free HBM) */
   unsigned int max_jobs;               /* concurrent jobs (0: 64) */
   /* A slice (one launch of the transport kernel over the admitted
-   * requests) ends after slice_us microseconds (0: 2000), or after
-   * slice_passes transport passes per thread (0: no such cap), whichever
-   * comes first; both double, up to 8 times, while no request waits. */
+   * requests) ends when a request arrives that can be admitted, when a
+   * request's last photon finishes, after slice_us microseconds (0: 32000),
+   * or after slice_passes transport passes per thread (0: no such cap),
+   * whichever comes first. */
   unsigned int slice_passes;
   /* Scheduling of a slice's photon tickets: the oldest admitted request (the
    * head) has a queue of its own; the requests whose remaining photons are
@@ -464,6 +465,7 @@ typedef struct mcfl_server_metrics_t {
   unsigned long long hbm_used, hbm_budget;
   double upload_s;                  /* server-thread wall time uploading admitted requests' media */
   double finish_s;                  /* server-thread wall time copying out and releasing finished requests */
+  double kernel_s;                  /* GPU time of the slices' transport launches (CUDA events) */
 } mcfl_server_metrics_t;
 
 /* Starts the server thread; it owns ctx (and its stream) until

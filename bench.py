@@ -341,8 +341,11 @@ def main():
     def one_step():
         return lib.mcfl_run(ctx.handle, med.handle, mc.ctypes.byref(rd), mc.ctypes.byref(stats_out))
 
-    # launch shape: time every kernel variant on a 4e6-photon sample, keep the fastest
-    variant, tune_rate = ctx.autotune(med, rd, sample_photons=4_000_000)
+    # launch shape: time every kernel variant on a 1.6e7-photon sample, keep
+    # the fastest (on 4e6-photon samples the excitation launch's choice did
+    # not carry over to the full budget: more of a small sample is launch
+    # tail)
+    variant, tune_rate = ctx.autotune(med, rd, sample_photons=16_000_000)
 
     for _ in range(args.warmup):
         mc.check(one_step())

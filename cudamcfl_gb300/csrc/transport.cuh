@@ -1295,12 +1295,14 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           n_c = c2.b.w;
         }
         const uint32_t w = MCFL_R2U_RU(c2.a.y * MCFL_U2R_RN(p.weight));
+        /* a zero drop kills the photon: its weight stays for the end branch
+         * to count, flagged in the pass count's top bit (which also sends
+         * the photon there: pst >= step_cap) */
         if (w > 0u) {
           p.weight -= w;
           absorbed += w;
         } else {
-          ev_add(MCFL_ST_W0_LOSS, p.weight);
-          p.weight = 0u;
+          pst |= 0x80000000u;
         }
         spin(p, c2, r);
       }
@@ -1385,6 +1387,11 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     /* PhotonSurvive, the pass cap and the photon's end: one branch for the
      * lean pass */
     if (!kLean || p.weight <= kWeightRoulette || pst >= L.step_cap) {
+      if (kLean && (pst & 0x80000000u)) { /* the pass's zero weight drop */
+        pst &= 0x7fffffffu;
+        ev_add(MCFL_ST_W0_LOSS, p.weight);
+        p.weight = 0u;
+      }
       if (p.weight <= kWeightRoulette) {
         if (p.weight == 0u) {
           alive = false;

@@ -1201,7 +1201,10 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
       const real xn = p.x + p.dx * s, yn = p.y + p.dy * s;
       const bool inside = MCFL_FABS(xn) < m.hx && MCFL_FABS(yn) < m.hy && zn < m.esp;
       const uint32_t vi = voxel_index(m, xn, yn, zn); /* clamped: always a voxel of the grid */
-      const uint32_t g = (uint32_t)m.labels[vi];
+      /* the end point's label, kept in L1 ahead of other lines (evict-last
+       * hint): the gather whose latency the excitation launch waits on */
+      uint32_t g;
+      asm("ld.global.nc.L1::evict_last.u8 %0, [%1];" : "=r"(g) : "l"(m.labels + vi));
       const uint32_t lab = inside ? g : 1u;
       const real n_old = kUniform ? n_c : rc.b.w;
       const real n_new = kUniform ? s_lab[2 * lab + 1].w : label_n(m, lab);

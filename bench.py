@@ -744,12 +744,14 @@ def serve_stream(mc, ctx_main, device, duration_s: float = 12.0, seed: int = 4, 
 
     if saturated:
         # saturation: the same kind of requests all queued at once (served),
-        # and one request per launch after another (plain), same requests
+        # and one request per launch after another (plain), same requests;
+        # a generator of their own, so that every run draws the same 24
+        brng = np.random.default_rng(seed + 1000)
         burst = []
         for i in range(24):
-            photons = int(math.exp(rng.uniform(math.log(1e5), math.log(1e8))))
-            lab, bulks, vox, fmap = pool[int(rng.integers(0, len(pool)))]
-            wide = rng.uniform() < 0.5
+            photons = int(math.exp(brng.uniform(math.log(1e5), math.log(1e8))))
+            lab, bulks, vox, fmap = pool[int(brng.integers(0, len(pool)))]
+            wide = brng.uniform() < 0.5
             burst.append((lab, bulks, vox, fmap, mcm.run_desc(photons, det=det, seed_exc=90_000 + i, width=4.0,
                                                              height=4.0, kind=mcm.SOURCE_WIDEFIELD if wide else
                                                              mcm.SOURCE_GAUSS_BEAM)))

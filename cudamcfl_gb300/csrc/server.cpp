@@ -555,7 +555,9 @@ extern "C" int mcfl_server_submit(mcfl_server *sv, const mcfl_medium_desc *mediu
   sv->cv.notify_all();
   /* a running slice ends early when this request can join the next one (a
    * free slot and room in the budget); the signal is ordered after that
-   * slice's reset of its stop word */
+   * slice's reset of its stop word.  It only shortens a slice: if it is lost
+   * (a failed call) or lands after the slice ended (the next one then stops
+   * at once), results are unchanged */
   if (sv->in_slice && sv->queue.size() == 1 && sv->used + r->footprint <= sv->budget) {
     unsigned used_slots = 0;
     for (auto &a : sv->active) used_slots += a ? 1u : 0u;

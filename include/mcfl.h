@@ -475,7 +475,11 @@ int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, mcfl_server 
 /* Queues one request: an excitation run (photons_per_voxel = 0, fluence
  * optional) on its own medium.  Thread-safe.  The medium's host arrays must
  * stay valid until mcfl_server_wait reports the request finished.  Requests
- * larger than the HBM budget finish with MCFL_E_RANGE. */
+ * larger than the HBM budget finish with MCFL_E_RANGE.  When a slice is
+ * running and the request can join the next one, the call ends that slice
+ * early with a 4-byte asynchronous copy on a stream of the server's own
+ * (made current on the server's device for the call and the caller's
+ * device restored). */
 int mcfl_server_submit(mcfl_server *server, const mcfl_medium_desc *medium, const mcfl_run_desc *run,
                        unsigned long long *id);
 

@@ -488,7 +488,7 @@ extern "C" int mcfl_server_create(mcfl_ctx *ctx, const mcfl_server_opts *opts, m
   sv->budget = opts && opts->hbm_budget_bytes ? (size_t)opts->hbm_budget_bytes : free_b / 2;
   sv->slots = opts && opts->max_jobs ? (unsigned)opts->max_jobs : 64u;
   sv->slice_iters = opts ? (uint32_t)opts->slice_passes : 0u;
-  if (opts && opts->slice_us) sv->slice_ns = (uint64_t)opts->slice_us * 1000u;
+  if (opts && opts->slice_us) sv->slice_ns = std::min<uint64_t>((uint64_t)opts->slice_us * 1000u, 4000000000ull);
   if (opts && opts->express_period) sv->express_period = opts->express_period;
   if (opts && opts->express_ratio) sv->express_ratio = opts->express_ratio;
   if (sv->slots > 4096) {

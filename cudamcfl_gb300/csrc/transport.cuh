@@ -320,7 +320,7 @@ __device__ __forceinline__ void region_of(const Med &m, int x, int y, int z, uin
   }
 }
 
-template <int kMode>
+template <int kMode, bool kVoxelSrc = true>
 __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, uint64_t k, const uint32_t *mult,
                                               Photon &p, Rng &r, uint32_t &src_idx) {
   const uint64_t stream = __ldg((const unsigned long long *)&J->rng_offset) + k;
@@ -331,7 +331,7 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
    * run starts at its photon offset), the index within the voxel's run for
    * an emitting voxel */
   uint64_t k_in_run = stream;
-  if (kind == MCFL_SRC_VOXELS) {
+  if (kVoxelSrc && kind == MCFL_SRC_VOXELS) {
     const uint32_t per = __ldg(&J->per_voxel);
     src_idx = (uint32_t)(k / per);
     k_in_run = k - (uint64_t)src_idx * per;
@@ -383,7 +383,7 @@ __device__ __forceinline__ void launch_photon(const McflJob *J, const Med &m, ui
   p.label = kMode == 1 ? __ldg(&J->start_layer) : start_label(m, p);
   p.tof = 0;
   if (kMode == 2) {
-    if (kind == MCFL_SRC_VOXELS) {
+    if (kVoxelSrc && kind == MCFL_SRC_VOXELS) {
       const uint32_t v = __ldg(&J->src_vox[src_idx]);
       p.ix = (int)(v % m.nx);
       p.iy = (int)((v / m.nx) % m.ny);
@@ -845,8 +845,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
   /* a slice of a served run: photons in flight are parked at its end and
    * resumed by the next slice */
   const bool sliced = !kUniform && (L.max_iters || L.slice_ns) && L.saved;
-  uint64_t t_begin = 0;
-  if (!kUniform && L.slice_ns) t_begin = __shfl_sync(kFull, global_ns(), 0);
+  uint32_t t_begin = 0; /* the low word of the clock: slices last under 2^32 ns */
+  if (!kUniform && L.slice_ns) t_begin = __shfl_sync(kFull, (uint32_t)global_ns(), 0);
   if (sliced) {
     const McflSaved sv = L.saved[gtid];
     if (sv.alive) {
@@ -890,7 +890,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     if (!kUniform && (L.slice_ns || L.stop_flag) && (it & 63u) == 0u) {
       int stop = 0;
       if (lane == 0)
-        stop = (L.slice_ns && global_ns() - t_begin >= L.slice_ns) ||
+        stop = (L.slice_ns && (uint32_t)global_ns() - t_begin >= (uint32_t)L.slice_ns) ||
                (L.stop_flag && *(volatile const unsigned int *)L.stop_flag != 0u);
       if (__shfl_sync(kFull, stop, 0)) break;
     }
@@ -935,7 +935,9 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
             }
             k = __ldg((const unsigned long long *)&J->photon_base) +
                 (t - __ldg((const unsigned long long *)&J->ticket_begin));
-            launch_photon<kMode>(J, m, k, L.mult, p, r, src_idx);
+            /* a mixed-media launch's jobs are beams (emission runs over
+             * one medium) */
+            launch_photon<kMode, kUniform>(J, m, k, L.mult, p, r, src_idx);
             if (!kUniform) rc = load_rec(m, p.label);
             if (kUniform && kLean) {
               mutr_c = s_lab[2 * p.label].x;
@@ -1084,7 +1086,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
               p.iz = niz;
               if (next == 0u || next == m.last) {
                 const bool top = next == 0u;
-                tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+                tally_exit(J, p.x, p.y, p.weight, top, kUniform ? src_idx : 0u);
                 if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
                 ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
                 p.weight = 0u;
@@ -1162,7 +1164,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.label = (uint32_t)new_layer;
           if (new_layer == 0 || new_layer > (int)nl) {
             const bool top = new_layer == 0;
-            tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+            tally_exit(J, p.x, p.y, p.weight, top, kUniform ? src_idx : 0u);
             if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
             ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
             p.weight = 0u;
@@ -1263,7 +1265,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
         phd_w = p.weight; /* before an exit takes it */
         if (p.label == 0u || p.label == m.last) {
           const bool top = p.label == 0u;
-          tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+          tally_exit(J, p.x, p.y, p.weight, top, kUniform ? src_idx : 0u);
           ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
           p.weight = 0u;
           s = MCFL_C(0.0);
@@ -1368,7 +1370,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
     }
     if (p.label == 0u || p.label == m.last) {
       const bool top = p.label == 0u;
-      tally_exit(J, p.x, p.y, p.weight, top, src_idx);
+      tally_exit(J, p.x, p.y, p.weight, top, kUniform ? src_idx : 0u);
       if (kTime) tally_time(J, p.x, p.y, p.weight, p.tof, top);
       ev_add(top ? MCFL_ST_EXIT_TOP : MCFL_ST_EXIT_BOTTOM, p.weight);
       p.weight = 0u;

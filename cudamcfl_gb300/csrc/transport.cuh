@@ -738,7 +738,7 @@ __device__ __noinline__ void tally_time(const McflJob *J, real px, real py, uint
 /* kPhdWarp (single medium, the SIMT-arranged pass): the hitting-density adds
  * of a warp's lanes aggregated per voxel, one add per distinct voxel. */
 template <bool kUniform, bool kTime, int kMode, int kThreads, int kMinBlocks, bool kPhdAgg = false,
-          bool kGeneral = false, bool kPhdWarp = false>
+          bool kGeneral = false, bool kPhdWarp = false, bool kNoPhd = false>
 __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERNEL_NAME(McflLaunch L) {
   constexpr bool kLayered = kMode == 1;
   constexpr bool kExactStep = kMode == 2;
@@ -1226,7 +1226,7 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           if (lab != p.label) rc = load_rec(m, lab);
         }
         p.label = lab;
-        phd_on = m.fhd && inside;
+        phd_on = !kNoPhd && m.fhd && inside;
         spin_now = true;
       } else {
         uint32_t new_bulk;
@@ -1260,7 +1260,8 @@ __global__ void __launch_bounds__(kThreads, MCFL_F64 ? 1 : kMinBlocks) MCFL_KERN
           p.label = new_bulk;
           if constexpr (!kUniform) rc = load_rec(m, new_bulk);
         }
-        phd_on = m.fhd && (vr != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp));
+        phd_on = !kNoPhd && m.fhd &&
+                 (vr != 0xffffffffu || (MCFL_FABS(p.x) < m.hx && MCFL_FABS(p.y) < m.hy && p.z < m.esp));
         if (phd_on) phd_idx = vr != 0xffffffffu ? vr : voxel_index(m, p.x, p.y, p.z);
         phd_w = p.weight; /* before an exit takes it */
         if (p.label == 0u || p.label == m.last) {
@@ -1477,7 +1478,9 @@ static size_t smem_bytes(int threads, bool uniform) {
  * 1 = 256 x 5, 2 = 128 x 9, chosen by the autotuner, and 7, 8, 9 the same
  * with the photon-hitting-density sums held in a register, 11, 12, 13 the
  * same with the pass in its per-test branching form, 14, 15, 16 the same
- * with the hitting-density adds aggregated per warp; 3 = 256 x 3 carrying
+ * with the hitting-density adds aggregated per warp, 17, 18, 19 the same
+ * as 0, 1, 2 with no hitting-density code (the launcher runs them for
+ * launches that tally none: emission, excitation without fluence); 3 = 256 x 3 carrying
  * the time of flight; layered medium 4 = 256 x 4, 5 = 256 x 3 with the time
  * of flight; voxel-boundary stepping 6 = 256 x 4, 10 = 256 x 3 with the time
  * of flight.  Mixed media: -1 = 256 x 3, -3 = 256 x 4, -4 = 128 x 7,
@@ -1521,6 +1524,9 @@ static TransportKernel kernel_of(int variant, int *threads) {
   case 14: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, false, false, true>;
   case 15: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, false, false, true>;
   case 16: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, false, false, true>;
+  case 17: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 4, false, false, false, true>;
+  case 18: *threads = 256; return MCFL_KERNEL_NAME<true, false, 0, 256, 5, false, false, false, true>;
+  case 19: *threads = 128; return MCFL_KERNEL_NAME<true, false, 0, 128, 9, false, false, false, true>;
   default: *threads = 0; return nullptr;
   }
 }
@@ -1543,7 +1549,10 @@ extern "C" cudaError_t MCFL_LAUNCHER(const McflLaunch *L, int grid, int block, c
                 : L->time_on        ? -2
                                     : mixed_variant_code(L->variant);
   int t = 0;
-  const TransportKernel fn = kernel_of(v, &t);
+  /* variants 0..2 without a hitting-density tally: their instantiations
+   * that compile none (17..19) */
+  const int vk = (v >= 0 && v <= 2 && !L->med.fhd) ? v + 17 : v;
+  const TransportKernel fn = kernel_of(vk, &t);
   if (!fn || block > t) return cudaErrorInvalidValue;
   cudaLaunchConfig_t cfg;
   memset(&cfg, 0, sizeof(cfg));
@@ -1596,6 +1605,12 @@ extern "C" cudaError_t MCFL_ATTR_FN(int variant, int *block, int *blocks_per_sm,
     const int pct = (int)std::min<size_t>(100, (need * 100 + (size_t)max_sm - 1) / (size_t)max_sm + 1);
     e = cudaFuncSetAttribute((const void *)fn, cudaFuncAttributePreferredSharedMemoryCarveout, pct);
     if (e != cudaSuccess) return e;
+    if (variant >= 0 && variant <= 2) { /* the same split for its instantiation without the tally */
+      int t2 = 0;
+      e = cudaFuncSetAttribute((const void *)kernel_of(variant + 17, &t2), cudaFuncAttributePreferredSharedMemoryCarveout,
+                               pct);
+      if (e != cudaSuccess) return e;
+    }
   }
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void *)fn, *block, smem);
 }
